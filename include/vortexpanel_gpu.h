@@ -1,0 +1,118 @@
+/* C ABI of the GB300-native (sm_103a) Galerkin hot path of VortexPanel.jl: libvortexpanel_gpu.so.
+ *
+ * Plain pointers and sizes only. Host arrays are caller-owned and read or written during the call; the assembled
+ * system and its factorization stay resident on the GPU behind opaque handles until freed. Indices are 0-based,
+ * matrices row-major unless stated. Every entry point returns a vp_status; vp_last_error() gives the message of the
+ * last failure on a context. One CUDA stream per context; calls are synchronous at the boundary. A context is not
+ * safe for concurrent use from several threads; separate contexts are independent.
+ *
+ * Reference interfaces replaced (paths within the VortexPanel.jl project):
+ *   vp_assemble        <- Assembly.assemble(g, dm, els, σ, V∞; opts, wake)       src/assembly/assemble.jl:377-447
+ *   vp_factorize       <- Assembly.factorize_galerkin(dm, A; W)                    src/assembly/solve.jl:81-87
+ *   vp_solve           <- Assembly.solve_galerkin(F::GalerkinFactorization, b)     src/assembly/solve.jl:95-99
+ *   vp_solve_system    <- Assembly.solve_galerkin(dm, A, b; W)                     src/assembly/solve.jl:51-59
+ */
+#ifndef VORTEXPANEL_GPU_H
+#define VORTEXPANEL_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    VP_OK = 0,
+    VP_ERR_ARG = 1,        /* invalid argument or option (ArgumentError / DimensionMismatch in the reference) */
+    VP_ERR_DEGENERATE = 2, /* degenerate triangle (SourceTriangle's ArgumentError, source_triangle.jl:21) */
+    VP_ERR_SINGULAR = 3,   /* zero pivot in the LU (LAPACK SingularException) */
+    VP_ERR_NOCONV = 4,     /* iterative refinement did not converge */
+    VP_ERR_TIMEOUT = 5,    /* a bounded device-side wait gave up */
+    VP_ERR_CUDA = 6,       /* CUDA runtime or cuBLAS failure */
+    VP_ERR_NOMEM = 7       /* device allocation failed */
+} vp_status;
+
+typedef enum {
+    VP_FP64 = 0,  /* every integral, the LU and the solve in FP64 */
+    VP_MIXED = 1  /* FP32 far/near tiers, FP64 touching tiers; FP32-class LU refined in FP64 */
+} vp_precision;
+
+typedef struct vp_ctx vp_ctx;
+typedef struct vp_system vp_system; /* the assembled A (nslot x (nslot + nwake)) and b, on the GPU */
+typedef struct vp_factor vp_factor; /* the LU of the bordered system, on the GPU */
+
+/* AssemblyOptions (src/assembly/assemble.jl:26-41); test: 0 hat, 1 onering, 2 dual */
+typedef struct {
+    int test;
+    double far_ratio;
+    int far_points;
+    int near_points;
+    double near_ratio;
+    int near_depth;
+    int touch_levels;
+    double touch_ratio;
+    int touch_order;
+    double corner_angle;
+    double contact_rel;
+    double kernel_far;
+    int precision; /* vp_precision */
+} vp_assembly_options;
+
+/* The reference's stats: pairs and quadrature points per tier (self, edge, vertex, contact, near, far) */
+typedef struct {
+    long long pairs[6];
+    long long points[6];
+    double time_ms;
+} vp_assembly_stats;
+
+/* Fill the reference's default AssemblyOptions (FP64). */
+void vp_default_options(vp_assembly_options* opts);
+
+/* A context on CUDA device `device`: its stream, cuBLAS handle and workspaces. */
+int vp_ctx_create(int device, vp_ctx** out);
+void vp_ctx_destroy(vp_ctx* ctx);
+const char* vp_last_error(const vp_ctx* ctx);
+
+/* assemble (src/assembly/assemble.jl:377-447).
+ *   x (nnode x 3), tris (ntri x 3), corner_slot (ntri x 3), touch_pairs (ntouch x 2, triangle pairs that get the
+ *   deeper near rule), sigma (ntri), vinf (3).
+ *   Wake (may be absent: nwnode = 0): wx (nwnode x 3), wtris (nwtri x 3, wake node indices), fil (nfil x 2).
+ * On success *out holds A (nslot x (nslot + nwnode)) and b (nslot) on the GPU; stats may be NULL. */
+int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,
+                const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
+                const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
+                const int* fil, vp_system** out, vp_assembly_stats* stats);
+
+/* Rows and columns of the assembled A. */
+int vp_system_shape(const vp_system* sys, int* nrows, int* ncols);
+/* Copy A (row-major, nrows x ncols) and/or b (nrows) to the host; either pointer may be NULL. */
+int vp_system_download(vp_ctx* ctx, const vp_system* sys, double* A, double* b);
+void vp_system_free(vp_system* sys);
+
+/* factorize_galerkin (src/assembly/solve.jl:81-87): the bordered system (solve.jl:15-38) of the reduction
+ * C' A [C; W] (src/dofmap/system.jl:141-145), one border row per body, factored by a blocked LU with partial
+ * pivoting on the GPU (precision: vp_precision).
+ *   C: CSR (nslot x nq): C_rowptr (nslot + 1), C_col, C_val.  W: CSR (nwake x nq) of the wake rows, or nwake = 0.
+ *   nbody bodies; q_body (nq, 1-based body of every unknown, 0 for none); slot_area, slot_body (nslot, 1-based).
+ * *cond receives the 1-norm condition estimate of the bordered matrix (may be NULL). */
+int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, int nq, const int* C_rowptr, const int* C_col,
+                 const double* C_val, int nwake, const int* W_rowptr, const int* W_col, const double* W_val,
+                 int nbody, const int* q_body, const double* slot_area, const int* slot_body, vp_factor** out,
+                 double* cond);
+
+/* solve_galerkin(F, b) (src/assembly/solve.jl:95-99) for nrhs right hand sides over the slots:
+ *   b (nslot x nrhs, column-major), q (nq x nrhs, column-major), lambda (nbody x nrhs, column-major; may be NULL).
+ * With VP_MIXED factors the solution is refined to FP64 accuracy with FP64 residuals of the bordered matrix. */
+int vp_solve(vp_ctx* ctx, const vp_factor* F, int nrhs, const double* b, double* q, double* lambda);
+
+/* solve_galerkin(dm, A, b; W) (src/assembly/solve.jl:51-59) for the system's own b: q (nq), lambda (nbody),
+ * residual = |M x - rhs| / |rhs| of the bordered system (any output may be NULL). */
+int vp_solve_system(vp_ctx* ctx, const vp_factor* F, const vp_system* sys, double* q, double* lambda,
+                    double* residual);
+
+/* Condition estimate and size of a factorization. */
+int vp_factor_info(const vp_factor* F, int* n, double* cond);
+void vp_factor_free(vp_factor* F);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VORTEXPANEL_GPU_H */

@@ -1,0 +1,116 @@
+// C-ABI entry points of libvortexpanel_gpu: contexts, errors, system handles (include/vortexpanel_gpu.h).
+#include <cstring>
+
+#include "vp_internal.h"
+
+int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
+                     const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
+                     const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
+                     const int* fil, vp_system** out, vp_assembly_stats* stats);
+
+int vp_fail(vp_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+extern "C" {
+
+void vp_default_options(vp_assembly_options* o) {
+    if (!o) return;
+    o->test = 0;
+    o->far_ratio = 3.0;
+    o->far_points = 3;
+    o->near_points = 7;
+    o->near_ratio = 1.5;
+    o->near_depth = 3;
+    o->touch_levels = 6;
+    o->touch_ratio = 0.15;
+    o->touch_order = 3;
+    o->corner_angle = 75.0;
+    o->contact_rel = 0.1;
+    o->kernel_far = 10.0;
+    o->precision = VP_FP64;
+}
+
+int vp_ctx_create(int device, vp_ctx** out) {
+    if (!out) return VP_ERR_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return VP_ERR_CUDA;
+    if (device < 0 || device >= ndev) return VP_ERR_ARG;
+    vp_ctx* c = new vp_ctx();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess) {
+        delete c;
+        return VP_ERR_CUDA;
+    }
+    cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return VP_ERR_CUDA;
+    }
+    if (cublasCreate(&c->blas) != CUBLAS_STATUS_SUCCESS) {
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return VP_ERR_CUDA;
+    }
+    cublasSetStream(c->blas, c->stream);
+    cublasSetMathMode(c->blas, CUBLAS_PEDANTIC_MATH);
+    if (cudaMalloc(&c->d_flag, 64 * sizeof(int)) != cudaSuccess) {
+        cublasDestroy(c->blas);
+        cudaStreamDestroy(c->stream);
+        delete c;
+        return VP_ERR_NOMEM;
+    }
+    cudaMemset(c->d_flag, 0, 64 * sizeof(int));
+    *out = c;
+    return VP_OK;
+}
+
+void vp_ctx_destroy(vp_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->d_flag) cudaFree(ctx->d_flag);
+    if (ctx->blas) cublasDestroy(ctx->blas);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char* vp_last_error(const vp_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,
+                const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
+                const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
+                const int* fil, vp_system** out, vp_assembly_stats* stats) {
+    if (!ctx) return VP_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    return vp_assemble_impl(ctx, opts, nnode, x, ntri, tris, corner_slot, nslot, ntouch, touch_pairs, sigma, vinf,
+                            nwnode, wx, nwtri, wtris, nfil, fil, out, stats);
+}
+
+int vp_system_shape(const vp_system* sys, int* nrows, int* ncols) {
+    if (!sys) return VP_ERR_ARG;
+    if (nrows) *nrows = sys->nslot;
+    if (ncols) *ncols = sys->ncols;
+    return VP_OK;
+}
+
+int vp_system_download(vp_ctx* ctx, const vp_system* sys, double* A, double* b) {
+    if (!ctx || !sys) return vp_fail(ctx, VP_ERR_ARG, "null argument");
+    if (A)
+        VP_CUDA(ctx, cudaMemcpyAsync(A, sys->A, sizeof(double) * size_t(sys->nslot) * sys->ncols, cudaMemcpyDeviceToHost,
+                                     ctx->stream));
+    if (b) VP_CUDA(ctx, cudaMemcpyAsync(b, sys->b, sizeof(double) * sys->nslot, cudaMemcpyDeviceToHost, ctx->stream));
+    VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return VP_OK;
+}
+
+void vp_system_free(vp_system* sys) {
+    if (!sys) return;
+    if (sys->A) cudaFree(sys->A);
+    if (sys->b) cudaFree(sys->b);
+    delete sys;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// Internal types of libvortexpanel_gpu: the context, the resident system and factorization, error handling.
+#pragma once
+#include <cublas_v2.h>
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/vortexpanel_gpu.h"
+
+struct vp_ctx {
+    int device = 0;
+    int nsm = 0;
+    cudaStream_t stream = nullptr;
+    cublasHandle_t blas = nullptr;
+    std::string err;
+    int* d_flag = nullptr;  // device error word of bounded waits and checks
+};
+
+// Element data of one triangle in FP64 (the FlatTriangle / SourceTriangle fields the kernels read).
+struct TriGeo {
+    double x[9];    // corners
+    double n[3];    // unit normal
+    double c[3];    // centroid
+    double area, diam, reach;
+    double gam[9];  // vortex sheet of a unit nodal value at each corner, gamma_b = -e_b / 2A
+    double nu[9];   // in-plane outward unit normals of the edges (edge a from corner a to a+1)
+    double len[3];  // edge lengths
+    double sigma;   // source strength (0 for wake sheets)
+    int node[3];    // corner nodes (for shared-corner tests)
+    int slot[3];    // corner slots (body) or wake-node columns
+};
+
+struct vp_system {
+    int nslot = 0, ncols = 0, nwnode = 0;
+    double* A = nullptr;  // nslot x ncols, row-major
+    double* b = nullptr;  // nslot
+};
+
+struct vp_factor {
+    int n = 0, nq = 0, nb = 0, nslot = 0, ncols = 0, precision = 0;
+    double cond = 0;
+    double* M = nullptr;     // bordered matrix, FP64, column-major n x n (kept for FP64 residuals)
+    double* LU64 = nullptr;  // FP64 factors (column-major n x n) for VP_FP64
+    float* LU32 = nullptr;   // FP32 factors (column-major n x n) for VP_MIXED
+    int* ipiv = nullptr;     // device pivots (row swapped with at each step), n
+    std::vector<int> h_ipiv;
+    int* perm = nullptr;     // device permutation: row of M in position i of the factors
+    double norm1 = 0;        // 1-norm of M
+    double* se = nullptr;    // border column scales (device, nb)
+    std::vector<double> h_se;
+    // C' as CSR over unknowns (nq x nslot) for the right hand side, on the device
+    int *Ct_ptr = nullptr, *Ct_col = nullptr;
+    double* Ct_val = nullptr;
+};
+
+int vp_fail(vp_ctx* ctx, int code, const std::string& msg);
+
+#define VP_CUDA(ctx, call)                                                                            \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return vp_fail((ctx), VP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));   \
+    } while (0)
+
+#define VP_BLAS(ctx, call)                                                                            \
+    do {                                                                                              \
+        cublasStatus_t s_ = (call);                                                                   \
+        if (s_ != CUBLAS_STATUS_SUCCESS)                                                              \
+            return vp_fail((ctx), VP_ERR_CUDA, std::string(#call) + ": cublas status " + std::to_string(int(s_))); \
+    } while (0)
+
+template <class T>
+int vp_alloc(vp_ctx* ctx, T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return vp_fail(ctx, VP_ERR_NOMEM, std::string("cudaMalloc of ") + std::to_string(n * sizeof(T)) + " bytes: " +
+                                              cudaGetErrorString(e));
+    }
+    return VP_OK;
+}
+
+template <class T>
+int vp_upload(vp_ctx* ctx, T** p, const T* h, size_t n) {
+    int r = vp_alloc(ctx, p, n);
+    if (r) return r;
+    if (n) VP_CUDA(ctx, cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    return VP_OK;
+}
+
+// linear algebra (vp_linalg.cu)
+int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F);

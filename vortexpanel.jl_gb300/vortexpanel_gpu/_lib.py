@@ -1,0 +1,125 @@
+"""ctypes binding of libvortexpanel_gpu.so (include/vortexpanel_gpu.h). There is no CPU fallback: if the library
+cannot be loaded or no CUDA device is present, every call raises."""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+from . import _build
+
+D = ctypes.POINTER(ctypes.c_double)
+I = ctypes.POINTER(ctypes.c_int)
+F32 = ctypes.POINTER(ctypes.c_float)
+
+VP_OK, VP_ERR_ARG, VP_ERR_DEGENERATE, VP_ERR_SINGULAR, VP_ERR_NOCONV, VP_ERR_TIMEOUT, VP_ERR_CUDA, VP_ERR_NOMEM = range(8)
+VP_FP64, VP_MIXED = 0, 1
+
+
+class vp_assembly_options(ctypes.Structure):
+    _fields_ = [("test", ctypes.c_int), ("far_ratio", ctypes.c_double), ("far_points", ctypes.c_int),
+                ("near_points", ctypes.c_int), ("near_ratio", ctypes.c_double), ("near_depth", ctypes.c_int),
+                ("touch_levels", ctypes.c_int), ("touch_ratio", ctypes.c_double), ("touch_order", ctypes.c_int),
+                ("corner_angle", ctypes.c_double), ("contact_rel", ctypes.c_double), ("kernel_far", ctypes.c_double),
+                ("precision", ctypes.c_int)]
+
+
+class vp_assembly_stats(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_longlong * 6), ("points", ctypes.c_longlong * 6), ("time_ms", ctypes.c_double)]
+
+
+# (name, restype, argtypes) of every entry point declared in include/vortexpanel_gpu.h
+SIGNATURES = [
+    ("vp_default_options", None, [ctypes.POINTER(vp_assembly_options)]),
+    ("vp_ctx_create", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    ("vp_ctx_destroy", None, [ctypes.c_void_p]),
+    ("vp_last_error", ctypes.c_char_p, [ctypes.c_void_p]),
+    ("vp_assemble", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
+      ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I, ctypes.POINTER(ctypes.c_void_p),
+      ctypes.POINTER(vp_assembly_stats)]),
+    ("vp_system_shape", ctypes.c_int, [ctypes.c_void_p, I, I]),
+    ("vp_system_download", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, D, D]),
+    ("vp_system_free", None, [ctypes.c_void_p]),
+    ("vp_factorize", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, I, I, D, ctypes.c_int, I, I, D, ctypes.c_int, I, D,
+      I, ctypes.POINTER(ctypes.c_void_p), D]),
+    ("vp_solve", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, D, D, D]),
+    ("vp_solve_system", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, D, D, D]),
+    ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
+    ("vp_factor_free", None, [ctypes.c_void_p]),
+]
+
+_lock = threading.Lock()
+_lib = None
+
+
+class VPError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"[vp status {code}] {msg}")
+        self.code = code
+
+
+class SingularError(VPError):
+    """The reference's LinearAlgebra.SingularException"""
+
+
+def load(build_if_missing: bool = True):
+    """The loaded library; builds it first (nvcc, sm_103a) when it is missing or stale and nvcc is available"""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if build_if_missing and not _build.up_to_date():
+                _build.build()
+            if not os.path.exists(_build.LIB):
+                raise RuntimeError(f"libvortexpanel_gpu.so is not built ({_build.LIB}); run build() first")
+            lib = ctypes.CDLL(_build.LIB)
+            for name, res, args in SIGNATURES:
+                f = getattr(lib, name)
+                f.restype = res
+                f.argtypes = args
+            _lib = lib
+        return _lib
+
+
+def check(ctx, code):
+    if code == VP_OK:
+        return
+    msg = load().vp_last_error(ctx).decode() if ctx else ""
+    if code in (VP_ERR_ARG, VP_ERR_DEGENERATE):
+        raise ValueError(f"[vp status {code}] {msg}")
+    if code == VP_ERR_SINGULAR:
+        raise SingularError(code, msg)
+    raise VPError(code, msg)
+
+
+class Context:
+    """A device context (stream, cuBLAS handle) of the library"""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        code = self.lib.vp_ctx_create(device, ctypes.byref(h))
+        if code != VP_OK:
+            raise VPError(code, f"cannot create a context on CUDA device {device} (no GPU, or the driver failed)")
+        self.h = h
+        self.device = device
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h:
+            try:
+                self.lib.vp_ctx_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+
+_default = None
+
+
+def default_context() -> Context:
+    global _default
+    if _default is None:
+        _default = Context(0)
+    return _default

@@ -1,0 +1,341 @@
+"""The reference's Julia API for the Galerkin hot path, over the GPU library.
+
+Same names, argument meaning and errors as VortexPanel.jl:
+  assemble(g, dm, els, σ, V∞; opts, wake) -> A, b, stats      src/assembly/assemble.jl:377-447
+  factorize_galerkin(dm, A; W) -> GalerkinFactorization          src/assembly/solve.jl:81-87
+  solve_galerkin(F, b) -> (q, μ, λ, cond)                        src/assembly/solve.jl:95-99
+  solve_galerkin(dm, A, b; W) -> (q, μ, λ, cond, residual)       src/assembly/solve.jl:51-59
+  source_strengths(els, V∞)                                      src/assembly/assemble.jl:364
+and the loads the hot path's outputs feed (src/post/Post.jl:19-23,72-84; src/post/forces.jl:11-81).
+
+``A`` stays on the GPU (a ``DeviceSystem``); ``np.asarray(A)`` or ``A.download()`` copies it to the host like the
+reference's Matrix. ArgumentError maps to ValueError, SingularException to ``SingularError``.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass, fields
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from ._lib import D, I, check, default_context, load
+
+TIER_NAMES = ("self", "edge", "vertex", "contact", "near", "far")
+
+
+@dataclass
+class AssemblyOptions:
+    """AssemblyOptions (assemble.jl:26-41) plus the arithmetic: precision = 'fp64' (every integral, the LU and the
+    solve in FP64) or 'mixed' (FP32 far and near tiers, FP64 touching and contact tiers, FP32 LU refined with FP64
+    residuals)."""
+    test: str = "hat"
+    far_ratio: float = 3.0
+    far_points: int = 3
+    near_points: int = 7
+    near_ratio: float = 1.5
+    near_depth: int = 3
+    touch_levels: int = 6
+    touch_ratio: float = 0.15
+    touch_order: int = 3
+    corner_angle: float = 75.0
+    contact_rel: float = 0.1
+    kernel_far: float = 10.0
+    precision: str = "fp64"
+    threaded: bool = True  # accepted for compatibility; the GPU path is always parallel
+
+    def c_struct(self) -> _lib.vp_assembly_options:
+        tests = {"hat": 0, "onering": 1, "dual": 2}
+        if self.test not in tests:
+            raise ValueError(f"test must be :hat, :onering or :dual, not {self.test}")
+        precs = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}
+        if self.precision not in precs:
+            raise ValueError(f"precision must be 'fp64' or 'mixed', not {self.precision}")
+        o = _lib.vp_assembly_options()
+        for f in fields(self):
+            if f.name in ("threaded",):
+                continue
+            v = getattr(self, f.name)
+            if f.name == "test":
+                v = tests[v]
+            elif f.name == "precision":
+                v = precs[v]
+            setattr(o, f.name, v)
+        return o
+
+
+def _dp(a):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    return a, a.ctypes.data_as(D)
+
+
+def _ip(a):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    return a, a.ctypes.data_as(I)
+
+
+# ---- elements (src/elements/flat_triangle.jl) -------------------------------------------------------------------------
+
+@dataclass
+class Elements:
+    """The FlatTriangle fields of every triangle, as arrays: n, area, centroid, diam, gradλ (3 x ntri x 3), γ"""
+    n: np.ndarray
+    area: np.ndarray
+    centroid: np.ndarray
+    diam: np.ndarray
+    gradl: list
+    gam: list
+
+
+def build_elements(g) -> Elements:
+    x, t = g.x, g.tris
+    a, b, c = x[t[:, 0]], x[t[:, 1]], x[t[:, 2]]
+    nA = np.cross(b - a, c - a)
+    A2 = np.linalg.norm(nA, axis=1)
+    if np.any(~(A2 > 0)):
+        raise ValueError(f"degenerate triangle {int(np.argmin(A2))}")
+    n = nA / A2[:, None]
+    e = [c - b, a - c, b - a]
+    diam = np.maximum.reduce([np.linalg.norm(b - a, axis=1), np.linalg.norm(c - b, axis=1), np.linalg.norm(a - c, axis=1)])
+    return Elements(n, A2 / 2, (a + b + c) / 3, diam, [np.cross(n, ek) / A2[:, None] for ek in e],
+                    [-ek / A2[:, None] for ek in e])
+
+
+def source_strengths(els: Elements, V, V_body=None) -> np.ndarray:
+    """σ = -(V∞ - V_body)·n (assemble.jl:364)"""
+    V = np.asarray(V, float)
+    if V_body is not None:
+        V = V - np.asarray(V_body, float)
+    return -(els.n @ V)
+
+
+# ---- assembly ----------------------------------------------------------------------------------------------------------
+
+class DeviceSystem:
+    """The assembled A (nslot x (nslot + nwake)) and b, resident on the GPU"""
+
+    def __init__(self, ctx, handle, nslot, ncols):
+        self.ctx, self.h, self.nslot, self.ncols = ctx, handle, nslot, ncols
+
+    @property
+    def shape(self):
+        return (self.nslot, self.ncols)
+
+    def download(self):
+        A = np.zeros((self.nslot, self.ncols))
+        check(self.ctx.h, load().vp_system_download(self.ctx.h, self.h, A.ctypes.data_as(D), None))
+        return A
+
+    def rhs(self):
+        b = np.zeros(self.nslot)
+        check(self.ctx.h, load().vp_system_download(self.ctx.h, self.h, None, b.ctypes.data_as(D)))
+        return b
+
+    def __array__(self, dtype=None, copy=None):
+        A = self.download()
+        return A if dtype is None else A.astype(dtype)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                load().vp_system_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, wake=None, ctx=None):
+    """A, b and stats (assemble.jl:377-447). A is a DeviceSystem; b and stats are on the host."""
+    opts = opts or AssemblyOptions()
+    if external is not None:
+        raise ValueError("external velocity fields are not supported by the GPU path")
+    ctx = ctx or default_context()
+    o = opts.c_struct()
+    x, px = _dp(g.x)
+    tr, pt = _ip(g.tris)
+    cs, pc = _ip(dm.corner_slot)
+    tp = np.asarray(g.touch_pairs, np.int32).reshape(-1, 2)
+    tpp, ptp = _ip(tp if len(tp) else np.zeros((1, 2), np.int32))
+    sg, ps = _dp(sigma)
+    if sg.shape != (g.ntri,):
+        raise ValueError(f"σ has {sg.shape[0]} entries, expected {g.ntri}")
+    VV, pV = _dp(V)
+    if wake is not None:
+        wx, pwx = _dp(wake.x)
+        wt, pwt = _ip(wake.tris if len(wake.tris) else np.zeros((1, 3)))
+        wf, pwf = _ip(wake.filaments if len(wake.filaments) else np.zeros((1, 2)))
+        nw, nwt, nf = wake.x.shape[0], len(wake.tris), len(wake.filaments)
+    else:
+        wx = wt = wf = None
+        pwx, pwt, pwf = None, None, None
+        nw = nwt = nf = 0
+    h = ctypes.c_void_p()
+    st = _lib.vp_assembly_stats()
+    check(ctx.h, load().vp_assemble(ctx.h, ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(tp), ptp, ps, pV,
+                                    nw, pwx, nwt, pwt, nf, pwf, ctypes.byref(h), ctypes.byref(st)))
+    A = DeviceSystem(ctx, h, dm.nslot, dm.nslot + nw)
+    stats = {"pairs": dict(zip(TIER_NAMES, list(st.pairs))), "points": dict(zip(TIER_NAMES, list(st.points))),
+             "time": st.time_ms / 1e3}
+    return A, A.rhs(), stats
+
+
+# ---- the bordered solve ------------------------------------------------------------------------------------------------
+
+class GalerkinFactorization:
+    """The LU of the bordered system on the GPU (solve.jl:65-72)"""
+
+    def __init__(self, ctx, handle, dm, precision):
+        self.ctx, self.h, self.dm, self.precision = ctx, handle, dm, precision
+        n = ctypes.c_int()
+        c = ctypes.c_double()
+        check(ctx.h, load().vp_factor_info(handle, ctypes.byref(n), ctypes.byref(c)))
+        self.n, self.cond = n.value, c.value
+        self.nq, self.nb = dm.nq, len(dm.body_closed)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                load().vp_factor_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+def _csr_parts(M):
+    M = sp.csr_matrix(M)
+    p, pp = _ip(M.indptr)
+    c, pc = _ip(M.indices if M.nnz else np.zeros(1))
+    v, pv = _dp(M.data if M.nnz else np.zeros(1))
+    return (p, c, v), (pp, pc, pv)
+
+
+def factorize_galerkin(dm, A: DeviceSystem, W=None, precision=None, ctx=None) -> GalerkinFactorization:
+    """Factor the bordered matrix of C' A [C; W] once, for many right hand sides (solve.jl:81-87)"""
+    ctx = ctx or A.ctx
+    precision = precision or "fp64"
+    prec = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}[precision]
+    keepC, (cp, cc, cv) = _csr_parts(dm.C)
+    nw = 0 if W is None else W.shape[0]
+    if A.ncols != dm.nslot + nw:
+        raise ValueError(f"A is {A.shape}, expected ({dm.nslot}, {dm.nslot + nw})")
+    if W is not None:
+        keepW, (wp, wc, wv) = _csr_parts(W)
+    else:
+        wp = wc = wv = None
+    qb, pqb = _ip(dm.q_body)
+    sa, psa = _dp(dm.slot_area)
+    sb, psb = _ip(dm.slot_body)
+    h = ctypes.c_void_p()
+    cond = ctypes.c_double()
+    check(ctx.h, load().vp_factorize(ctx.h, A.h, prec, dm.nq, cp, cc, cv, nw, wp, wc, wv, len(dm.body_closed), pqb, psa,
+                                     psb, ctypes.byref(h), ctypes.byref(cond)))
+    return GalerkinFactorization(ctx, h, dm, precision)
+
+
+def solve_galerkin(*args, W=None, precision=None, ctx=None):
+    """solve_galerkin(F, b) (solve.jl:95-99) or solve_galerkin(dm, A, b; W) (solve.jl:51-59). b may hold several right
+    hand sides as columns."""
+    if isinstance(args[0], GalerkinFactorization):
+        F, b = args
+        b = np.asarray(b, float)
+        nrhs = 1 if b.ndim == 1 else b.shape[1]
+        bb, pb = _dp(b.reshape(F.dm.nslot, nrhs).T.copy().ravel())  # column-major
+        q = np.zeros(F.nq * nrhs)
+        lam = np.zeros(max(F.nb, 1) * nrhs)
+        check(F.ctx.h, load().vp_solve(F.ctx.h, F.h, nrhs, pb, q.ctypes.data_as(D), lam.ctypes.data_as(D)))
+        q = q.reshape(nrhs, F.nq).T
+        lam = lam[:F.nb * nrhs].reshape(nrhs, F.nb).T
+        if b.ndim == 1:
+            q, lam = q[:, 0], lam[:, 0]
+        return dict(q=q, mu=F.dm.C @ q, lam=lam, cond=F.cond)
+    dm, A, b = args
+    F = factorize_galerkin(dm, A, W=W, precision=precision, ctx=ctx)
+    res = ctypes.c_double()
+    q = np.zeros(dm.nq)
+    lam = np.zeros(max(F.nb, 1))
+    if np.array_equal(np.asarray(b), A.rhs()):
+        check(F.ctx.h, load().vp_solve_system(F.ctx.h, F.h, A.h, q.ctypes.data_as(D), lam.ctypes.data_as(D),
+                                              ctypes.byref(res)))
+        residual = res.value
+    else:
+        s = solve_galerkin(F, b)
+        q, lam = s["q"], s["lam"]
+        residual = float("nan")
+    return dict(q=q, mu=dm.C @ q, lam=lam[:F.nb], cond=F.cond, residual=residual, F=F)
+
+
+# ---- loads (src/post/Post.jl, src/post/forces.jl) ------------------------------------------------------------------
+
+def element_values(dm, mu):
+    return np.asarray(mu)[dm.corner_slot]
+
+
+def gradient_velocity(els: Elements, dm, mu, V):
+    """V∞ - (V∞·n)n + ∇μ on every triangle (Post.jl:72-73)"""
+    V = np.asarray(V, float)
+    m = element_values(dm, mu)
+    grad = sum(m[:, k:k + 1] * els.gradl[k] for k in range(3))
+    return V - (els.n @ V)[:, None] * els.n + grad
+
+
+def pressure_coefficient(u, V, dmudt=None):
+    V = np.asarray(V, float)
+    s = np.einsum("ij,ij->i", u, u)
+    if dmudt is not None:
+        s = s + 2 * np.asarray(dmudt)
+    return 1 - s / (V @ V)
+
+
+def pressure_force(els: Elements, cp, origin=(0.0, 0.0, 0.0)):
+    f = -(np.asarray(cp) * els.area)[:, None] * els.n
+    return f.sum(axis=0), np.cross(els.centroid - np.asarray(origin, float), f).sum(axis=0)
+
+
+def _te_segments(wte):
+    out = []
+    for line, closed in zip(wte.lines, wte.closed):
+        m = len(line)
+        for i in range(m if closed else m - 1):
+            out.append((line[i], line[(i + 1) % m]))
+    return out
+
+
+def kutta_joukowski_force(wte, mu_w, V):
+    """(2/|V∞|²) V∞ × ∫μ_w dl along the trailing edge lines (forces.jl:34-39)"""
+    V = np.asarray(V, float)
+    G = np.zeros(3)
+    for a, b in _te_segments(wte):
+        G += (mu_w[a] + mu_w[b]) / 2 * (wte.x[b] - wte.x[a])
+    return 2 / (V @ V) * np.cross(V, G)
+
+
+def trefftz_drag(wte, mu_w, V):
+    """Induced drag in the Trefftz plane, in units of q∞ (forces.jl:53-81)"""
+    V = np.asarray(V, float)
+    d = V / np.linalg.norm(V)
+    P = lambda x: x - (x @ d) * d  # noqa: E731
+    vort, strips = [], []
+    for line, closed in zip(wte.lines, wte.closed):
+        m = len(line)
+        nseg = m if closed else m - 1
+        G = [(mu_w[line[i]] + mu_w[line[(i + 1) % m]]) / 2 for i in range(nseg)]
+        for i in range(m):
+            before = G[i - 1] if i > 0 else (G[nseg - 1] if closed else 0.0)
+            after = G[i] if i < nseg else 0.0
+            vort.append((P(wte.x[line[i]]), after - before))
+        for i in range(nseg):
+            strips.append((P(wte.x[line[i]]), P(wte.x[line[(i + 1) % m]]), G[i]))
+    if not strips:
+        return 0.0
+    pv = np.array([v[0] for v in vort])
+    dG = np.array([v[1] for v in vort])
+    Dsum = 0.0
+    for a, b, Gk in strips:
+        c, l = (a + b) / 2, np.linalg.norm(b - a)
+        n = np.cross(d, (b - a) / l)
+        r = c - pv
+        v = (dG[:, None] / (4 * math.pi) * np.cross(d, r) / np.einsum("ij,ij->i", r, r)[:, None]).sum(axis=0)
+        Dsum += Gk * (n @ v) * l
+    return 2 * Dsum / (V @ V)
