@@ -1,0 +1,286 @@
+"""Benchmark of the Galerkin hot path on the 25k-triangle lifting wing.
+
+Workload: rectangular wing of aspect ratio 8, NACA 0012 section, 112 full-cosine chordwise x 56 full-cosine spanwise
+panels per side (25,088 surface + 444 cap triangles, 12.9k unknowns), rigid wake 2.5 spans (20 chords) long along +x
+with tip filaments, alpha = 5 deg. One step = assemble (all tiers) + factorize (bordered LU) + solve + loads (CL by
+pressure, CDi by Trefftz) through the library, in mixed precision (FP32 far/near tiers and LU, FP64 touching tiers and
+refinement). The plain FP64 GPU path is timed on the same workload for the comparison, with |dCL| and |dCDi|.
+
+Every N > 1 rank runs an independent replica (the solve of one wing does not shard in this build).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "vortexpanel.jl_gb300"))
+
+METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|<1e-6"
+NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
+
+
+def workload():
+    from vortexpanel_gpu import meshes
+
+    w = meshes.wing(NCHORD, NSPAN, aspect=ASPECT)
+    wake = meshes.build_wake(w.g, w.dm, (1.0, 0.0, 0.0), length=2.5)
+    W = meshes.wake_rows(w.dm, wake.te)
+    a = math.radians(ALPHA)
+    V = np.array([math.cos(a), 0.0, math.sin(a)])
+    eL = np.array([-math.sin(a), 0.0, math.cos(a)])
+    return w, wake, W, V, eL
+
+
+def step(vp, w, wake, W, V, eL, precision, ctx):
+    """one pass of the hot path; returns CL, CDi and the assembly stats"""
+    els = vp.build_elements(w.g)
+    sig = vp.source_strengths(els, V)
+    A, b, stats = vp.assemble(w.g, w.dm, els, sig, V, wake=wake, opts=vp.AssemblyOptions(precision=precision), ctx=ctx)
+    F = vp.factorize_galerkin(w.dm, A, W=W, precision=precision, ctx=ctx)
+    s = vp.solve_galerkin(F, b)
+    S = w.span * w.chord
+    cp = vp.pressure_coefficient(vp.gradient_velocity(els, w.dm, s["mu"], V), V)
+    CL = float(vp.pressure_force(els, cp)[0] @ eL / S)
+    CDi = float(vp.trefftz_drag(w.dm.wake_te, w.dm.K @ s["q"], V) / S)
+    del A, F
+    return CL, CDi, stats, s["cond"]
+
+
+class Clocks:
+    """nvidia-smi samples of the SM clock and throttle reasons while the timed region runs"""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_baseline(w, wake, W, V, eL, budget_s=20.0):
+    """The oracle (C++ restatement of the reference's assembly, OpenMP over test triangles as assemble.jl:395, and the
+    reference's LAPACK dgetrf/dgetrs through scipy) on a bounded sample: the rows of a slice of test triangles, and
+    the LU of a leading principal block; scaled to the full step (rows linearly, the LU by n^3)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    import scipy.linalg as sla
+
+    oracle.build()
+    from vortexpanel_gpu import api
+
+    els = api.build_elements(w.g)
+    sig = api.source_strengths(els, V)
+    nt = w.g.ntri
+    cores = os.cpu_count() or 1
+    # assembly: grow the slice until it takes a measurable time
+    rows = max(8, nt // 2000)
+    while True:
+        t0 = time.perf_counter()
+        oracle.assemble(w.g, w.dm, sig, V, wake=wake, rows=(nt // 2, nt // 2 + rows), nthreads=cores)
+        ta = time.perf_counter() - t0
+        if ta > budget_s / 4 or rows >= nt // 4:
+            break
+        rows = min(nt // 4, int(rows * max(2.0, (budget_s / 4) / max(ta, 1e-3))))
+    t_asm = ta * nt / rows
+    n = w.dm.nq + 1
+    m = min(n, 4000)
+    M = np.random.default_rng(1).standard_normal((m, m)) + m * np.eye(m)
+    t0 = time.perf_counter()
+    lu = sla.lu_factor(M, check_finite=False)
+    sla.lu_solve(lu, np.ones(m), check_finite=False)
+    tl = time.perf_counter() - t0
+    t_lu = tl * (n / m) ** 3
+    return {"value": t_asm + t_lu, "unit": "s", "cores": cores, "kind": "port",
+            "sample": f"oracle assembly of {rows} of {nt} test-triangle rows ({ta:.1f} s, scaled x{nt / rows:.0f}) + "
+                      f"scipy/LAPACK dgetrf of a {m}x{m} block ({tl:.2f} s, scaled by (n/m)^3 to n={n})",
+            "assembly_s": t_asm, "lu_s": t_lu}
+
+
+def dist_setup(n_gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return rank, world, local, dist
+    return rank, world, local, None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    args = ap.parse_args()
+    rank, world, local, dist = dist_setup(args.gpus)
+    w, wake, W, V, eL = workload()
+    config = {"workload": f"wing AR{ASPECT:g} NACA0012 {NCHORD}x{NSPAN}/side ({w.g.ntri} tris, {w.dm.nq} unknowns), "
+                          f"rigid wake {len(wake.tris)} tris + {len(wake.filaments)} filaments, alpha {ALPHA:g} deg",
+              "ntri": w.g.ntri, "nq": w.dm.nq, "nwake_nodes": wake.nwake, "precision": "mixed",
+              "l2": "inputs larger than L2 (A is 1.6 GB FP64)", "parallelism": f"replicas x{world}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline(w, wake, W, V, eL)
+        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": world, "steps": 1, "warmup": 0,
+                "ms_per_step": cb["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import vortexpanel_gpu as vp
+
+    ctx = vp.Context(local)
+    for _ in range(args.warmup):
+        step(vp, w, wake, W, V, eL, "mixed", ctx)
+    ctx.phase_times(reset=True)
+    ctx.transfer_bytes(reset=True)
+    if dist:
+        dist.barrier()
+    walls = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            CL, CDi, stats, cond = step(vp, w, wake, W, V, eL, "mixed", ctx)
+            walls.append(time.perf_counter() - t0)
+    phases, launches = ctx.phase_times(reset=True)
+    h2d, d2h = ctx.transfer_bytes(reset=True)
+    dev_s = sum(phases.values()) / 1e3 / args.steps
+    e2e_s = sum(walls) / args.steps
+    if dist:
+        import torch
+
+        t = torch.tensor([dev_s, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_s, e2e_s = float(t[0]), float(t[1])
+    # the plain FP64 GPU path on the same workload
+    fp = {}
+    if args.fp64_steps > 0:
+        step(vp, w, wake, W, V, eL, "fp64", ctx)
+        ctx.phase_times(reset=True)
+        fw = []
+        for _ in range(args.fp64_steps):
+            t0 = time.perf_counter()
+            CL64, CDi64, stats64, cond64 = step(vp, w, wake, W, V, eL, "fp64", ctx)
+            fw.append(time.perf_counter() - t0)
+        ph64, _ = ctx.phase_times(reset=True)
+        fp = {"fp64_s": sum(ph64.values()) / 1e3 / args.fp64_steps, "fp64_e2e_s": sum(fw) / len(fw),
+              "fp64_phases_ms": {k: v / args.fp64_steps for k, v in ph64.items()},
+              "CL_fp64": CL64, "CDi_fp64": CDi64, "dCL": abs(CL - CL64), "dCDi": abs(CDi - CDi64)}
+        fp["speedup_vs_fp64"] = fp["fp64_s"] / dev_s
+    if rank != 0:
+        return
+    per = {k: v / args.steps for k, v in phases.items()}
+    # roofline of the dominant kernel: FP32 CUDA-core bound (the pair integrals); algorithmic flops per evaluated
+    # point (kernel evaluation + contraction into the hat block) from the device's per-tier point counts
+    pk, src = peaks()
+    dom = max(("far", "near", "lu"), key=lambda k: per[k])
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal FP32 FMA rate at the max SM clock
+    FLOP_FAR_POINT = 230 + 18
+    if dom == "far":
+        flops = stats["points"]["far"] * FLOP_FAR_POINT
+        roof = {"kernel": "far_kernel<float,8>", "bound": "fp32", "achieved": flops / (per["far"] / 1e3) / 1e12,
+                "peak": fp32_peak, "unit": "TFLOP/s"}
+    elif dom == "near":
+        pts = stats["points"]
+        flops = pts["near"] * FLOP_FAR_POINT
+        roof = {"kernel": "near_kernel", "bound": "fp32", "achieved": flops / (per["near"] / 1e3) / 1e12,
+                "peak": fp32_peak, "unit": "TFLOP/s"}
+    else:
+        n = w.dm.nq + 1
+        roof = {"kernel": "lu (cluster panels + sgemm)", "bound": "tensor",
+                "achieved": 2 / 3 * n ** 3 / (per["lu"] / 1e3) / 1e12, "peak": pk.get("bf16_tflops", 1900.0),
+                "unit": "TFLOP/s"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["peak_source"] = "nominal (152 SMs x 128 FP32 lanes x 2 x max SM clock)" if roof["bound"] == "fp32" else src
+    roof["traffic"] = None
+    line = {"metric": METRIC, "value": dev_s, "unit": "s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_s * 1e3, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": config,
+            "e2e": {"value": e2e_s, "unit": "s", "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps},
+            "gpu_launches": launches // args.steps * args.steps, "phases_ms": per,
+            "CL": CL, "CDi": CDi, "cond": cond, "tiers": stats, "roofline": roof, "clocks": clk.summary(),
+            "adjoint": "not included yet"}
+    line.update(fp)
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline(w, wake, W, V, eL)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -108,6 +108,13 @@ int vp_solve(vp_ctx* ctx, const vp_factor* F, int nrhs, const double* b, double*
 int vp_solve_system(vp_ctx* ctx, const vp_factor* F, const vp_system* sys, double* q, double* lambda,
                     double* residual);
 
+/* Instrumentation (no counterpart in the reference, which only times with @elapsed): device milliseconds per phase
+ * since the last reset, measured with CUDA events on the context's stream, in the order setup, classify, far, near,
+ * reduce, lu, cond, solve, adjoint (n entries at most), and the number of this library's kernel launches. */
+int vp_phase_times(vp_ctx* ctx, double* ms, int n, long long* launches, int reset);
+/* Instrumentation (no counterpart in the reference): bytes copied host->device and device->host by the library. */
+int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset);
+
 /* Condition estimate and size of a factorization. */
 int vp_factor_info(const vp_factor* F, int* n, double* cond);
 void vp_factor_free(vp_factor* F);

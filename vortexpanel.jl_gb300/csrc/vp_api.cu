@@ -13,6 +13,33 @@ int vp_fail(vp_ctx* ctx, int code, const std::string& msg) {
     return code;
 }
 
+int vp_phase_begin(vp_ctx* ctx, int ph) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess)
+        return vp_fail(ctx, VP_ERR_CUDA, "cudaEventCreate");
+    cudaEventRecord(a, ctx->stream);
+    ctx->pending.push_back({ph, {a, b}});
+    return VP_OK;
+}
+
+int vp_phase_end(vp_ctx* ctx) {
+    if (ctx->pending.empty()) return VP_OK;
+    cudaEventRecord(ctx->pending.back().second.second, ctx->stream);
+    return VP_OK;
+}
+
+void vp_phase_flush(vp_ctx* ctx) {
+    for (auto& p : ctx->pending) {
+        float ms = 0;
+        if (cudaEventSynchronize(p.second.second) == cudaSuccess &&
+            cudaEventElapsedTime(&ms, p.second.first, p.second.second) == cudaSuccess)
+            ctx->phase_ms[p.first] += ms;
+        cudaEventDestroy(p.second.first);
+        cudaEventDestroy(p.second.second);
+    }
+    ctx->pending.clear();
+}
+
 extern "C" {
 
 void vp_default_options(vp_assembly_options* o) {
@@ -71,6 +98,7 @@ void vp_ctx_destroy(vp_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    vp_phase_flush(ctx);
     if (ctx->d_flag) cudaFree(ctx->d_flag);
     if (ctx->blas) cublasDestroy(ctx->blas);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -78,6 +106,27 @@ void vp_ctx_destroy(vp_ctx* ctx) {
 }
 
 const char* vp_last_error(const vp_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int vp_phase_times(vp_ctx* ctx, double* ms, int n, long long* launches, int reset) {
+    if (!ctx) return VP_ERR_ARG;
+    vp_phase_flush(ctx);
+    for (int k = 0; k < n && k < PH_COUNT; ++k)
+        if (ms) ms[k] = ctx->phase_ms[k];
+    if (launches) *launches = ctx->launches;
+    if (reset) {
+        for (double& v : ctx->phase_ms) v = 0;
+        ctx->launches = 0;
+    }
+    return VP_OK;
+}
+
+int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset) {
+    if (!ctx) return VP_ERR_ARG;
+    if (h2d) *h2d = ctx->h2d_bytes;
+    if (d2h) *d2h = ctx->d2h_bytes;
+    if (reset) ctx->h2d_bytes = ctx->d2h_bytes = 0;
+    return VP_OK;
+}
 
 int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,
                 const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
@@ -99,9 +148,8 @@ int vp_system_shape(const vp_system* sys, int* nrows, int* ncols) {
 int vp_system_download(vp_ctx* ctx, const vp_system* sys, double* A, double* b) {
     if (!ctx || !sys) return vp_fail(ctx, VP_ERR_ARG, "null argument");
     if (A)
-        VP_CUDA(ctx, cudaMemcpyAsync(A, sys->A, sizeof(double) * size_t(sys->nslot) * sys->ncols, cudaMemcpyDeviceToHost,
-                                     ctx->stream));
-    if (b) VP_CUDA(ctx, cudaMemcpyAsync(b, sys->b, sizeof(double) * sys->nslot, cudaMemcpyDeviceToHost, ctx->stream));
+        VP_CUDA(ctx, vp_d2h(ctx, A, sys->A, sizeof(double) * size_t(sys->nslot) * sys->ncols));
+    if (b) VP_CUDA(ctx, vp_d2h(ctx, b, sys->b, sizeof(double) * sys->nslot));
     VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return VP_OK;
 }

@@ -1340,7 +1340,10 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
     for (size_t c = 0; c < colours.size(); ++c) {
         fa.tiles = d_tiles + off[c];
         int nb = off[c + 1] - off[c];
-        if (nb) far_kernel<T, TT><<<nb, FAR_NT, 0, ctx->stream>>>(fa);
+        if (nb) {
+            far_kernel<T, TT><<<nb, FAR_NT, 0, ctx->stream>>>(fa);
+            ctx->launches++;
+        }
     }
     VP_CUDA(ctx, cudaGetLastError());
     return VP_OK;
@@ -1435,6 +1438,7 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
 
     DevList dl;
     int r;
+    vp_phase_begin(ctx, PH_SETUP);
     TriGeo *d_tg, *d_wg;
     CentF *d_tc, *d_wc;
     double *d_tq, *d_tw, *d_wx = nullptr;
@@ -1454,7 +1458,9 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         for (int k = 0; k < 5; ++k)
             if ((r = dl.up(ctx, &d_rule[k], *R[k]))) return r;
     }
+    vp_phase_end(ctx);
     // classification of the non-far sources of every test triangle
+    vp_phase_begin(ctx, PH_CLASSIFY);
     long long *d_nfptr, *d_wfptr;
     int *d_nf, *d_wf, *d_cnt;
     if ((r = dl.alloc(ctx, &d_cnt, size_t(ntri)))) return r;
@@ -1463,13 +1469,15 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
     const float ratio32 = float(o->far_ratio);
     classify_kernel<<<ntri, 256, 0, ctx->stream>>>(0, ntri, d_tc, d_tg, ntri, d_tc, d_tg, ratio32, o->far_ratio, d_cnt,
                                                    nullptr, nullptr);
-    VP_CUDA(ctx, cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * ntri, cudaMemcpyDeviceToHost, ctx->stream));
+    ctx->launches++;
+    VP_CUDA(ctx, vp_d2h(ctx, cnt.data(), d_cnt, sizeof(int) * ntri));
     VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (int t = 0; t < ntri; ++t) nfptr[t + 1] = nfptr[t] + cnt[t];
     if (nwtri > 0) {
         classify_kernel<<<ntri, 256, 0, ctx->stream>>>(0, ntri, d_tc, d_tg, nwtri, d_wc, d_wg, ratio32, o->far_ratio,
                                                        d_cnt, nullptr, nullptr);
-        VP_CUDA(ctx, cudaMemcpyAsync(cnt.data(), d_cnt, sizeof(int) * ntri, cudaMemcpyDeviceToHost, ctx->stream));
+        ctx->launches++;
+        VP_CUDA(ctx, vp_d2h(ctx, cnt.data(), d_cnt, sizeof(int) * ntri));
         VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         for (int t = 0; t < ntri; ++t) wfptr[t + 1] = wfptr[t] + cnt[t];
     }
@@ -1479,10 +1487,14 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         return r;
     classify_kernel<<<ntri, 256, 0, ctx->stream>>>(1, ntri, d_tc, d_tg, ntri, d_tc, d_tg, ratio32, o->far_ratio,
                                                    nullptr, d_nfptr, d_nf);
-    if (nwtri > 0)
+    ctx->launches++;
+    if (nwtri > 0) {
         classify_kernel<<<ntri, 256, 0, ctx->stream>>>(1, ntri, d_tc, d_tg, nwtri, d_wc, d_wg, ratio32, o->far_ratio,
                                                        nullptr, d_wfptr, d_wf);
+        ctx->launches++;
+    }
     VP_CUDA(ctx, cudaGetLastError());
+    vp_phase_end(ctx);
 
     // the system
     vp_system* sys = new vp_system();
@@ -1549,7 +1561,9 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
             }
         }
         std::vector<int> cs(corner_slot, corner_slot + 3 * ntri);
+        vp_phase_begin(ctx, PH_FAR);
         r = mixed ? run_far<float, 8>(ctx, fa, tg, cs, nslot, dl) : run_far<double, 4>(ctx, fa, tg, cs, nslot, dl);
+        vp_phase_end(ctx);
         if (r) { vp_system_free(sys); return r; }
     }
 
@@ -1615,16 +1629,21 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
             na.tint[k] = o->test == 1 ? 1.0 : 1.0 / 3;
         }
         na.stats = d_stats;
+        vp_phase_begin(ctx, PH_NEAR);
         for (size_t c = 0; c < colours.size(); ++c) {
             na.tests = d_tests + off[c];
             na.ntests = off[c + 1] - off[c];
             int nb = (na.ntests + NEAR_WARPS - 1) / NEAR_WARPS;
-            if (nb) near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+            if (nb) {
+                near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+                ctx->launches++;
+            }
         }
+        vp_phase_end(ctx);
         VP_CUDA(ctx, cudaGetLastError());
     }
     unsigned long long hs[12];
-    VP_CUDA(ctx, cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+    VP_CUDA(ctx, vp_d2h(ctx, hs, d_stats, sizeof(hs)));
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
         vp_system_free(sys);

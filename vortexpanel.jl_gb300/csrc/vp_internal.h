@@ -8,6 +8,20 @@
 
 #include "../../include/vortexpanel_gpu.h"
 
+// phases timed with CUDA events on the context's stream (vp_phase_times)
+enum {
+    PH_SETUP = 0,   // element data and tile uploads
+    PH_CLASSIFY,    // non-far source lists
+    PH_FAR,         // far tier tile kernel
+    PH_NEAR,        // near, touching and contact tiers
+    PH_REDUCE,      // C' A [C; W] and the border
+    PH_LU,          // LU factorization
+    PH_COND,        // condition estimate
+    PH_SOLVE,       // triangular solves and refinement
+    PH_ADJOINT,     // adjoint pair derivatives
+    PH_COUNT
+};
+
 struct vp_ctx {
     int device = 0;
     int nsm = 0;
@@ -15,7 +29,17 @@ struct vp_ctx {
     cublasHandle_t blas = nullptr;
     std::string err;
     int* d_flag = nullptr;  // device error word of bounded waits and checks
+    // instrumentation: per-phase device time (ms, cumulative) and launches of this library's kernels
+    double phase_ms[PH_COUNT] = {};
+    long long launches = 0;
+    long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies made by the library
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
 };
+
+// record the start/end of a phase on the context's stream; vp_phase_flush() accumulates the elapsed times
+int vp_phase_begin(vp_ctx* ctx, int ph);
+int vp_phase_end(vp_ctx* ctx);
+void vp_phase_flush(vp_ctx* ctx);
 
 // Element data of one triangle in FP64 (the FlatTriangle / SourceTriangle fields the kernels read).
 struct TriGeo {
@@ -88,7 +112,18 @@ int vp_upload(vp_ctx* ctx, T** p, const T* h, size_t n) {
     int r = vp_alloc(ctx, p, n);
     if (r) return r;
     if (n) VP_CUDA(ctx, cudaMemcpyAsync(*p, h, n * sizeof(T), cudaMemcpyHostToDevice, ctx->stream));
+    ctx->h2d_bytes += (long long)(n * sizeof(T));
     return VP_OK;
+}
+
+// counted copies between host and device on the context's stream
+inline cudaError_t vp_h2d(vp_ctx* ctx, void* d, const void* h, size_t bytes) {
+    ctx->h2d_bytes += (long long)bytes;
+    return cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, ctx->stream);
+}
+inline cudaError_t vp_d2h(vp_ctx* ctx, void* h, const void* d, size_t bytes) {
+    ctx->d2h_bytes += (long long)bytes;
+    return cudaMemcpyAsync(h, d, bytes, cudaMemcpyDeviceToHost, ctx->stream);
 }
 
 // linear algebra (vp_linalg.cu)

@@ -312,6 +312,7 @@ int launch_leaf(vp_ctx* ctx, T* A, int lda, int c0, int m, int w, int* ipiv, int
     if (smem > 227 * 1024) return vp_fail(ctx, VP_ERR_ARG, "LU leaf panel does not fit shared memory");
     VP_CUDA(ctx, cudaFuncSetAttribute(lu_leaf_kernel<T, W>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
     lu_leaf_kernel<T, W><<<LU_CL, LU_THREADS, smem, ctx->stream>>>(A, lda, c0, m, w, R, ipiv, info);
+    ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
     return VP_OK;
 }
@@ -336,6 +337,7 @@ int laswp(vp_ctx* ctx, T* A, int lda, int cs, int ce, int j0, int j1, const int*
     if (ce <= cs || j1 <= j0) return VP_OK;
     int nc = ce - cs;
     laswp_kernel<T><<<(nc + 127) / 128, 128, 0, ctx->stream>>>(A, lda, cs, ce, j0, j1, ipiv);
+    ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
     return VP_OK;
 }
@@ -369,6 +371,7 @@ int lu_solve(vp_ctx* ctx, const vp_factor* F, const T* LU, const int* d_perm, in
     int nb = int((tot + 255) / 256);
     if (!trans) {
         permute_kernel<T><<<nb, 256, 0, ctx->stream>>>(n, nrhs, d_perm, 0, b, work);
+        ctx->launches++;
         if ((r = trsm<T>(ctx, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_UNIT, n, nrhs, LU, n, work, n))) return r;
         if ((r = trsm<T>(ctx, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, nrhs, LU, n, work, n))) return r;
         VP_CUDA(ctx, cudaMemcpyAsync(b, work, sizeof(T) * tot, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -376,6 +379,7 @@ int lu_solve(vp_ctx* ctx, const vp_factor* F, const T* LU, const int* d_perm, in
         if ((r = trsm<T>(ctx, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n, nrhs, LU, n, b, n))) return r;
         if ((r = trsm<T>(ctx, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_UNIT, n, nrhs, LU, n, b, n))) return r;
         permute_kernel<T><<<nb, 256, 0, ctx->stream>>>(n, nrhs, d_perm, 1, b, work);
+        ctx->launches++;
         VP_CUDA(ctx, cudaMemcpyAsync(b, work, sizeof(T) * tot, cudaMemcpyDeviceToDevice, ctx->stream));
     }
     VP_CUDA(ctx, cudaGetLastError());
@@ -391,6 +395,7 @@ int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F) {
     VP_CUDA(ctx, cudaMemsetAsync(d_info, 0, sizeof(int), ctx->stream));
     if ((r = vp_alloc(ctx, &F->ipiv, size_t(n)))) return r;
     iota_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(n, F->ipiv);  // every swap index valid from the start
+    ctx->launches++;
     if (precision == VP_FP64) {
         if ((r = vp_alloc(ctx, &F->LU64, size_t(n) * n))) return r;
         VP_CUDA(ctx, cudaMemcpyAsync(F->LU64, M64, sizeof(double) * size_t(n) * n, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -400,6 +405,7 @@ int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F) {
     } else {
         if ((r = vp_alloc(ctx, &F->LU32, size_t(n) * n))) return r;
         convert_kernel<double, float><<<4 * ctx->nsm, 256, 0, ctx->stream>>>(size_t(n) * n, M64, F->LU32);
+        ctx->launches++;
         int lw = leaf_width<float>(n);
         if (!lw) return vp_fail(ctx, VP_ERR_ARG, "matrix too large for the LU panel");
         r = rgetrf<float>(ctx, F->LU32, n, 0, n, lw, F->ipiv, d_info);
@@ -410,8 +416,8 @@ int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F) {
     }
     int info = 0;
     F->h_ipiv.resize(n);
-    VP_CUDA(ctx, cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    VP_CUDA(ctx, cudaMemcpyAsync(F->h_ipiv.data(), F->ipiv, sizeof(int) * n, cudaMemcpyDeviceToHost, ctx->stream));
+    VP_CUDA(ctx, vp_d2h(ctx, &info, d_info, sizeof(int)));
+    VP_CUDA(ctx, vp_d2h(ctx, F->h_ipiv.data(), F->ipiv, sizeof(int) * n));
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     cudaFree(d_info);
     if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("LU: ") + cudaGetErrorString(e));
@@ -494,13 +500,16 @@ extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, in
     if ((r = vp_upload(ctx, &d_cfi, cfi.data(), cfi.size()))) { cudaFree(d_cfp); return fail(r); }
     if ((r = vp_upload(ctx, &d_cfv, cfv.data(), cfv.size()))) { cudaFree(d_cfp); cudaFree(d_cfi); return fail(r); }
     if ((r = vp_alloc(ctx, &F->M, size_t(n) * n))) { cudaFree(d_cfp); cudaFree(d_cfi); cudaFree(d_cfv); return fail(r); }
+    vp_phase_begin(ctx, PH_REDUCE);
     VP_CUDA(ctx, cudaMemsetAsync(F->M, 0, sizeof(double) * size_t(n) * n, ctx->stream));
     dim3 grid((nq + 31) / 32, (nq + 31) / 32), block(32, 8);
     reduce_kernel<<<grid, block, 0, ctx->stream>>>(nq, n, sys->A, sys->ncols, F->Ct_ptr, F->Ct_col, F->Ct_val, d_cfp,
                                                    d_cfi, d_cfv, F->M);
+    ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
     // border (bordered_matrix, solve.jl:23-38): scale = mean |diag|, e_k and c_k scaled to 2-norm = scale
     std::vector<double> diag(nq);
+    vp_phase_end(ctx);
     VP_CUDA(ctx, cudaMemcpy2DAsync(diag.data(), sizeof(double), F->M, sizeof(double) * (size_t(n) + 1), sizeof(double), nq,
                                    cudaMemcpyDeviceToHost, ctx->stream));
     VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -535,6 +544,7 @@ extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, in
         if ((r = vp_upload(ctx, &d_e, ecol.data(), ecol.size()))) return fail(r);
         if ((r = vp_upload(ctx, &d_c, crow.data(), crow.size()))) { cudaFree(d_e); return fail(r); }
         border_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(nq, n, nb, d_e, d_c, F->M);
+        ctx->launches++;
         VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         cudaFree(d_e);
         cudaFree(d_c);
@@ -544,13 +554,17 @@ extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, in
         double* d_cs;
         if ((r = vp_alloc(ctx, &d_cs, size_t(n)))) return fail(r);
         col_abs_sum_kernel<double><<<n, 256, 0, ctx->stream>>>(n, F->M, d_cs);
+        ctx->launches++;
         std::vector<double> cs(n);
-        VP_CUDA(ctx, cudaMemcpyAsync(cs.data(), d_cs, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+        VP_CUDA(ctx, vp_d2h(ctx, cs.data(), d_cs, sizeof(double) * n));
         VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
         cudaFree(d_cs);
         F->norm1 = *std::max_element(cs.begin(), cs.end());
     }
-    if ((r = vp_lu_factor(ctx, precision, n, F->M, F))) return fail(r);
+    vp_phase_begin(ctx, PH_LU);
+    r = vp_lu_factor(ctx, precision, n, F->M, F);
+    vp_phase_end(ctx);
+    if (r) return fail(r);
     // permutation from the sequential swaps
     std::vector<int> perm(n);
     for (int i = 0; i < n; ++i) perm[i] = i;
@@ -559,14 +573,15 @@ extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, in
     if (!F->h_se.empty() && (r = vp_upload(ctx, &F->se, F->h_se.data(), F->h_se.size()))) return fail(r);
     // 1-norm condition estimate (LAPACK dgecon / dlacn2: Hager's method with Higham's refinements)
     {
+        vp_phase_begin(ctx, PH_COND);
         std::vector<double> hx(n), hy(n);
         double *dx;
         if ((r = vp_alloc(ctx, &dx, size_t(n)))) return fail(r);
         auto solve1 = [&](bool trans) -> int {
-            VP_CUDA(ctx, cudaMemcpyAsync(dx, hx.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+            VP_CUDA(ctx, vp_h2d(ctx, dx, hx.data(), sizeof(double) * n));
             int rr = solve_core(ctx, F, 1, dx, trans, nullptr);
             if (rr) return rr;
-            VP_CUDA(ctx, cudaMemcpyAsync(hy.data(), dx, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream));
+            VP_CUDA(ctx, vp_d2h(ctx, hy.data(), dx, sizeof(double) * n));
             VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             return VP_OK;
         };
@@ -612,6 +627,7 @@ extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, in
         temp = 2 * temp / (3.0 * n);
         if (temp > est) est = temp;
         cudaFree(dx);
+        vp_phase_end(ctx);
         F->cond = est * F->norm1;
     }
     if (cond) *cond = F->cond;
@@ -650,8 +666,10 @@ static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool
     VP_CUDA(ctx, cudaMemcpyAsync(rhs, x, sizeof(double) * tot, cudaMemcpyDeviceToDevice, ctx->stream));
     int g = std::min<int>(4 * ctx->nsm, int((tot + 255) / 256));
     convert_kernel<double, float><<<g, 256, 0, ctx->stream>>>(tot, rhs, f);
+    ctx->launches++;
     if ((r = lu_solve<float>(ctx, F, F->LU32, d_perm, nrhs, f, fw, trans))) { cleanup(); return r; }
     convert_kernel<float, double><<<g, 256, 0, ctx->stream>>>(tot, f, x);
+    ctx->launches++;
     const double one = 1.0, mone = -1.0;
     const cublasOperation_t op = trans ? CUBLAS_OP_T : CUBLAS_OP_N;
     std::vector<double> rn(nrhs), xn(nrhs);
@@ -670,8 +688,8 @@ static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool
             VP_BLAS(ctx, cublasIdamax(ctx->blas, n, res + size_t(k) * n, 1, &ir));
             VP_BLAS(ctx, cublasIdamax(ctx->blas, n, x + size_t(k) * n, 1, &ix));
             double a, bx;
-            VP_CUDA(ctx, cudaMemcpyAsync(&a, res + size_t(k) * n + (ir - 1), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-            VP_CUDA(ctx, cudaMemcpyAsync(&bx, x + size_t(k) * n + (ix - 1), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+            VP_CUDA(ctx, vp_d2h(ctx, &a, res + size_t(k) * n + (ir - 1), sizeof(double)));
+            VP_CUDA(ctx, vp_d2h(ctx, &bx, x + size_t(k) * n + (ix - 1), sizeof(double)));
             VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
             double ratio = std::fabs(a) / (norm1 * std::fabs(bx) + 1e-300);
             worst = std::max(worst, ratio);
@@ -684,8 +702,10 @@ static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool
         if (it > 3 && worst > 0.5 * prev) break;  // stagnation
         prev = worst;
         convert_kernel<double, float><<<g, 256, 0, ctx->stream>>>(tot, res, f);
+        ctx->launches++;
         if ((r = lu_solve<float>(ctx, F, F->LU32, d_perm, nrhs, f, fw, trans))) { cleanup(); return r; }
         axpy_f2d_kernel<<<g, 256, 0, ctx->stream>>>(tot, f, x);
+        ctx->launches++;
     }
     cleanup();
     if (iters) *iters = it;
@@ -704,12 +724,15 @@ extern "C" int vp_solve(vp_ctx* ctx, const vp_factor* F, int nrhs, const double*
     double *db, *x;
     if ((r = vp_alloc(ctx, &db, size_t(nslot) * nrhs))) return r;
     if ((r = vp_alloc(ctx, &x, tot))) { cudaFree(db); return r; }
-    VP_CUDA(ctx, cudaMemcpyAsync(db, b, sizeof(double) * size_t(nslot) * nrhs, cudaMemcpyHostToDevice, ctx->stream));
+    VP_CUDA(ctx, vp_h2d(ctx, db, b, sizeof(double) * size_t(nslot) * nrhs));
     ctb_kernel<<<int((tot + 255) / 256), 256, 0, ctx->stream>>>(nq, n, nslot, nrhs, F->Ct_ptr, F->Ct_col, F->Ct_val, db, x);
+    ctx->launches++;
+    vp_phase_begin(ctx, PH_SOLVE);
     r = solve_core(ctx, F, nrhs, x, false, nullptr);
+    vp_phase_end(ctx);
     if (!r) {
         std::vector<double> hx(tot);
-        cudaMemcpyAsync(hx.data(), x, sizeof(double) * tot, cudaMemcpyDeviceToHost, ctx->stream);
+        vp_d2h(ctx, hx.data(), x, sizeof(double) * tot);
         cudaError_t e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) r = vp_fail(ctx, VP_ERR_CUDA, cudaGetErrorString(e));
         for (int k = 0; k < nrhs && !r; ++k) {
@@ -733,11 +756,14 @@ extern "C" int vp_solve_system(vp_ctx* ctx, const vp_factor* F, const vp_system*
     if ((r = vp_alloc(ctx, &x, size_t(n)))) return r;
     if ((r = vp_alloc(ctx, &rhs, size_t(n)))) { cudaFree(x); return r; }
     ctb_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(nq, n, F->nslot, 1, F->Ct_ptr, F->Ct_col, F->Ct_val, sys->b, x);
+    ctx->launches++;
     VP_CUDA(ctx, cudaMemcpyAsync(rhs, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    vp_phase_begin(ctx, PH_SOLVE);
     r = solve_core(ctx, F, 1, x, false, nullptr);
+    vp_phase_end(ctx);
     if (!r) {
         std::vector<double> hx(n);
-        cudaMemcpyAsync(hx.data(), x, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+        vp_d2h(ctx, hx.data(), x, sizeof(double) * n);
         if (residual) {
             double nr = 0, nrhs = 0;
             cublasDnrm2(ctx->blas, n, rhs, 1, &nrhs);

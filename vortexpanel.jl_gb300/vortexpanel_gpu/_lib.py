@@ -46,6 +46,9 @@ SIGNATURES = [
       I, ctypes.POINTER(ctypes.c_void_p), D]),
     ("vp_solve", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, D, D, D]),
     ("vp_solve_system", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, D, D, D]),
+    ("vp_phase_times", ctypes.c_int, [ctypes.c_void_p, D, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
+    ("vp_transfer_bytes", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                         ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]
@@ -104,6 +107,20 @@ class Context:
             raise VPError(code, f"cannot create a context on CUDA device {device} (no GPU, or the driver failed)")
         self.h = h
         self.device = device
+
+    PHASES = ("setup", "classify", "far", "near", "reduce", "lu", "cond", "solve", "adjoint")
+
+    def phase_times(self, reset=False):
+        """Device milliseconds per phase since the last reset, and the number of the library's kernel launches"""
+        ms = (ctypes.c_double * len(self.PHASES))()
+        n = ctypes.c_longlong()
+        check(self.h, self.lib.vp_phase_times(self.h, ms, len(self.PHASES), ctypes.byref(n), int(reset)))
+        return dict(zip(self.PHASES, list(ms))), n.value
+
+    def transfer_bytes(self, reset=False):
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        check(self.h, self.lib.vp_transfer_bytes(self.h, ctypes.byref(a), ctypes.byref(b), int(reset)))
+        return a.value, b.value
 
     def __del__(self):
         h = getattr(self, "h", None)
