@@ -29,11 +29,14 @@ sys.path.insert(0, os.path.join(ROOT, "vortexpanel.jl_gb300"))
 
 METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|<1e-6"
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
+SIZES = {"wing25k": (112, 56), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
 
-def workload():
+def workload(name="wing25k"):
     from vortexpanel_gpu import meshes
 
+    global NCHORD, NSPAN
+    NCHORD, NSPAN = SIZES[name]
     w = meshes.wing(NCHORD, NSPAN, aspect=ASPECT)
     wake = meshes.build_wake(w.g, w.dm, (1.0, 0.0, 0.0), length=2.5)
     W = meshes.wake_rows(w.dm, wake.te)
@@ -180,9 +183,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--workload", default="wing25k", choices=list(SIZES),
+                    help="wing25k (the measured configuration) or small (28x14 panels per side, for profiler captures)")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup(args.gpus)
-    w, wake, W, V, eL = workload()
+    w, wake, W, V, eL = workload(args.workload)
     config = {"workload": f"wing AR{ASPECT:g} NACA0012 {NCHORD}x{NSPAN}/side ({w.g.ntri} tris, {w.dm.nq} unknowns), "
                           f"rigid wake {len(wake.tris)} tris + {len(wake.filaments)} filaments, alpha {ALPHA:g} deg",
               "ntri": w.g.ntri, "nq": w.dm.nq, "nwake_nodes": wake.nwake, "precision": "mixed",
@@ -274,6 +279,7 @@ def main():
                     "d2h_bytes_per_step": d2h // args.steps},
             "gpu_launches": launches // args.steps * args.steps, "phases_ms": per,
             "CL": CL, "CDi": CDi, "cond": cond, "tiers": stats, "roofline": roof, "clocks": clk.summary(),
+            "fp64_point_share": stats["points_fp64"] / max(1, sum(stats["points"].values())),
             "adjoint": "not included yet"}
     line.update(fp)
     if not args.no_cpu_baseline:

@@ -61,6 +61,7 @@ typedef struct {
     long long pairs[6];
     long long points[6];
     double time_ms;
+    long long points_fp64; /* points evaluated in FP64 (all of them with VP_FP64) */
 } vp_assembly_stats;
 
 /* Fill the reference's default AssemblyOptions (FP64). */

@@ -249,7 +249,6 @@ __global__ void classify_kernel(int mode, int ntest, const CentF* __restrict__ t
                                 double ratio, int* __restrict__ counts, const long long* __restrict__ offs,
                                 int* __restrict__ list) {
     __shared__ int warp_tot[32];
-    __shared__ int base_sh;
     const int t = blockIdx.x;
     if (t >= ntest) return;
     const CentF T = tc[t];
@@ -279,7 +278,6 @@ __global__ void classify_kernel(int mode, int ntest, const CentF* __restrict__ t
         __syncthreads();
     }
     if (!mode && threadIdx.x == 0) counts[t] = total;
-    (void)base_sh;
 }
 
 // ------------------------------------------------------------------------------------------------------------------
@@ -525,7 +523,7 @@ struct NearArgs {
     double far_ratio, near_ratio, corner_angle, contact_rel, kernel_far;
     double vinf[3];
     double tint[3];
-    unsigned long long* stats;  // pairs[6], points[6]
+    unsigned long long* stats;  // pairs[6], points[6], points evaluated in FP64
 };
 
 struct Bary9 {
@@ -533,13 +531,14 @@ struct Bary9 {
 };
 
 struct WarpSh {
-    double E[27];          // E[3k+a] (x3): x_T,k - v_S,a
+    double E[27];          // E[9k+3a+z]: x_T,k - v_S,a (filament: x_T,k - a, x_T,k - b)
     double D[9];           // x_T,k - c_S
     double Sd[9], Sn[3], Snu[9], Slen[3], Sarea, Sdiam;
-    float Ef[9];           // D in FP32
+    float E32[27];         // E in FP32
+    float D32[9];          // D in FP32
     float Sdf[9], Snf[3], Snuf[9], Slenf[3], Sareaf, Sdiamf;
     double leaf[LEAFBUF][10];
-    double seg[6];         // filament ends relative: x_T,k - a (9) kept in E
+    double q64[64][4];     // points waiting for FP64: barycentrics and weight
 };
 
 __device__ __forceinline__ v3<double> ld3(const double* p) { return mk3(p[0], p[1], p[2]); }
@@ -593,9 +592,10 @@ __device__ __forceinline__ v3<double> tpoint(const TriGeo& T, const double* b) {
 
 // per-lane accumulators of a pair
 struct Acc {
-    v3<double> P[3];  // triangle source: sum of W psi_a w
+    v3<double> P[3];      // triangle source: sum of W psi_a w
     double ca[3], cb[3];  // filament source: the two end parts
-    v3<float> Pf[3];
+    v3<float> Pf[3];      // FP32 partial sums, folded into P every few points
+    int nf;               // points in Pf
 };
 
 struct PairCtx {
@@ -605,10 +605,22 @@ struct PairCtx {
     int lane;
     int kind;       // 0 triangle source, 1 filament
     int side;       // 1 for the self pair
-    int leaf_fp32;  // leaves of this pair in FP32
+    int fp32;       // evaluate in FP32 with the FP64 guard (VP_MIXED, triangle sources)
     int nleaf;      // buffered leaves (uniform)
+    int nq64;       // queued FP64 points (uniform)
     long long npts; // points of this pair (uniform)
+    long long n64;  // points of this pair evaluated in FP64 (uniform)
 };
+
+__device__ __forceinline__ void fold32(Acc& acc) {
+    for (int k = 0; k < 3; ++k) {
+        acc.P[k].x += double(acc.Pf[k].x);
+        acc.P[k].y += double(acc.Pf[k].y);
+        acc.P[k].z += double(acc.Pf[k].z);
+        acc.Pf[k] = mk3(0.f, 0.f, 0.f);
+    }
+    acc.nf = 0;
+}
 
 // evaluate one point (barycentric l on T, weight W) in FP64
 __device__ __forceinline__ void eval_point64(const PairCtx& pc, Acc& acc, double l0, double l1, double l2, double W) {
@@ -649,12 +661,10 @@ __device__ __forceinline__ void eval_point64(const PairCtx& pc, Acc& acc, double
     }
 }
 
-// evaluate one point in FP32 (triangle sources of the near tier in VP_MIXED)
-__device__ __forceinline__ void eval_point32(const PairCtx& pc, Acc& acc, float l0, float l1, float l2, float W) {
+// evaluate one point in FP32 (triangle sources in VP_MIXED); false when it lies where FP32 cancels
+__device__ __forceinline__ bool eval_point32(const PairCtx& pc, Acc& acc, float l0, float l1, float l2, float W) {
+    if (pc.a->test_mode == 2) return false;  // the dual test's ties are decided in FP64
     const WarpSh& sh = *pc.sh;
-    v3<float> psi = test_weights(pc.a->test_mode, l0, l1, l2);
-    v3<float> r = l0 * mk3(sh.Ef[0], sh.Ef[1], sh.Ef[2]) + l1 * mk3(sh.Ef[3], sh.Ef[4], sh.Ef[5]) +
-                  l2 * mk3(sh.Ef[6], sh.Ef[7], sh.Ef[8]);
     SrcKern<float> S;
     for (int k = 0; k < 3; ++k) {
         S.d[k] = mk3(sh.Sdf[3 * k], sh.Sdf[3 * k + 1], sh.Sdf[3 * k + 2]);
@@ -664,25 +674,85 @@ __device__ __forceinline__ void eval_point32(const PairCtx& pc, Acc& acc, float 
     S.n = mk3(sh.Snf[0], sh.Snf[1], sh.Snf[2]);
     S.area = sh.Sareaf;
     S.diam = sh.Sdiamf;
-    v3<float> w = sv_rel(S, r, 0, float(pc.a->kernel_far), 1e-12f);
+    v3<float> r = l0 * mk3(sh.D32[0], sh.D32[1], sh.D32[2]) + l1 * mk3(sh.D32[3], sh.D32[4], sh.D32[5]) +
+                  l2 * mk3(sh.D32[6], sh.D32[7], sh.D32[8]);
+    v3<float> w;
+    float fd = float(pc.a->kernel_far) * S.diam;
+    if (dot(r, r) > fd * fd) {
+        w = sv_far(S, r);
+    } else {
+        const float* E = sh.E32;
+        v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
+        v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
+        v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
+        const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+        if (!sv_exact3_guarded(S, ra, rb, rc, pc.side, g, w)) return false;
+    }
+    v3<float> psi = pc.a->test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);
     acc.Pf[0] += (W * psi.x) * w;
     acc.Pf[1] += (W * psi.y) * w;
     acc.Pf[2] += (W * psi.z) * w;
+    if (++acc.nf == 16) fold32(acc);
+    return true;
 }
 
-// a piece carrying a whole tabulated rule: lanes stride over its points (FP64)
+// drain 32 queued FP64 points (or all of them when `all`), one per lane
+__device__ void drain64(PairCtx& pc, Acc& acc, bool all) {
+    while (pc.nq64 >= 32 || (all && pc.nq64 > 0)) {
+        __syncwarp();
+        int take = pc.nq64 < 32 ? pc.nq64 : 32;
+        if (pc.lane < take) {
+            const double* q = pc.sh->q64[pc.lane];
+            eval_point64(pc, acc, q[0], q[1], q[2], q[3]);
+        }
+        __syncwarp();
+        int rest = pc.nq64 - take;
+        if (pc.lane < rest)
+            for (int k = 0; k < 4; ++k) pc.sh->q64[pc.lane][k] = pc.sh->q64[take + pc.lane][k];
+        __syncwarp();
+        pc.nq64 = rest;
+        pc.n64 += take;
+    }
+}
+
+// one point per lane (all lanes call this together): FP64 directly, or FP32 with the guarded points queued for FP64
+__device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, double l0, double l1, double l2, double W) {
+    if (!pc.fp32) {
+        if (valid) eval_point64(pc, acc, l0, l1, l2, W);
+        return;
+    }
+    bool need = valid && !eval_point32(pc, acc, float(l0), float(l1), float(l2), float(W));
+    unsigned m = __ballot_sync(0xffffffffu, need);
+    if (m) {
+        int pos = pc.nq64 + __popc(m & ((1u << pc.lane) - 1u));
+        if (need) {
+            double* q = pc.sh->q64[pos];
+            q[0] = l0;
+            q[1] = l1;
+            q[2] = l2;
+            q[3] = W;
+        }
+        pc.nq64 += __popc(m);
+        if (pc.nq64 >= 32) drain64(pc, acc, false);
+    }
+}
+
+// a piece carrying a whole tabulated rule: lanes stride over its points
 __device__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, double frac) {
     const RulePt* R = pc.a->rule[rid];
     const int n = pc.a->nrule[rid];
     const double areaT = pc.T->area;
-    for (int i = pc.lane; i < n; i += 32) {
-        RulePt m = R[i];
+    for (int i0 = 0; i0 < n; i0 += 32) {
+        int i = i0 + pc.lane;
+        bool valid = i < n;
+        RulePt m = R[valid ? i : 0];
         double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
         double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
         double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
-        eval_point64(pc, acc, l0, l1, l2, (m.w * frac) * areaT);
+        point_step(pc, acc, valid, l0, l1, l2, (m.w * frac) * areaT);
     }
     pc.npts += n;
+    if (!pc.fp32) pc.n64 += n;
 }
 
 __device__ void flush_leaves(PairCtx& pc, Acc& acc) {
@@ -692,20 +762,19 @@ __device__ void flush_leaves(PairCtx& pc, Acc& acc) {
     const RulePt* R = pc.a->rule[R_NEAR];
     const int n = pc.a->nrule[R_NEAR];
     const double areaT = pc.T->area;
-    for (int i = pc.lane; i < nl * n; i += 32) {
-        int lf = i / n, q = i - lf * n;
+    for (int i0 = 0; i0 < nl * n; i0 += 32) {
+        int i = i0 + pc.lane;
+        bool valid = i < nl * n;
+        int lf = valid ? i / n : 0, q = valid ? i - lf * n : 0;
         const double* b = pc.sh->leaf[lf];
         RulePt m = R[q];
         double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
         double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
         double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
-        double W = (m.w * b[9]) * areaT;
-        if (pc.leaf_fp32)
-            eval_point32(pc, acc, float(l0), float(l1), float(l2), float(W));
-        else
-            eval_point64(pc, acc, l0, l1, l2, W);
+        point_step(pc, acc, valid, l0, l1, l2, (m.w * b[9]) * areaT);
     }
     pc.npts += (long long)nl * n;
+    if (!pc.fp32) pc.n64 += (long long)nl * n;
     __syncwarp();
     pc.nleaf = 0;
 }
@@ -922,19 +991,20 @@ __device__ void setup_tri_source(PairCtx& pc, const TriGeo& S) {
         const TriGeo& T = *pc.T;
         for (int k = 0; k < 3; ++k)
             for (int q = 0; q < 3; ++q)
-                for (int z = 0; z < 3; ++z) sh.E[9 * k + 3 * q + z] = T.x[3 * k + z] - S.x[3 * q + z];
+                for (int z = 0; z < 3; ++z) {
+                    sh.E[9 * k + 3 * q + z] = T.x[3 * k + z] - S.x[3 * q + z];
+                    sh.E32[9 * k + 3 * q + z] = float(sh.E[9 * k + 3 * q + z]);
+                }
         for (int k = 0; k < 3; ++k)
             for (int z = 0; z < 3; ++z) {
                 sh.D[3 * k + z] = T.x[3 * k + z] - S.c[z];
-                sh.Ef[3 * k + z] = float(sh.D[3 * k + z]);
+                sh.D32[3 * k + z] = float(sh.D[3 * k + z]);
             }
         for (int k = 0; k < 9; ++k) {
-            int q = k / 3, z = k % 3;
-            sh.Sd[k] = S.x[k] - S.c[z];
+            sh.Sd[k] = S.x[k] - S.c[k % 3];
             sh.Snu[k] = S.nu[k];
             sh.Sdf[k] = float(sh.Sd[k]);
             sh.Snuf[k] = float(S.nu[k]);
-            (void)q;
         }
         for (int k = 0; k < 3; ++k) {
             sh.Sn[k] = S.n[k];
@@ -958,8 +1028,8 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
     setup_tri_source(pc, S);
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     pc.side = (!wake && s == t) ? 1 : 0;
+    pc.fp32 = a.mixed;
     if (!wake && s == t) {
-        pc.leaf_fp32 = 0;
         emit_rule(pc, acc, R_SELF, corners, 1.0);
         return TIER_SELF;
     }
@@ -970,7 +1040,6 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
             shared[k] = T.node[k] == S.node[0] || T.node[k] == S.node[1] || T.node[k] == S.node[2];
             ns += shared[k];
         }
-    pc.leaf_fp32 = 0;
     if (contact_rule(pc, acc, S, shared)) {
         flush_leaves(pc, acc);
         return TIER_CONTACT;
@@ -1014,7 +1083,6 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
         }
         if (lo < a.ntouch && a.touch[lo] == key) depth += 4;
     }
-    pc.leaf_fp32 = a.mixed;
     SrcRef src{0, S.x, {}, {}};
     near_pieces(pc, acc, src, corners, 1.0, depth);
     flush_leaves(pc, acc);
@@ -1022,12 +1090,15 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
 }
 
 __device__ void add_block(PairCtx& pc, Acc& acc, const TriGeo& S, int col0, double* rbt, bool with_rhs) {
-    // reduce the per-lane sums, contract with n_T x gamma_b and add the block to this warp's rows
+    // finish the queued FP64 points, reduce the per-lane sums, contract with n_T x gamma_b and add the block to this
+    // warp's rows
+    drain64(pc, acc, true);
+    fold32(acc);
     double P[9];
     for (int a = 0; a < 3; ++a) {
-        P[3 * a + 0] = warp_sum(acc.P[a].x + double(acc.Pf[a].x));
-        P[3 * a + 1] = warp_sum(acc.P[a].y + double(acc.Pf[a].y));
-        P[3 * a + 2] = warp_sum(acc.P[a].z + double(acc.Pf[a].z));
+        P[3 * a + 0] = warp_sum(acc.P[a].x);
+        P[3 * a + 1] = warp_sum(acc.P[a].y);
+        P[3 * a + 2] = warp_sum(acc.P[a].z);
     }
     const TriGeo& T = *pc.T;
     v3<double> nT = ld3(T.n);
@@ -1063,8 +1134,383 @@ __device__ void vertex_rule(PairCtx& pc, Acc& acc, int k) {
     }
 }
 
+// ---- the near tier, one pair per lane ---------------------------------------------------------------------------
+// A warp takes up to 32 sources of its test triangle at once. Each lane decides its own pair's tier (FP64, exactly as
+// pair_rule / wake_pair_rule) and, for a pair in the near tier, walks near_pieces' quadtree to its leaves. The
+// warp then evaluates all leaves' points of the 32 pairs together, one point per lane (FP32, guarded; flagged points
+// are queued and evaluated 32 at a time in FP64), reduces them per pair in a fixed order and adds the blocks to A
+// pair by pair. Pairs of the other tiers are returned (a lane mask) for the warp-cooperative path.
+struct NearChunkSh {
+    uint8_t leaf[32][64];  // leaf codes: level << 6 | path (level base-4 digits, most significant first)
+    float E32[32][27];     // x_T,k - v_S,a
+    float D32[32][9];      // x_T,k - c_S
+    float S32[32][26];     // d (9), nu (9), len (3), n (3), area, diam
+    double acc[32][9];     // per pair: sum of W psi_a w
+    int off[33];           // points before each pair
+    int qp[64], qk[64];    // queued FP64 points: pair, point within the pair
+};
+
+union WarpSmem {
+    WarpSh w;
+    NearChunkSh c;
+};
+
+__device__ __forceinline__ void leaf_corners32(int code, float* b) {
+    // the corners of a quadtree node in the test triangle's barycentrics (dyadic, exact in FP32)
+    int level = code >> 6, path = code & 63;
+    float c[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int l = 0; l < level; ++l) {
+        int digit = (path >> (2 * (level - 1 - l))) & 3;
+        float m12[3], m23[3], m31[3];
+        for (int z = 0; z < 3; ++z) {
+            m12[z] = 0.5f * (c[z] + c[3 + z]);
+            m23[z] = 0.5f * (c[3 + z] + c[6 + z]);
+            m31[z] = 0.5f * (c[6 + z] + c[z]);
+        }
+        float n[9];
+        for (int z = 0; z < 3; ++z) {
+            if (digit == 0) { n[z] = c[z]; n[3 + z] = m12[z]; n[6 + z] = m31[z]; }
+            else if (digit == 1) { n[z] = m12[z]; n[3 + z] = c[3 + z]; n[6 + z] = m23[z]; }
+            else if (digit == 2) { n[z] = m31[z]; n[3 + z] = m23[z]; n[6 + z] = c[6 + z]; }
+            else { n[z] = m12[z]; n[3 + z] = m23[z]; n[6 + z] = m31[z]; }
+        }
+        for (int z = 0; z < 9; ++z) c[z] = n[z];
+    }
+    for (int z = 0; z < 9; ++z) b[z] = c[z];
+}
+
+// per-lane contributions W psi_a w_c (9 values), keyed by pair (non-decreasing over the lanes, 32+ for none):
+// segmented sums in a fixed order, added to the pairs' FP64 accumulators
+template <class V>
+__device__ __forceinline__ void seg_accumulate(NearChunkSh& ns, int lane, int key, V* v) {
+    const unsigned FULL = 0xffffffffu;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int ky = __shfl_up_sync(FULL, key, o);
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+            V y = __shfl_up_sync(FULL, v[k], o);
+            if (lane >= o && ky == key) v[k] += y;
+        }
+    }
+    int kn = __shfl_down_sync(FULL, key, 1);
+    bool last = lane == 31 || kn != key;
+    if (last && key < 32)
+        for (int k = 0; k < 9; ++k) ns.acc[key][k] += double(v[k]);
+    __syncwarp();
+}
+
+// the FP64 evaluation of point k of pair p (queued by the FP32 guard): contributions in v
+__device__ void near_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S, const NearChunkSh& ns, int p, int k,
+                             double* v) {
+    const int nr = a.nrule[R_NEAR];
+    int leaf = k / nr, q = k - leaf * nr;
+    float bf[9];
+    leaf_corners32(ns.leaf[p][leaf], bf);
+    double b[9];
+    for (int z = 0; z < 9; ++z) b[z] = double(bf[z]);
+    RulePt m = a.rule[R_NEAR][q];
+    double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
+    double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
+    double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
+    int level = ns.leaf[p][leaf] >> 6;
+    double W = (m.w * ldexp(1.0, -2 * level)) * T.area;
+    v3<double> x = mk3(l0 * T.x[0] + l1 * T.x[3] + l2 * T.x[6], l0 * T.x[1] + l1 * T.x[4] + l2 * T.x[7],
+                       l0 * T.x[2] + l1 * T.x[5] + l2 * T.x[8]);
+    v3<double> ra = mk3(l0 * (T.x[0] - S.x[0]) + l1 * (T.x[3] - S.x[0]) + l2 * (T.x[6] - S.x[0]),
+                        l0 * (T.x[1] - S.x[1]) + l1 * (T.x[4] - S.x[1]) + l2 * (T.x[7] - S.x[1]),
+                        l0 * (T.x[2] - S.x[2]) + l1 * (T.x[5] - S.x[2]) + l2 * (T.x[8] - S.x[2]));
+    v3<double> rb = mk3(l0 * (T.x[0] - S.x[3]) + l1 * (T.x[3] - S.x[3]) + l2 * (T.x[6] - S.x[3]),
+                        l0 * (T.x[1] - S.x[4]) + l1 * (T.x[4] - S.x[4]) + l2 * (T.x[7] - S.x[4]),
+                        l0 * (T.x[2] - S.x[5]) + l1 * (T.x[5] - S.x[5]) + l2 * (T.x[8] - S.x[5]));
+    v3<double> rc = mk3(l0 * (T.x[0] - S.x[6]) + l1 * (T.x[3] - S.x[6]) + l2 * (T.x[6] - S.x[6]),
+                        l0 * (T.x[1] - S.x[7]) + l1 * (T.x[4] - S.x[7]) + l2 * (T.x[7] - S.x[7]),
+                        l0 * (T.x[2] - S.x[8]) + l1 * (T.x[5] - S.x[8]) + l2 * (T.x[8] - S.x[8]));
+    v3<double> r = x - ld3(S.c);
+    SrcKern<double> K;
+    for (int z = 0; z < 3; ++z) {
+        K.d[z] = mk3(S.x[3 * z] - S.c[0], S.x[3 * z + 1] - S.c[1], S.x[3 * z + 2] - S.c[2]);
+        K.nu[z] = ld3(S.nu + 3 * z);
+        K.len[z] = S.len[z];
+    }
+    K.n = ld3(S.n);
+    K.area = S.area;
+    K.diam = S.diam;
+    double fd = a.kernel_far * K.diam;
+    v3<double> w = dot(r, r) > fd * fd ? sv_far(K, r) : sv_exact3(K, ra, rb, rc, r, 0, 1e-12);
+    v3<double> psi = test_weights(a.test_mode, l0, l1, l2);
+    double ps[3] = {W * psi.x, W * psi.y, W * psi.z};
+    for (int ai = 0; ai < 3; ++ai) {
+        v[3 * ai + 0] = ps[ai] * w.x;
+        v[3 * ai + 1] = ps[ai] * w.y;
+        v[3 * ai + 2] = ps[ai] * w.z;
+    }
+}
+
+__device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* list, int cnt, bool wake, int col0,
+                               double* rbt, unsigned long long* P, unsigned long long* Q, unsigned long long& Q64) {
+    const NearArgs& a = *pc.a;
+    const TriGeo& T = *pc.T;
+    const int lane = pc.lane;
+    const unsigned FULL = 0xffffffffu;
+    const bool valid = lane < cnt;
+    const int s = valid ? list[lane] : 0;
+    const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
+    // 1. the tier of this lane's pair
+    bool near = valid && a.test_mode != 2 && a.near_depth <= 3 && !(!wake && s == t);
+    if (near && !wake) {
+        for (int k = 0; k < 3; ++k)
+            if (T.node[k] == S.node[0] || T.node[k] == S.node[1] || T.node[k] == S.node[2]) near = false;
+        if (near && a.ntouch > 0) {
+            long long key = (long long)t * a.ntri + s;
+            int lo = 0, hi = a.ntouch;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (a.touch[mid] < key) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo < a.ntouch && a.touch[lo] == key) near = false;
+        }
+    }
+    if (near) {  // contact_rule (assemble.jl:199-207) finds no contact beyond shared corners
+        double tol = a.contact_rel * fmin(T.diam, S.diam);
+        if (!(vnorm(ld3(S.c) - ld3(T.c)) > T.reach + S.reach + tol)) {
+            bool extra = false;
+            for (int k = 0; k < 3 && !extra; ++k)
+                if (dist_tri(S.x, ld3(T.x + 3 * k)) <= tol) extra = true;
+            for (int k = 0; k < 3 && !extra; ++k)
+                for (int q = 0; q < 3 && !extra; ++q) {
+                    double tt;
+                    if (on_edge_split(ld3(S.x + 3 * q), ld3(T.x + 3 * k), ld3(T.x + 3 * ((k + 1) % 3)), tol, tt))
+                        extra = true;
+                }
+            if (extra) near = false;
+        }
+    }
+    // 2. near_pieces' leaves (assemble.jl:131-142)
+    int nleaf = 0;
+    if (near) {
+        const int depth = a.near_depth;
+        int level = 0;
+        unsigned path = 0;
+        for (int guard = 0; guard < 1024; ++guard) {
+            double b[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+            for (int l = 0; l < level; ++l) {
+                int digit = (path >> (2 * (level - 1 - l))) & 3;
+                double m12[3], m23[3], m31[3], nb[9];
+                bmix(m12, b, 0.5, b + 3, 0.5);
+                bmix(m23, b + 3, 0.5, b + 6, 0.5);
+                bmix(m31, b + 6, 0.5, b, 0.5);
+                const double *c0, *c1, *c2;
+                if (digit == 0) { c0 = b; c1 = m12; c2 = m31; }
+                else if (digit == 1) { c0 = m12; c1 = b + 3; c2 = m23; }
+                else if (digit == 2) { c0 = m31; c1 = m23; c2 = b + 6; }
+                else { c0 = m12; c1 = m23; c2 = m31; }
+                for (int z = 0; z < 3; ++z) {
+                    nb[z] = c0[z];
+                    nb[3 + z] = c1[z];
+                    nb[6 + z] = c2[z];
+                }
+                for (int z = 0; z < 9; ++z) b[z] = nb[z];
+            }
+            v3<double> p1 = tpoint(T, b), p2 = tpoint(T, b + 3), p3 = tpoint(T, b + 6);
+            double size = fmax(vnorm(p2 - p1), fmax(vnorm(p3 - p2), vnorm(p1 - p3)));
+            if (level < depth && dist_tri(S.x, (p1 + p2 + p3) / 3.0) < a.near_ratio * size) {
+                level++;
+                path *= 4;
+                continue;
+            }
+            ns.leaf[lane][nleaf++] = uint8_t((level << 6) | path);
+            while (level > 0 && (path & 3) == 3) {
+                path >>= 2;
+                level--;
+            }
+            if (level == 0) break;
+            path++;
+        }
+        for (int k = 0; k < 3; ++k)
+            for (int q = 0; q < 3; ++q)
+                for (int z = 0; z < 3; ++z) ns.E32[lane][9 * k + 3 * q + z] = float(T.x[3 * k + z] - S.x[3 * q + z]);
+        for (int k = 0; k < 3; ++k)
+            for (int z = 0; z < 3; ++z) ns.D32[lane][3 * k + z] = float(T.x[3 * k + z] - S.c[z]);
+        for (int k = 0; k < 9; ++k) {
+            ns.S32[lane][k] = float(S.x[k] - S.c[k % 3]);
+            ns.S32[lane][9 + k] = float(S.nu[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            ns.S32[lane][18 + k] = float(S.len[k]);
+            ns.S32[lane][21 + k] = float(S.n[k]);
+        }
+        ns.S32[lane][24] = float(S.area);
+        ns.S32[lane][25] = float(S.diam);
+    }
+    for (int k = 0; k < 9; ++k) ns.acc[lane][k] = 0.0;
+    const int nr = a.nrule[R_NEAR];
+    int incl = near ? nleaf * nr : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    ns.off[lane + 1] = incl;
+    if (lane == 0) ns.off[0] = 0;
+    const int total = __shfl_sync(FULL, incl, 31);
+    const unsigned nearmask = __ballot_sync(FULL, near);
+    __syncwarp();
+    // 3. every leaf point of the chunk, one per lane
+    const float kf = float(a.kernel_far), areaT = float(T.area);
+    const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+    int nq = 0;
+    unsigned long long n64 = 0;
+    for (int i0 = 0; i0 < total; i0 += 32) {
+        const int i = i0 + lane;
+        const bool v = i < total;
+        int p = 32 + lane, k = 0;
+        float vals[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+        bool need = false;
+        if (v && !a.mixed) {  // FP64: every point through the FP64 queue
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (ns.off[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            p = lo;
+            k = i - ns.off[p];
+            need = true;
+        } else if (v) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (ns.off[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            p = lo;
+            k = i - ns.off[p];
+            int leaf = k / nr, q = k - leaf * nr;
+            int code = ns.leaf[p][leaf];
+            float b[9];
+            leaf_corners32(code, b);
+            RulePt m = a.rule[R_NEAR][q];
+            float m0 = float(m.l0), m1 = float(m.l1), m2 = float(m.l2);
+            float l0 = m0 * b[0] + m1 * b[3] + m2 * b[6];
+            float l1 = m0 * b[1] + m1 * b[4] + m2 * b[7];
+            float l2 = m0 * b[2] + m1 * b[5] + m2 * b[8];
+            float W = float(m.w) * ldexpf(1.f, -2 * (code >> 6)) * areaT;
+            const float* E = ns.E32[p];
+            const float* Dp = ns.D32[p];
+            const float* Sf = ns.S32[p];
+            SrcKern<float> K;
+            for (int z = 0; z < 3; ++z) {
+                K.d[z] = mk3(Sf[3 * z], Sf[3 * z + 1], Sf[3 * z + 2]);
+                K.nu[z] = mk3(Sf[9 + 3 * z], Sf[10 + 3 * z], Sf[11 + 3 * z]);
+                K.len[z] = Sf[18 + z];
+            }
+            K.n = mk3(Sf[21], Sf[22], Sf[23]);
+            K.area = Sf[24];
+            K.diam = Sf[25];
+            v3<float> r = l0 * mk3(Dp[0], Dp[1], Dp[2]) + l1 * mk3(Dp[3], Dp[4], Dp[5]) + l2 * mk3(Dp[6], Dp[7], Dp[8]);
+            v3<float> w;
+            float fd = kf * K.diam;
+            bool ok = true;
+            if (dot(r, r) > fd * fd) {
+                w = sv_far(K, r);
+            } else {
+                v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
+                v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
+                v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
+                ok = sv_exact3_guarded(K, ra, rb, rc, 0, g, w);
+            }
+            if (ok) {
+                v3<float> psi = a.test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);
+                float ps[3] = {W * psi.x, W * psi.y, W * psi.z};
+                for (int ai = 0; ai < 3; ++ai) {
+                    vals[3 * ai + 0] = ps[ai] * w.x;
+                    vals[3 * ai + 1] = ps[ai] * w.y;
+                    vals[3 * ai + 2] = ps[ai] * w.z;
+                }
+            } else {
+                need = true;
+            }
+        }
+        if (a.mixed) seg_accumulate(ns, lane, p, vals);  // flagged points add zero here, their FP64 value when drained
+        unsigned m = __ballot_sync(FULL, need);
+        if (m) {
+            int pos = nq + __popc(m & ((1u << lane) - 1u));
+            if (need) {
+                ns.qp[pos] = p;
+                ns.qk[pos] = k;
+            }
+            nq += __popc(m);
+            __syncwarp();
+        }
+        while (nq >= 32 || (nq > 0 && i0 + 32 >= total)) {
+            const int take = nq < 32 ? nq : 32;
+            int qpair = 32 + lane;
+            double qv[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+            if (lane < take) {
+                qpair = ns.qp[lane];
+                const TriGeo& Sq = wake ? a.wtri[list[qpair]] : a.tri[list[qpair]];
+                near_point64(a, T, Sq, ns, qpair, ns.qk[lane], qv);
+            }
+            seg_accumulate(ns, lane, qpair, qv);
+            const int rest = nq - take;
+            int mp = 0, mk = 0;
+            if (lane < rest) {
+                mp = ns.qp[take + lane];
+                mk = ns.qk[take + lane];
+            }
+            __syncwarp();
+            if (lane < rest) {
+                ns.qp[lane] = mp;
+                ns.qk[lane] = mk;
+            }
+            __syncwarp();
+            nq = rest;
+            n64 += take;
+        }
+    }
+    __syncwarp();
+    // 4. the pairs' blocks, added pair by pair in source order
+    double blk[9], rb[3] = {0, 0, 0};
+    if (near) {
+        v3<double> nT = ld3(T.n);
+        for (int bb = 0; bb < 3; ++bb) {
+            v3<double> mv = cross(nT, ld3(S.gam + 3 * bb));
+            for (int ai = 0; ai < 3; ++ai)
+                blk[3 * ai + bb] = ns.acc[lane][3 * ai] * mv.x + ns.acc[lane][3 * ai + 1] * mv.y +
+                                   ns.acc[lane][3 * ai + 2] * mv.z;
+        }
+        for (int ai = 0; ai < 3; ++ai)
+            rb[ai] = -S.sigma * (ns.acc[lane][3 * ai] * nT.x + ns.acc[lane][3 * ai + 1] * nT.y +
+                                 ns.acc[lane][3 * ai + 2] * nT.z);
+    }
+    for (int k = 0; k < cnt; ++k) {
+        if (!((nearmask >> k) & 1u)) continue;
+        double vk[9];
+        for (int z = 0; z < 9; ++z) vk[z] = __shfl_sync(FULL, blk[z], k);
+        if (!wake)
+            for (int z = 0; z < 3; ++z) rbt[z] += __shfl_sync(FULL, rb[z], k);
+        if (lane < 9) {
+            int ai = lane / 3, bb = lane % 3;
+            const TriGeo& Sk = wake ? a.wtri[list[k]] : a.tri[list[k]];
+            double* dst = a.A + size_t(T.slot[ai]) * size_t(a.lda) + col0 + Sk.slot[bb];
+            double val = vk[0];
+            for (int z = 1; z < 9; ++z)
+                if (z == lane) val = vk[z];
+            *dst += val;
+        }
+        __syncwarp();
+    }
+    P[TIER_NEAR] += __popc(nearmask);
+    Q[TIER_NEAR] += (unsigned long long)total;
+    Q64 += n64;
+    return __ballot_sync(FULL, valid && !near);
+}
+
 __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
-    __shared__ WarpSh shm[NEAR_WARPS];
+    extern __shared__ __align__(16) unsigned char near_smem[];
+    WarpSmem* shm = reinterpret_cast<WarpSmem*>(near_smem);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int idx = blockIdx.x * NEAR_WARPS + w;
     if (idx >= a.ntests) return;
@@ -1073,33 +1519,42 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
     PairCtx pc;
     pc.a = &a;
     pc.T = &T;
-    pc.sh = &shm[w];
+    pc.sh = &shm[w].w;
     pc.lane = lane;
     pc.nleaf = 0;
-    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0};
+    pc.nq64 = 0;
+    pc.fp32 = 0;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
     double rbt[3] = {0, 0, 0};
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    // body sources (assemble.jl:408-419)
-    for (long long e = a.nf_ptr[t]; e < a.nf_ptr[t + 1]; ++e) {
-        int s = a.nf_src[e];
-        Acc acc = {};
-        pc.kind = 0;
-        pc.npts = 0;
-        int tier = tri_pair(pc, acc, t, s, false);
-        add_block(pc, acc, a.tri[s], 0, rbt, true);
-        P[tier] += 1;
-        Q[tier] += pc.npts;
-    }
-    // wake sheets (add_wake!, assemble.jl:333-343): wake_pair_rule, no shared corners
-    for (long long e = a.wf_ptr[t]; e < a.wf_ptr[t + 1]; ++e) {
-        int s = a.wf_src[e];
-        Acc acc = {};
-        pc.kind = 0;
-        pc.npts = 0;
-        int tier = tri_pair(pc, acc, t, s, true);
-        add_block(pc, acc, a.wtri[s], a.nslot, rbt, false);
-        P[tier] += 1;
-        Q[tier] += pc.npts;
+    // body sources (assemble.jl:408-419), then the wake's sheets (add_wake!, assemble.jl:333-343)
+    for (int set = 0; set < 2; ++set) {
+        const bool wake = set == 1;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t], e1 = wake ? a.wf_ptr[t + 1] : a.nf_ptr[t + 1];
+        const int* src = wake ? a.wf_src : a.nf_src;
+        const int col0 = wake ? a.nslot : 0;
+        for (long long c0 = e0; c0 < e1; c0 += 32) {
+            const int cnt = int(e1 - c0 < 32 ? e1 - c0 : 32);
+            unsigned rest = near_chunk(pc, shm[w].c, t, src + c0, cnt, wake, col0, rbt, P, Q, Q64);
+            __syncwarp();
+            while (rest) {
+                const int k = __ffs(rest) - 1;
+                rest &= rest - 1;
+                const int s = src[c0 + k];
+                Acc acc = {};
+                pc.kind = 0;
+                pc.npts = 0;
+                pc.n64 = 0;
+                pc.nleaf = 0;
+                pc.nq64 = 0;
+                int tier = tri_pair(pc, acc, t, s, wake);
+                add_block(pc, acc, wake ? a.wtri[s] : a.tri[s], col0, rbt, !wake);
+                P[tier] += 1;
+                Q[tier] += pc.npts;
+                Q64 += pc.n64;
+            }
+            __syncwarp();
+        }
     }
     // tip filaments (assemble.jl:344-354): segment_rule (:299-306) and segment_block (:312-321), FP64
     for (int f = 0; f < a.nfil; ++f) {
@@ -1119,8 +1574,9 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
         Acc acc = {};
         pc.kind = 1;
         pc.npts = 0;
+        pc.n64 = 0;
         pc.side = 0;
-        pc.leaf_fp32 = 0;
+        pc.fp32 = 0;
         double L = vnorm(fb - fa);
         int tier;
         if (vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, L)) {
@@ -1154,6 +1610,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
         __syncwarp();
         P[tier] += 1;
         Q[tier] += pc.npts;
+        Q64 += pc.n64;
     }
     // freestream, exact (assemble.jl:422), and the rows of b
     if (lane == 0) {
@@ -1163,6 +1620,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
             if (P[k]) atomicAdd(a.stats + k, P[k]);
             if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
         }
+        if (Q64) atomicAdd(a.stats + 12, Q64);
     }
 }
 
@@ -1569,8 +2027,8 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
 
     // near, touching and contact tiers, one launch per colour of test triangles
     unsigned long long* d_stats;
-    if ((r = dl.alloc(ctx, &d_stats, 12))) { vp_system_free(sys); return r; }
-    VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 12, ctx->stream));
+    if ((r = dl.alloc(ctx, &d_stats, 13))) { vp_system_free(sys); return r; }
+    VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
     {
         std::vector<std::vector<int>> groups(ntri);
         for (int t = 0; t < ntri; ++t) groups[t] = {corner_slot[3 * t], corner_slot[3 * t + 1], corner_slot[3 * t + 2]};
@@ -1630,19 +2088,21 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         }
         na.stats = d_stats;
         vp_phase_begin(ctx, PH_NEAR);
+        const size_t near_smem = sizeof(WarpSmem) * NEAR_WARPS;
+        VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(near_smem)));
         for (size_t c = 0; c < colours.size(); ++c) {
             na.tests = d_tests + off[c];
             na.ntests = off[c + 1] - off[c];
             int nb = (na.ntests + NEAR_WARPS - 1) / NEAR_WARPS;
             if (nb) {
-                near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+                near_kernel<<<nb, 32 * NEAR_WARPS, near_smem, ctx->stream>>>(na);
                 ctx->launches++;
             }
         }
         vp_phase_end(ctx);
         VP_CUDA(ctx, cudaGetLastError());
     }
-    unsigned long long hs[12];
+    unsigned long long hs[13];
     VP_CUDA(ctx, vp_d2h(ctx, hs, d_stats, sizeof(hs)));
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
@@ -1661,6 +2121,7 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         long long far_tri = total - nonfar - far_fil;
         stats->pairs[TIER_FAR] = far_tri + far_fil;
         stats->points[TIER_FAR] = (long long)hs[6 + TIER_FAR] + far_tri * nq;
+        stats->points_fp64 = (long long)hs[12] + (mixed ? 0 : far_tri * nq);
         stats->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     }
     *out = sys;

@@ -49,16 +49,6 @@ struct SrcKern {
     T area, diam;
 };
 
-// edge_log (source_triangle.jl:39-44): ln((r_i + r_j + d)^2 / (2(r_i r_j + ri.rj))), cancellation-free denominator
-template <class T>
-__device__ __forceinline__ T edge_log(v3<T> ri, v3<T> rj, T d) {
-    T a = vnorm(ri), b = vnorm(rj);
-    T p = dot(ri, rj);
-    T s2d2 = p < T(0) ? T(2) * norm2(cross(ri, rj)) / (a * b - p) : T(2) * (a * b + p);
-    T num = a + b + d;
-    return vlog(num * num / s2d2);
-}
-
 // inplane_fraction (source_triangle.jl:52-64) with the vertices given relative to the point (q_k = v_k - x)
 template <class T>
 __device__ T inplane_fraction_rel(const v3<T> q[3], v3<T> n, T area, T tol) {
@@ -79,25 +69,80 @@ __device__ T inplane_fraction_rel(const v3<T> q[3], v3<T> n, T area, T tol) {
     return vacos(cs) / (T(2) * vp_pi<T>());
 }
 
+// edge_log with the distances to the edge's ends given: ln((r_i + r_j + d)^2 / (2(r_i r_j + ri.rj))), the denominator
+// formed without cancellation as |ri x rj|^2 / (r_i r_j - ri.rj) when ri.rj < 0 (source_triangle.jl:39-44)
+template <class T>
+__device__ __forceinline__ T edge_log_n(v3<T> ri, v3<T> rj, T li, T lj, T d) {
+    T p = dot(ri, rj);
+    T num = li + lj + d;
+    T q = p < T(0) ? (li * lj - p) / (T(2) * norm2(cross(ri, rj))) : T(1) / (T(2) * (li * lj + p));
+    return vlog(num * num * q);
+}
+
 // source_velocity_exact (source_triangle.jl:75-89) from the point's offsets to the three vertices ra, rb, rc
 // (r_a = x - v_a) and to the centroid r = x - c.
 template <class T>
 __device__ __forceinline__ v3<T> sv_exact3(const SrcKern<T>& S, v3<T> ra, v3<T> rb, v3<T> rc, v3<T> r, int side,
                                            T plane_tol) {
-    v3<T> wt = edge_log(ra, rb, S.len[0]) * S.nu[0] + edge_log(rb, rc, S.len[1]) * S.nu[1] +
-               edge_log(rc, ra, S.len[2]) * S.nu[2];
+    T la = vnorm(ra), lb = vnorm(rb), lc = vnorm(rc);
+    v3<T> wt = edge_log_n(ra, rb, la, lb, S.len[0]) * S.nu[0] + edge_log_n(rb, rc, lb, lc, S.len[1]) * S.nu[1] +
+               edge_log_n(rc, ra, lc, la, S.len[2]) * S.nu[2];
     T z = dot(r, S.n);
     T Om;
     if (fabs(z) <= plane_tol * S.diam) {
         v3<T> q[3] = {-ra, -rb, -rc};
         Om = side == 0 ? T(0) : T(side) * T(2) * vp_pi<T>() * inplane_fraction_rel(q, S.n, S.area, plane_tol);
     } else {
-        T la = vnorm(ra), lb = vnorm(rb), lc = vnorm(rc);
         T N = dot(ra, cross(rb, rc));
         T D = la * lb * lc + dot(ra, rb) * lc + dot(ra, rc) * lb + dot(rb, rc) * la;
         Om = T(2) * vatan2(N, D);
     }
     return (wt + Om * S.n) * (T(1) / (T(4) * vp_pi<T>()));
+}
+
+// The exact kernel in FP32 where FP32 is accurate, for a point off the source's singular set: returns false (and
+// leaves w unset) when the point is near a corner, next to an edge segment (the offsets to its ends nearly
+// antiparallel), or near the plane over the triangle (the branch of the solid angle), where the log/atan forms
+// cancel and the point must be evaluated in FP64. side != 0 marks the self pair (coplanar, interior points).
+struct Fp32Guard {
+    float corner, edge_sin2, plane;
+};
+
+__device__ __forceinline__ bool sv_exact3_guarded(const SrcKern<float>& S, v3<float> ra, v3<float> rb, v3<float> rc,
+                                                  int side, const Fp32Guard& g, v3<float>& w) {
+    float la = vnorm(ra), lb = vnorm(rb), lc = vnorm(rc);
+    if (fminf(la, fminf(lb, lc)) < g.corner * S.diam) return false;
+    const v3<float> R[3] = {ra, rb, rc};
+    const float L[3] = {la, lb, lc};
+    v3<float> wt = mk3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        v3<float> ri = R[e], rj = R[(e + 1) % 3];
+        float li = L[e], lj = L[(e + 1) % 3];
+        float p = dot(ri, rj);
+        float num = li + lj + S.len[e];
+        float q;
+        if (p < 0.f) {
+            float c2 = norm2(cross(ri, rj));
+            if (c2 < g.edge_sin2 * (li * li) * (lj * lj)) return false;
+            q = (li * lj - p) / (2.f * c2);
+        } else {
+            q = 1.f / (2.f * (li * lj + p));
+        }
+        wt += logf(num * num * q) * S.nu[e];
+    }
+    float Om;
+    if (side != 0) {
+        Om = float(side) * 2.f * vp_pi<float>();
+    } else {
+        float P3 = la * lb * lc;
+        float N = dot(ra, cross(rb, rc));
+        float D = P3 + dot(ra, rb) * lc + dot(ra, rc) * lb + dot(rb, rc) * la;
+        if (fabsf(N) < g.plane * P3 && (D < 0.f || fabsf(D) < g.plane * P3)) return false;
+        Om = 2.f * atan2f(N, D);
+    }
+    w = (wt + Om * S.n) * (1.f / (4.f * vp_pi<float>()));
+    return true;
 }
 
 // source_velocity_far (source_triangle.jl:100-119): monopole + quadrupole + octupole about the centroid

@@ -25,7 +25,8 @@ class vp_assembly_options(ctypes.Structure):
 
 
 class vp_assembly_stats(ctypes.Structure):
-    _fields_ = [("pairs", ctypes.c_longlong * 6), ("points", ctypes.c_longlong * 6), ("time_ms", ctypes.c_double)]
+    _fields_ = [("pairs", ctypes.c_longlong * 6), ("points", ctypes.c_longlong * 6), ("time_ms", ctypes.c_double),
+                ("points_fp64", ctypes.c_longlong)]
 
 
 # (name, restype, argtypes) of every entry point declared in include/vortexpanel_gpu.h

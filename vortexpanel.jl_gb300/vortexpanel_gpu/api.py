@@ -177,7 +177,7 @@ def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, 
                                     nw, pwx, nwt, pwt, nf, pwf, ctypes.byref(h), ctypes.byref(st)))
     A = DeviceSystem(ctx, h, dm.nslot, dm.nslot + nw)
     stats = {"pairs": dict(zip(TIER_NAMES, list(st.pairs))), "points": dict(zip(TIER_NAMES, list(st.points))),
-             "time": st.time_ms / 1e3}
+             "time": st.time_ms / 1e3, "points_fp64": st.points_fp64}
     return A, A.rhs(), stats
 
 
