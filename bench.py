@@ -29,7 +29,7 @@ sys.path.insert(0, os.path.join(ROOT, "vortexpanel.jl_gb300"))
 
 METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|<1e-6"
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
-SIZES = {"wing25k": (112, 56), "small": (28, 14)}  # panels per side: chordwise, spanwise
+SIZES = {"wing25k": (112, 56), "medium": (56, 28), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
 
 def workload(name="wing25k"):
@@ -184,7 +184,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--workload", default="wing25k", choices=list(SIZES),
-                    help="wing25k (the measured configuration) or small (28x14 panels per side, for profiler captures)")
+                    help="wing25k (the measured configuration); medium (56x28 per side) and small (28x14) for profiler captures")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup(args.gpus)
     w, wake, W, V, eL = workload(args.workload)

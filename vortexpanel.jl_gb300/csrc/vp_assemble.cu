@@ -510,9 +510,13 @@ struct NearArgs {
     const int* nf_src;
     const long long* wf_ptr;
     const int* wf_src;
+    int* rest_src;   // per test, at the offsets of nf_src: the body sources left to the warp-cooperative path
+    int* wrest_src;  // the same for the wake sources
+    int* rest_cnt;   // per test: counts of both (2 x ntri)
     const long long* touch;  // sorted keys t * ntri + s
     int ntouch;
     const RulePt* rule[5];
+    const float4* rulef[5];  // the same rules in FP32 (l0, l1, l2, w)
     int nrule[5];
     double* A;
     long long lda;
@@ -538,7 +542,7 @@ struct WarpSh {
     float D32[9];          // D in FP32
     float Sdf[9], Snf[3], Snuf[9], Slenf[3], Sareaf, Sdiamf;
     double leaf[LEAFBUF][10];
-    double q64[64][4];     // points waiting for FP64: barycentrics and weight
+    int qi[64], ql[64];    // points waiting for FP64: rule point, and leaf (-1: the current piece)
 };
 
 __device__ __forceinline__ v3<double> ld3(const double* p) { return mk3(p[0], p[1], p[2]); }
@@ -571,6 +575,32 @@ __device__ double dist_tri(const double* X, v3<double> p) {
     double denom = 1 / (va + vb + vc);
     return vnorm(p - (a + (vb * denom) * ab + (vc * denom) * ac));
 }
+
+// distance_to on corners a, b, c given as vectors (any frame, any precision)
+template <class T>
+__device__ T dist_tri_v(v3<T> a, v3<T> b, v3<T> c, v3<T> p) {
+    v3<T> ab = b - a, ac = c - a, ap = p - a;
+    T d1 = dot(ab, ap), d2 = dot(ac, ap);
+    if (d1 <= T(0) && d2 <= T(0)) return vnorm(ap);
+    v3<T> bp = p - b;
+    T d3 = dot(ab, bp), d4 = dot(ac, bp);
+    if (d3 >= T(0) && d4 <= d3) return vnorm(bp);
+    T vc = d1 * d4 - d3 * d2;
+    if (vc <= T(0) && d1 >= T(0) && d3 <= T(0)) return vnorm(p - (a + (d1 / (d1 - d3)) * ab));
+    v3<T> cp = p - c;
+    T d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d6 >= T(0) && d5 <= d6) return vnorm(cp);
+    T vb = d5 * d2 - d1 * d6;
+    if (vb <= T(0) && d2 >= T(0) && d6 <= T(0)) return vnorm(p - (a + (d2 / (d2 - d6)) * ac));
+    T va = d3 * d6 - d5 * d4;
+    if (va <= T(0) && d4 - d3 >= T(0) && d5 - d6 >= T(0))
+        return vnorm(p - (b + ((d4 - d3) / ((d4 - d3) + (d5 - d6))) * (c - b)));
+    T denom = T(1) / (va + vb + vc);
+    return vnorm(p - (a + (vb * denom) * ab + (vc * denom) * ac));
+}
+
+// outcome of a comparison x < y decided in FP32 with absolute error bound e: 1 true, 0 false, -1 undecided
+__device__ __forceinline__ int lt32(float x, float y, float e) { return x < y - e ? 1 : (x > y + e ? 0 : -1); }
 
 struct SrcRef {  // a source for distance tests: a triangle (X) or a segment (a, b)
     int kind;    // 0 triangle, 1 segment
@@ -696,61 +726,87 @@ __device__ __forceinline__ bool eval_point32(const PairCtx& pc, Acc& acc, float 
     return true;
 }
 
-// drain 32 queued FP64 points (or all of them when `all`), one per lane
-__device__ void drain64(PairCtx& pc, Acc& acc, bool all) {
+// FP64 evaluation of the queued points, 32 at a time (all of them when `all`): rule point qi of the current piece
+// (corners b, fraction frac) or of buffered leaf ql
+__device__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* b, double frac) {
+    const RulePt* R = pc.a->rule[rid];
+    const double areaT = pc.T->area;
     while (pc.nq64 >= 32 || (all && pc.nq64 > 0)) {
         __syncwarp();
         int take = pc.nq64 < 32 ? pc.nq64 : 32;
         if (pc.lane < take) {
-            const double* q = pc.sh->q64[pc.lane];
-            eval_point64(pc, acc, q[0], q[1], q[2], q[3]);
+            int i = pc.sh->qi[pc.lane], lf = pc.sh->ql[pc.lane];
+            const double* c = lf < 0 ? b : pc.sh->leaf[lf];
+            double fr = lf < 0 ? frac : pc.sh->leaf[lf][9];
+            RulePt m = R[i];
+            double l0 = m.l0 * c[0] + m.l1 * c[3] + m.l2 * c[6];
+            double l1 = m.l0 * c[1] + m.l1 * c[4] + m.l2 * c[7];
+            double l2 = m.l0 * c[2] + m.l1 * c[5] + m.l2 * c[8];
+            eval_point64(pc, acc, l0, l1, l2, (m.w * fr) * areaT);
         }
         __syncwarp();
         int rest = pc.nq64 - take;
-        if (pc.lane < rest)
-            for (int k = 0; k < 4; ++k) pc.sh->q64[pc.lane][k] = pc.sh->q64[take + pc.lane][k];
+        int mi = 0, ml = 0;
+        if (pc.lane < rest) {
+            mi = pc.sh->qi[take + pc.lane];
+            ml = pc.sh->ql[take + pc.lane];
+        }
+        __syncwarp();
+        if (pc.lane < rest) {
+            pc.sh->qi[pc.lane] = mi;
+            pc.sh->ql[pc.lane] = ml;
+        }
         __syncwarp();
         pc.nq64 = rest;
         pc.n64 += take;
     }
 }
 
-// one point per lane (all lanes call this together): FP64 directly, or FP32 with the guarded points queued for FP64
-__device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, double l0, double l1, double l2, double W) {
+// one point per lane (all lanes call this together). FP64: evaluated at once from the FP64 barycentrics. FP32: the
+// FP32 barycentrics are evaluated under the guard; guarded points are queued (rule point i, leaf lf) for drain64.
+__device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, int rid, int i, int lf, const double* b,
+                                           const float* bf, double frac) {
     if (!pc.fp32) {
-        if (valid) eval_point64(pc, acc, l0, l1, l2, W);
+        if (valid) {
+            RulePt m = pc.a->rule[rid][i];
+            double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
+            double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
+            double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
+            eval_point64(pc, acc, l0, l1, l2, (m.w * frac) * pc.T->area);
+        }
         return;
     }
-    bool need = valid && !eval_point32(pc, acc, float(l0), float(l1), float(l2), float(W));
-    unsigned m = __ballot_sync(0xffffffffu, need);
-    if (m) {
-        int pos = pc.nq64 + __popc(m & ((1u << pc.lane) - 1u));
+    bool need = false;
+    if (valid) {
+        float4 m = pc.a->rulef[rid][i];
+        float l0 = m.x * bf[0] + m.y * bf[3] + m.z * bf[6];
+        float l1 = m.x * bf[1] + m.y * bf[4] + m.z * bf[7];
+        float l2 = m.x * bf[2] + m.y * bf[5] + m.z * bf[8];
+        need = !eval_point32(pc, acc, l0, l1, l2, m.w * bf[9]);
+    }
+    unsigned msk = __ballot_sync(0xffffffffu, need);
+    if (msk) {
+        int pos = pc.nq64 + __popc(msk & ((1u << pc.lane) - 1u));
         if (need) {
-            double* q = pc.sh->q64[pos];
-            q[0] = l0;
-            q[1] = l1;
-            q[2] = l2;
-            q[3] = W;
+            pc.sh->qi[pos] = i;
+            pc.sh->ql[pos] = lf;
         }
-        pc.nq64 += __popc(m);
-        if (pc.nq64 >= 32) drain64(pc, acc, false);
+        pc.nq64 += __popc(msk);
     }
 }
 
 // a piece carrying a whole tabulated rule: lanes stride over its points
 __device__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, double frac) {
-    const RulePt* R = pc.a->rule[rid];
     const int n = pc.a->nrule[rid];
-    const double areaT = pc.T->area;
+    float bf[10];
+    for (int z = 0; z < 9; ++z) bf[z] = float(b[z]);
+    bf[9] = float(frac * pc.T->area);
     for (int i0 = 0; i0 < n; i0 += 32) {
         int i = i0 + pc.lane;
-        bool valid = i < n;
-        RulePt m = R[valid ? i : 0];
-        double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
-        double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
-        double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
-        point_step(pc, acc, valid, l0, l1, l2, (m.w * frac) * areaT);
+        point_step(pc, acc, i < n, rid, i < n ? i : 0, -1, b, bf, frac);
+        if (pc.nq64 >= 32) drain64(pc, acc, false, rid, b, frac);
     }
+    drain64(pc, acc, true, rid, b, frac);
     pc.npts += n;
     if (!pc.fp32) pc.n64 += n;
 }
@@ -759,20 +815,19 @@ __device__ void flush_leaves(PairCtx& pc, Acc& acc) {
     const int nl = pc.nleaf;
     if (nl == 0) return;
     __syncwarp();
-    const RulePt* R = pc.a->rule[R_NEAR];
     const int n = pc.a->nrule[R_NEAR];
-    const double areaT = pc.T->area;
     for (int i0 = 0; i0 < nl * n; i0 += 32) {
         int i = i0 + pc.lane;
         bool valid = i < nl * n;
         int lf = valid ? i / n : 0, q = valid ? i - lf * n : 0;
         const double* b = pc.sh->leaf[lf];
-        RulePt m = R[q];
-        double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
-        double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
-        double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
-        point_step(pc, acc, valid, l0, l1, l2, (m.w * b[9]) * areaT);
+        float bf[10];
+        for (int z = 0; z < 9; ++z) bf[z] = float(b[z]);
+        bf[9] = float(b[9] * pc.T->area);
+        point_step(pc, acc, valid, R_NEAR, q, lf, b, bf, b[9]);
+        if (pc.nq64 >= 32) drain64(pc, acc, false, R_NEAR, nullptr, 0.0);
     }
+    drain64(pc, acc, true, R_NEAR, nullptr, 0.0);
     pc.npts += (long long)nl * n;
     if (!pc.fp32) pc.n64 += (long long)nl * n;
     __syncwarp();
@@ -1090,9 +1145,7 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
 }
 
 __device__ void add_block(PairCtx& pc, Acc& acc, const TriGeo& S, int col0, double* rbt, bool with_rhs) {
-    // finish the queued FP64 points, reduce the per-lane sums, contract with n_T x gamma_b and add the block to this
-    // warp's rows
-    drain64(pc, acc, true);
+    // reduce the per-lane sums, contract with n_T x gamma_b and add the block to this warp's rows
     fold32(acc);
     double P[9];
     for (int a = 0; a < 3; ++a) {
@@ -1145,14 +1198,10 @@ struct NearChunkSh {
     float E32[32][27];     // x_T,k - v_S,a
     float D32[32][9];      // x_T,k - c_S
     float S32[32][26];     // d (9), nu (9), len (3), n (3), area, diam
-    double acc[32][9];     // per pair: sum of W psi_a w
+    double acc[32][9];     // per pair: sum of W psi_a w (FP64 evaluations)
+    float accf[32][9];     // per pair: the same sums of the FP32 evaluations
     int off[33];           // points before each pair
     int qp[64], qk[64];    // queued FP64 points: pair, point within the pair
-};
-
-union WarpSmem {
-    WarpSh w;
-    NearChunkSh c;
 };
 
 __device__ __forceinline__ void leaf_corners32(int code, float* b) {
@@ -1195,8 +1244,12 @@ __device__ __forceinline__ void seg_accumulate(NearChunkSh& ns, int lane, int ke
     }
     int kn = __shfl_down_sync(FULL, key, 1);
     bool last = lane == 31 || kn != key;
-    if (last && key < 32)
-        for (int k = 0; k < 9; ++k) ns.acc[key][k] += double(v[k]);
+    if (last && key < 32) {
+        if (sizeof(V) == 4)
+            for (int k = 0; k < 9; ++k) ns.accf[key][k] += float(v[k]);
+        else
+            for (int k = 0; k < 9; ++k) ns.acc[key][k] += double(v[k]);
+    }
     __syncwarp();
 }
 
@@ -1272,50 +1325,93 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
             if (lo < a.ntouch && a.touch[lo] == key) near = false;
         }
     }
-    if (near) {  // contact_rule (assemble.jl:199-207) finds no contact beyond shared corners
-        double tol = a.contact_rel * fmin(T.diam, S.diam);
-        if (!(vnorm(ld3(S.c) - ld3(T.c)) > T.reach + S.reach + tol)) {
-            bool extra = false;
-            for (int k = 0; k < 3 && !extra; ++k)
-                if (dist_tri(S.x, ld3(T.x + 3 * k)) <= tol) extra = true;
-            for (int k = 0; k < 3 && !extra; ++k)
-                for (int q = 0; q < 3 && !extra; ++q) {
-                    double tt;
-                    if (on_edge_split(ld3(S.x + 3 * q), ld3(T.x + 3 * k), ld3(T.x + 3 * ((k + 1) % 3)), tol, tt))
-                        extra = true;
-                }
-            if (extra) near = false;
+    // FP32 frame of this pair: S's corner 0 at the origin (differences taken in FP64); e32 bounds the FP32 rounding
+    v3<float> sv[3], tv[3];
+    float e32 = 0.f;
+    if (near) {
+        for (int q = 0; q < 3; ++q) {
+            sv[q] = mk3(float(S.x[3 * q] - S.x[0]), float(S.x[3 * q + 1] - S.x[1]), float(S.x[3 * q + 2] - S.x[2]));
+            tv[q] = mk3(float(T.x[3 * q] - S.x[0]), float(T.x[3 * q + 1] - S.x[1]), float(T.x[3 * q + 2] - S.x[2]));
+            e32 = fmaxf(e32, fmaxf(vnorm(sv[q]), vnorm(tv[q])));
         }
+        e32 *= 1e-4f;
     }
-    // 2. near_pieces' leaves (assemble.jl:131-142)
+    if (near) {  // contact_rule (assemble.jl:199-207) finds no contact beyond shared corners
+        const double tol = a.contact_rel * fmin(T.diam, S.diam);
+        const float tolf = float(tol);
+        // FP32 pass: 1 contact, 0 none, -1 undecided (then the FP64 test decides)
+        int res;
+        {
+            v3<float> dc = (sv[1] + sv[2]) * (1.f / 3.f) - (tv[0] + tv[1] + tv[2]) * (1.f / 3.f);
+            int far_reach = lt32(float(T.reach + S.reach + tol), vnorm(dc), e32);
+            if (far_reach == 1) {
+                res = 0;
+            } else {
+                bool any_true = false, any_undec = far_reach < 0;
+                for (int k = 0; k < 3; ++k) {
+                    int c = lt32(dist_tri_v(sv[0], sv[1], sv[2], tv[k]), tolf, e32);
+                    if (c == 1) any_true = true;
+                    else if (c < 0) any_undec = true;
+                }
+                for (int k = 0; k < 3 && !any_true; ++k) {
+                    v3<float> ta = tv[k], tc = tv[(k + 1) % 3];
+                    v3<float> ev = tc - ta;
+                    float L = vnorm(ev);
+                    for (int q = 0; q < 3; ++q) {
+                        float t = dot(sv[q] - ta, ev) / dot(ev, ev);
+                        t = fminf(fmaxf(t, 0.f), 1.f);
+                        float d = vnorm(sv[q] - (ta + t * ev));
+                        int c1 = lt32(d, tolf, e32) , c2 = lt32(tolf, t * L, 2.f * e32), c3 = lt32(tolf, (1.f - t) * L, 2.f * e32);
+                        if (d == tolf) c1 = -1;
+                        if (c1 == 1 && c2 == 1 && c3 == 1) any_true = true;
+                        else if (c1 != 0 && c2 != 0 && c3 != 0) any_undec = true;
+                    }
+                }
+                res = any_true ? 1 : (any_undec ? -1 : 0);
+                if (far_reach < 0 && res == 1) res = -1;  // contact needs the reach test passed
+            }
+        }
+        if (res < 0) {  // the reference's FP64 test
+            res = 0;
+            if (!(vnorm(ld3(S.c) - ld3(T.c)) > T.reach + S.reach + tol)) {
+                bool extra = false;
+                for (int k = 0; k < 3 && !extra; ++k)
+                    if (dist_tri(S.x, ld3(T.x + 3 * k)) <= tol) extra = true;
+                for (int k = 0; k < 3 && !extra; ++k)
+                    for (int q = 0; q < 3 && !extra; ++q) {
+                        double tt;
+                        if (on_edge_split(ld3(S.x + 3 * q), ld3(T.x + 3 * k), ld3(T.x + 3 * ((k + 1) % 3)), tol, tt))
+                            extra = true;
+                    }
+                res = extra ? 1 : 0;
+            }
+        }
+        if (res == 1) near = false;
+    }
+    // 2. near_pieces' leaves (assemble.jl:131-142), decided in FP32 unless a node is too close to the threshold
     int nleaf = 0;
     if (near) {
         const int depth = a.near_depth;
+        const float ratiof = float(a.near_ratio);
         int level = 0;
         unsigned path = 0;
         for (int guard = 0; guard < 1024; ++guard) {
-            double b[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-            for (int l = 0; l < level; ++l) {
-                int digit = (path >> (2 * (level - 1 - l))) & 3;
-                double m12[3], m23[3], m31[3], nb[9];
-                bmix(m12, b, 0.5, b + 3, 0.5);
-                bmix(m23, b + 3, 0.5, b + 6, 0.5);
-                bmix(m31, b + 6, 0.5, b, 0.5);
-                const double *c0, *c1, *c2;
-                if (digit == 0) { c0 = b; c1 = m12; c2 = m31; }
-                else if (digit == 1) { c0 = m12; c1 = b + 3; c2 = m23; }
-                else if (digit == 2) { c0 = m31; c1 = m23; c2 = b + 6; }
-                else { c0 = m12; c1 = m23; c2 = m31; }
-                for (int z = 0; z < 3; ++z) {
-                    nb[z] = c0[z];
-                    nb[3 + z] = c1[z];
-                    nb[6 + z] = c2[z];
-                }
-                for (int z = 0; z < 9; ++z) b[z] = nb[z];
+            float bf[9];
+            leaf_corners32((level << 6) | int(path), bf);
+            v3<float> p1 = bf[0] * tv[0] + bf[1] * tv[1] + bf[2] * tv[2];
+            v3<float> p2 = bf[3] * tv[0] + bf[4] * tv[1] + bf[5] * tv[2];
+            v3<float> p3 = bf[6] * tv[0] + bf[7] * tv[1] + bf[8] * tv[2];
+            float size = fmaxf(vnorm(p2 - p1), fmaxf(vnorm(p3 - p2), vnorm(p1 - p3)));
+            float d = dist_tri_v(sv[0], sv[1], sv[2], (p1 + p2 + p3) * (1.f / 3.f));
+            int split = level < depth ? lt32(d, ratiof * size, 2.f * e32) : 0;
+            if (split < 0) {  // the reference's FP64 test at this node
+                double b[9];
+                for (int z = 0; z < 9; ++z) b[z] = double(bf[z]);
+                v3<double> q1 = tpoint(T, b), q2 = tpoint(T, b + 3), q3 = tpoint(T, b + 6);
+                double sz = fmax(vnorm(q2 - q1), fmax(vnorm(q3 - q2), vnorm(q1 - q3)));
+                split = dist_tri(S.x, (q1 + q2 + q3) / 3.0) < a.near_ratio * sz ? 1 : 0;
             }
-            v3<double> p1 = tpoint(T, b), p2 = tpoint(T, b + 3), p3 = tpoint(T, b + 6);
-            double size = fmax(vnorm(p2 - p1), fmax(vnorm(p3 - p2), vnorm(p1 - p3)));
-            if (level < depth && dist_tri(S.x, (p1 + p2 + p3) / 3.0) < a.near_ratio * size) {
+            if (split) {
                 level++;
                 path *= 4;
                 continue;
@@ -1344,7 +1440,10 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
         ns.S32[lane][24] = float(S.area);
         ns.S32[lane][25] = float(S.diam);
     }
-    for (int k = 0; k < 9; ++k) ns.acc[lane][k] = 0.0;
+    for (int k = 0; k < 9; ++k) {
+        ns.acc[lane][k] = 0.0;
+        ns.accf[lane][k] = 0.f;
+    }
     const int nr = a.nrule[R_NEAR];
     int incl = near ? nleaf * nr : 0;
 #pragma unroll
@@ -1391,12 +1490,11 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
             int code = ns.leaf[p][leaf];
             float b[9];
             leaf_corners32(code, b);
-            RulePt m = a.rule[R_NEAR][q];
-            float m0 = float(m.l0), m1 = float(m.l1), m2 = float(m.l2);
-            float l0 = m0 * b[0] + m1 * b[3] + m2 * b[6];
-            float l1 = m0 * b[1] + m1 * b[4] + m2 * b[7];
-            float l2 = m0 * b[2] + m1 * b[5] + m2 * b[8];
-            float W = float(m.w) * ldexpf(1.f, -2 * (code >> 6)) * areaT;
+            float4 m = a.rulef[R_NEAR][q];
+            float l0 = m.x * b[0] + m.y * b[3] + m.z * b[6];
+            float l1 = m.x * b[1] + m.y * b[4] + m.z * b[7];
+            float l2 = m.x * b[2] + m.y * b[5] + m.z * b[8];
+            float W = m.w * ldexpf(1.f, -2 * (code >> 6)) * areaT;
             const float* E = ns.E32[p];
             const float* Dp = ns.D32[p];
             const float* Sf = ns.S32[p];
@@ -1474,16 +1572,14 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
     // 4. the pairs' blocks, added pair by pair in source order
     double blk[9], rb[3] = {0, 0, 0};
     if (near) {
+        double Pp[9];
+        for (int k = 0; k < 9; ++k) Pp[k] = ns.acc[lane][k] + double(ns.accf[lane][k]);
         v3<double> nT = ld3(T.n);
         for (int bb = 0; bb < 3; ++bb) {
             v3<double> mv = cross(nT, ld3(S.gam + 3 * bb));
-            for (int ai = 0; ai < 3; ++ai)
-                blk[3 * ai + bb] = ns.acc[lane][3 * ai] * mv.x + ns.acc[lane][3 * ai + 1] * mv.y +
-                                   ns.acc[lane][3 * ai + 2] * mv.z;
+            for (int ai = 0; ai < 3; ++ai) blk[3 * ai + bb] = Pp[3 * ai] * mv.x + Pp[3 * ai + 1] * mv.y + Pp[3 * ai + 2] * mv.z;
         }
-        for (int ai = 0; ai < 3; ++ai)
-            rb[ai] = -S.sigma * (ns.acc[lane][3 * ai] * nT.x + ns.acc[lane][3 * ai + 1] * nT.y +
-                                 ns.acc[lane][3 * ai + 2] * nT.z);
+        for (int ai = 0; ai < 3; ++ai) rb[ai] = -S.sigma * (Pp[3 * ai] * nT.x + Pp[3 * ai + 1] * nT.y + Pp[3 * ai + 2] * nT.z);
     }
     for (int k = 0; k < cnt; ++k) {
         if (!((nearmask >> k) & 1u)) continue;
@@ -1508,9 +1604,10 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
     return __ballot_sync(FULL, valid && !near);
 }
 
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
+// near tier, one pair per lane; the other pairs are listed for near_kernel_rest
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a) {
     extern __shared__ __align__(16) unsigned char near_smem[];
-    WarpSmem* shm = reinterpret_cast<WarpSmem*>(near_smem);
+    NearChunkSh* shm = reinterpret_cast<NearChunkSh*>(near_smem);
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int idx = blockIdx.x * NEAR_WARPS + w;
     if (idx >= a.ntests) return;
@@ -1519,7 +1616,48 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
     PairCtx pc;
     pc.a = &a;
     pc.T = &T;
-    pc.sh = &shm[w].w;
+    pc.sh = nullptr;
+    pc.lane = lane;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+    double rbt[3] = {0, 0, 0};
+    for (int set = 0; set < 2; ++set) {
+        const bool wake = set == 1;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t], e1 = wake ? a.wf_ptr[t + 1] : a.nf_ptr[t + 1];
+        const int* src = wake ? a.wf_src : a.nf_src;
+        int* rest = wake ? a.wrest_src : a.rest_src;
+        const int col0 = wake ? a.nslot : 0;
+        int nrest = 0;
+        for (long long c0 = e0; c0 < e1; c0 += 32) {
+            const int cnt = int(e1 - c0 < 32 ? e1 - c0 : 32);
+            unsigned m = near_chunk(pc, shm[w], t, src + c0, cnt, wake, col0, rbt, P, Q, Q64);
+            if ((m >> lane) & 1u) rest[e0 + nrest + __popc(m & ((1u << lane) - 1u))] = src[c0 + lane];
+            nrest += __popc(m);
+            __syncwarp();
+        }
+        if (lane == 0) a.rest_cnt[2 * t + set] = nrest;
+    }
+    if (lane == 0) {
+        for (int k = 0; k < 3; ++k) a.b[T.slot[k]] += rbt[k];
+        for (int k = 0; k < 6; ++k) {
+            if (P[k]) atomicAdd(a.stats + k, P[k]);
+            if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
+        }
+        if (Q64) atomicAdd(a.stats + 12, Q64);
+    }
+}
+
+// the self, touching and contact pairs (one warp per test triangle), the tip filaments and the freestream
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int idx = blockIdx.x * NEAR_WARPS + w;
+    if (idx >= a.ntests) return;
+    const int t = a.tests[idx];
+    const TriGeo& T = a.tri[t];
+    PairCtx pc;
+    pc.a = &a;
+    pc.T = &T;
+    pc.sh = &shm[w];
     pc.lane = lane;
     pc.nleaf = 0;
     pc.nq64 = 0;
@@ -1527,33 +1665,25 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel(NearArgs a) {
     unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
     double rbt[3] = {0, 0, 0};
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    // body sources (assemble.jl:408-419), then the wake's sheets (add_wake!, assemble.jl:333-343)
     for (int set = 0; set < 2; ++set) {
         const bool wake = set == 1;
-        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t], e1 = wake ? a.wf_ptr[t + 1] : a.nf_ptr[t + 1];
-        const int* src = wake ? a.wf_src : a.nf_src;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
+        const int n = a.rest_cnt[2 * t + set];
+        const int* rest = wake ? a.wrest_src : a.rest_src;
         const int col0 = wake ? a.nslot : 0;
-        for (long long c0 = e0; c0 < e1; c0 += 32) {
-            const int cnt = int(e1 - c0 < 32 ? e1 - c0 : 32);
-            unsigned rest = near_chunk(pc, shm[w].c, t, src + c0, cnt, wake, col0, rbt, P, Q, Q64);
-            __syncwarp();
-            while (rest) {
-                const int k = __ffs(rest) - 1;
-                rest &= rest - 1;
-                const int s = src[c0 + k];
-                Acc acc = {};
-                pc.kind = 0;
-                pc.npts = 0;
-                pc.n64 = 0;
-                pc.nleaf = 0;
-                pc.nq64 = 0;
-                int tier = tri_pair(pc, acc, t, s, wake);
-                add_block(pc, acc, wake ? a.wtri[s] : a.tri[s], col0, rbt, !wake);
-                P[tier] += 1;
-                Q[tier] += pc.npts;
-                Q64 += pc.n64;
-            }
-            __syncwarp();
+        for (int e = 0; e < n; ++e) {
+            const int s = rest[e0 + e];
+            Acc acc = {};
+            pc.kind = 0;
+            pc.npts = 0;
+            pc.n64 = 0;
+            pc.nleaf = 0;
+            pc.nq64 = 0;
+            int tier = tri_pair(pc, acc, t, s, wake);
+            add_block(pc, acc, wake ? a.wtri[s] : a.tri[s], col0, rbt, !wake);
+            P[tier] += 1;
+            Q[tier] += pc.npts;
+            Q64 += pc.n64;
         }
     }
     // tip filaments (assemble.jl:344-354): segment_rule (:299-306) and segment_block (:312-321), FP64
@@ -1911,10 +2041,15 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         if ((r = dl.up(ctx, &d_wx, hwx)) || (r = dl.up(ctx, &d_fil, hfil))) return r;
     }
     RulePt* d_rule[5];
+    float4* d_rulef[5];
     {
         const std::vector<RulePt>* R[5] = {&rnear, &rself, &redge, &rvert, &rfar};
-        for (int k = 0; k < 5; ++k)
-            if ((r = dl.up(ctx, &d_rule[k], *R[k]))) return r;
+        for (int k = 0; k < 5; ++k) {
+            std::vector<float4> f(R[k]->size());
+            for (size_t i = 0; i < f.size(); ++i)
+                f[i] = make_float4(float((*R[k])[i].l0), float((*R[k])[i].l1), float((*R[k])[i].l2), float((*R[k])[i].w));
+            if ((r = dl.up(ctx, &d_rule[k], *R[k])) || (r = dl.up(ctx, &d_rulef[k], f))) return r;
+        }
     }
     vp_phase_end(ctx);
     // classification of the non-far sources of every test triangle
@@ -2069,6 +2204,7 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         const int nr[5] = {(int)rnear.size(), (int)rself.size(), (int)redge.size(), (int)rvert.size(), (int)rfar.size()};
         for (int k = 0; k < 5; ++k) {
             na.rule[k] = d_rule[k];
+            na.rulef[k] = d_rulef[k];
             na.nrule[k] = nr[k];
         }
         na.A = sys->A;
@@ -2087,18 +2223,31 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
             na.tint[k] = o->test == 1 ? 1.0 : 1.0 / 3;
         }
         na.stats = d_stats;
+        int *d_rest, *d_wrest, *d_rcnt;
+        if ((r = dl.alloc(ctx, &d_rest, size_t(std::max(nfptr[ntri], 1LL)))) ||
+            (r = dl.alloc(ctx, &d_wrest, size_t(std::max(wfptr[ntri], 1LL)))) ||
+            (r = dl.alloc(ctx, &d_rcnt, size_t(2) * ntri))) {
+            vp_system_free(sys);
+            return r;
+        }
+        na.rest_src = d_rest;
+        na.wrest_src = d_wrest;
+        na.rest_cnt = d_rcnt;
         vp_phase_begin(ctx, PH_NEAR);
-        const size_t near_smem = sizeof(WarpSmem) * NEAR_WARPS;
-        VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(near_smem)));
-        for (size_t c = 0; c < colours.size(); ++c) {
-            na.tests = d_tests + off[c];
-            na.ntests = off[c + 1] - off[c];
-            int nb = (na.ntests + NEAR_WARPS - 1) / NEAR_WARPS;
-            if (nb) {
-                near_kernel<<<nb, 32 * NEAR_WARPS, near_smem, ctx->stream>>>(na);
+        const size_t near_smem = sizeof(NearChunkSh) * NEAR_WARPS;
+        VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, int(near_smem)));
+        for (int pass = 0; pass < 2; ++pass)
+            for (size_t c = 0; c < colours.size(); ++c) {
+                na.tests = d_tests + off[c];
+                na.ntests = off[c + 1] - off[c];
+                int nb = (na.ntests + NEAR_WARPS - 1) / NEAR_WARPS;
+                if (!nb) continue;
+                if (pass == 0)
+                    near_kernel_lanes<<<nb, 32 * NEAR_WARPS, near_smem, ctx->stream>>>(na);
+                else
+                    near_kernel_rest<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
                 ctx->launches++;
             }
-        }
         vp_phase_end(ctx);
         VP_CUDA(ctx, cudaGetLastError());
     }
