@@ -116,6 +116,16 @@ int vp_phase_times(vp_ctx* ctx, double* ms, int n, long long* launches, int rese
 /* Instrumentation (no counterpart in the reference): bytes copied host->device and device->host by the library. */
 int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset);
 
+/* Diagnostics (no counterpart in the reference): the device kernels at n points, one thread per point.
+ *   mode 0: w (3 per point), the unit source velocity of triangle tri (9 per point) at x (3 per point), with the
+ *           far-field switch kernel_far and the in-plane side (source_triangle.jl:134-138);
+ *   mode 1: s = w·m (m: 3 per point) and its derivatives with respect to x and the triangle's corners (1 + 3 + 9);
+ *   mode 2: the filament from tri[0:3] to tri[3:6] with end weights ca = tri[6], cb = tri[7]: s = ca va·m + cb vb·m
+ *           (segment.jl:15-25) and its derivatives with respect to x and the two ends (1 + 3 + 6).
+ * precision VP_FP64 or VP_MIXED (the FP32 kernels, without the FP64 guard). */
+int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const double* tri, const double* x, const double* m,
+                   int side, double kernel_far, double* out);
+
 /* Condition estimate and size of a factorization. */
 int vp_factor_info(const vp_factor* F, int* n, double* cond);
 void vp_factor_free(vp_factor* F);

@@ -1,0 +1,185 @@
+// Reverse-mode derivatives of the pair-integral kernels for the adjoint (templated on float / double).
+//
+// A quadrature point contributes W nu(q) s, s = w(x)·m, with w the unit source-triangle velocity
+// (src/kernels/source_triangle.jl:75-138) and m a per-pair vector. w depends on the point only through the offsets
+// r_a = x - v_a to the source's corners, and on the source's shape through its edge normals nu_e, edge lengths, unit
+// normal n (exact form) or its corner offsets d_a and area (multipole form). The functions below return s, the
+// derivative of s with respect to the offsets at fixed shape, and the per-point factors of the shape derivatives,
+// which the caller sums over the points of a pair and turns into corner derivatives once per pair.
+#pragma once
+#include "vp_math.cuh"
+
+// shape factors of one exact-kernel point: s depends on the shape through
+//   sum_e L_e (nu_e·m)/4pi + Omega (n·m)/4pi, with L_e depending on the edge length through num_e = r_i + r_j + len_e
+template <class T>
+struct ExactShape {
+    T L[3];      // edge logs
+    T dLdlen[3]; // dL_e / d len_e = 2 / num_e
+    T Om;        // solid angle
+};
+
+// s = w·m of the exact kernel at fixed shape (nu, len, n from the source) and ds/dr_a.
+template <class T>
+__device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r1, v3<T> r2, v3<T> r, v3<T> m,
+                                          int side, T plane_tol, v3<T>& g0, v3<T>& g1, v3<T>& g2, ExactShape<T>& sh) {
+    const T i4pi = T(1) / (T(4) * vp_pi<T>());
+    const v3<T> R[3] = {r0, r1, r2};
+    T l[3] = {vnorm(r0), vnorm(r1), vnorm(r2)};
+    v3<T> gr[3] = {mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0))};
+    T lbar[3] = {T(0), T(0), T(0)};
+    T s = T(0);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = (e + 1) % 3;
+        v3<T> ri = R[i], rj = R[j];
+        T p = dot(ri, rj);
+        T num = l[i] + l[j] + S.len[e];
+        T L, dLdli, dLdlj, dLdp;
+        v3<T> c = cross(ri, rj);
+        T c2 = norm2(c);
+        if (p < T(0)) {
+            T den = l[i] * l[j] - p;
+            T q = den / (T(2) * c2);
+            L = vlog(num * num * q);
+            // d log q: li -> lj/den, lj -> li/den, p -> -1/den, c2 -> -1/c2
+            dLdli = T(2) / num + l[j] / den;
+            dLdlj = T(2) / num + l[i] / den;
+            dLdp = -T(1) / den;
+            T dLdc2 = -T(1) / c2;
+            T coef = dot(S.nu[e], m) * i4pi;
+            // c2 = |ri x rj|^2: d/dri = 2 rj x c, d/drj = 2 c x ri
+            gr[i] += (coef * dLdc2 * T(2)) * cross(rj, c);
+            gr[j] += (coef * dLdc2 * T(2)) * cross(c, ri);
+        } else {
+            T den = l[i] * l[j] + p;
+            L = sizeof(T) == 4 ? T(log1pf(float(S.len[e] * num / den))) : vlog(num * num / (T(2) * den));
+            dLdli = T(2) / num - l[j] / den;
+            dLdlj = T(2) / num - l[i] / den;
+            dLdp = -T(1) / den;
+        }
+        T coef = dot(S.nu[e], m) * i4pi;
+        s += L * coef;
+        lbar[i] += coef * dLdli;
+        lbar[j] += coef * dLdlj;
+        gr[i] += (coef * dLdp) * rj;
+        gr[j] += (coef * dLdp) * ri;
+        sh.L[e] = L;
+        sh.dLdlen[e] = T(2) / num;
+    }
+    T z = dot(r, S.n);
+    T nm = dot(S.n, m) * i4pi;
+    if (fabs(z) <= plane_tol * S.diam) {
+        v3<T> q[3] = {-r0, -r1, -r2};
+        sh.Om = side == 0 ? T(0) : T(side) * T(2) * vp_pi<T>() * inplane_fraction_rel(q, S.n, S.area, plane_tol);
+    } else {
+        T N = dot(r0, cross(r1, r2));
+        T D = l[0] * l[1] * l[2] + dot(r0, r1) * l[2] + dot(r0, r2) * l[1] + dot(r1, r2) * l[0];
+        sh.Om = T(2) * vatan2(N, D);
+        T h = T(2) / (N * N + D * D);
+        T Nb = nm * D * h, Db = -nm * N * h;
+        gr[0] += Nb * cross(r1, r2);
+        gr[1] += Nb * cross(r2, r0);
+        gr[2] += Nb * cross(r0, r1);
+        lbar[0] += Db * (l[1] * l[2] + dot(r1, r2));
+        lbar[1] += Db * (l[0] * l[2] + dot(r0, r2));
+        lbar[2] += Db * (l[0] * l[1] + dot(r0, r1));
+        gr[0] += Db * (l[2] * r1 + l[1] * r2);
+        gr[1] += Db * (l[2] * r0 + l[0] * r2);
+        gr[2] += Db * (l[1] * r0 + l[0] * r1);
+    }
+    s += sh.Om * nm;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) gr[a] += (lbar[a] / l[a]) * R[a];
+    g0 = gr[0];
+    g1 = gr[1];
+    g2 = gr[2];
+    return s;
+}
+
+// s = w·m of the multipole form (source_triangle.jl:100-119) and its derivatives with respect to r = x - c, to the
+// corner offsets d_a (gd) and the area (ga)
+template <class T>
+__device__ __forceinline__ T sv_far_vjp(const SrcKern<T>& S, v3<T> r, v3<T> m, v3<T>& gr, v3<T>* gd, T& ga) {
+    const T k = S.area / (T(4) * vp_pi<T>());
+    T R2 = dot(r, r);
+    T R = vsqrt(R2);
+    T iR2 = T(1) / R2, iR3 = iR2 / R, iR5 = iR3 * iR2, iR7 = iR5 * iR2, iR9 = iR7 * iR2, iR11 = iR9 * iR2;
+    T rm = dot(r, m);
+    // F·m = iR3 rm + sum_a g_a(dr, dd, rm, dm, R2)
+    T Fm = iR3 * rm;
+    v3<T> gF = iR3 * m;  // d(F·m)/dr, accumulated
+    T dR2 = T(-1.5) * iR5 * rm;  // d(F·m)/dR2
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        v3<T> d = S.d[a];
+        T dr = dot(d, r), dd = dot(d, d), dm = dot(d, m);
+        // quad·m / 24 - oct·m / 180
+        T g = (T(15) * dr * dr * iR7 * rm - T(6) * dr * iR5 * dm - T(3) * dd * iR5 * rm) / T(24) -
+              (T(45) * dr * dr * iR7 * dm - T(105) * dr * dr * dr * iR9 * rm - T(9) * dd * iR5 * dm +
+               T(45) * dd * dr * iR7 * rm) / T(180);
+        Fm += g;
+        T g_dr = (T(30) * dr * iR7 * rm - T(6) * iR5 * dm) / T(24) -
+                 (T(90) * dr * iR7 * dm - T(315) * dr * dr * iR9 * rm + T(45) * dd * iR7 * rm) / T(180);
+        T g_dd = (-T(3) * iR5 * rm) / T(24) - (-T(9) * iR5 * dm + T(45) * dr * iR7 * rm) / T(180);
+        T g_rm = (T(15) * dr * dr * iR7 - T(3) * dd * iR5) / T(24) -
+                 (-T(105) * dr * dr * dr * iR9 + T(45) * dd * dr * iR7) / T(180);
+        T g_dm = (-T(6) * dr * iR5) / T(24) - (T(45) * dr * dr * iR7 - T(9) * dd * iR5) / T(180);
+        // iR_k = R2^(-k/2): d/dR2 = -(k/2) iR_(k+2)
+        T g_R2 = (T(15) * dr * dr * (T(-3.5) * iR9) * rm - T(6) * dr * (T(-2.5) * iR7) * dm -
+                  T(3) * dd * (T(-2.5) * iR7) * rm) / T(24) -
+                 (T(45) * dr * dr * (T(-3.5) * iR9) * dm - T(105) * dr * dr * dr * (T(-4.5) * iR11) * rm -
+                  T(9) * dd * (T(-2.5) * iR7) * dm + T(45) * dd * dr * (T(-3.5) * iR9) * rm) / T(180);
+        gF += g_dr * d + g_rm * m;
+        dR2 += g_R2;
+        gd[a] = k * (g_dr * r + (T(2) * g_dd) * d + g_dm * m);
+    }
+    gF += (T(2) * dR2) * r;
+    gr = k * gF;
+    ga = Fm / (T(4) * vp_pi<T>());
+    return k * Fm;
+}
+
+// the two end parts of a filament (segment.jl:15-25) contracted with ca, cb: s = ca (va·n) + cb (vb·n), and its
+// derivatives with respect to ra = x - a and rb = x - b
+template <class T>
+__device__ __forceinline__ T seg_vjp(v3<T> ra, v3<T> rb, v3<T> n, T ca, T cb, v3<T>& ga, v3<T>& gb) {
+    T Ra = vnorm(ra), Rb = vnorm(rb);
+    v3<T> c = cross(ra, rb);
+    T p = dot(ra, rb);
+    T den, c2 = norm2(c);
+    bool neg = p < T(0);
+    den = neg ? c2 / (Ra * Rb - p) : Ra * Rb + p;
+    ga = mk3(T(0), T(0), T(0));
+    gb = ga;
+    if (den == T(0) || Ra == T(0) || Rb == T(0)) return T(0);
+    const T i4pi = T(1) / (T(4) * vp_pi<T>());
+    T cn = dot(c, n);
+    T wsum = ca / Ra + cb / Rb;
+    T s = cn * i4pi / den * wsum;
+    // s = cn * i4pi * wsum / den
+    T s_cn = i4pi * wsum / den;
+    T s_den = -s / den;
+    T s_Ra = -cn * i4pi / den * ca / (Ra * Ra);
+    T s_Rb = -cn * i4pi / den * cb / (Rb * Rb);
+    // cn = (ra x rb)·n: d/dra = rb x n, d/drb = n x ra
+    ga += s_cn * cross(rb, n);
+    gb += s_cn * cross(n, ra);
+    if (neg) {  // den = c2 / (Ra Rb - p)
+        T q = Ra * Rb - p;
+        T d_c2 = T(1) / q, d_q = -c2 / (q * q);
+        ga += (s_den * d_c2 * T(2)) * cross(rb, c);
+        gb += (s_den * d_c2 * T(2)) * cross(c, ra);
+        s_Ra += s_den * d_q * Rb;
+        s_Rb += s_den * d_q * Ra;
+        ga += (-s_den * d_q) * rb;
+        gb += (-s_den * d_q) * ra;
+    } else {  // den = Ra Rb + p
+        s_Ra += s_den * Rb;
+        s_Rb += s_den * Ra;
+        ga += s_den * rb;
+        gb += s_den * ra;
+    }
+    ga += (s_Ra / Ra) * ra;
+    gb += (s_Rb / Rb) * rb;
+    return s;
+}

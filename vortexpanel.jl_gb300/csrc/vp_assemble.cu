@@ -24,6 +24,7 @@
 #include <numeric>
 #include <unordered_map>
 
+#include "vp_adjoint_common.cuh"
 #include "vp_internal.h"
 #include "vp_math.cuh"
 
@@ -34,6 +35,8 @@ constexpr int NQMAX = 7;     // points of the far rule, at most
 constexpr int NFIELD = 42;   // scalar fields per source in the far kernel's SoA
 constexpr int NEAR_WARPS = 4;
 constexpr int LEAFBUF = 32;
+// FP32 guard of the adjoint's derivative evaluations (corner, edge sin^2, plane): tighter than the forward's
+#define ADJ_GUARD 3e-2f, 1e-1f, 1e-3f
 
 // ------------------------------------------------------------------------------------------------------------------
 // host: quadrature rules (src/elements/rules.jl)
@@ -620,8 +623,8 @@ __device__ __forceinline__ v3<double> tpoint(const TriGeo& T, const double* b) {
                b[0] * T.x[2] + b[1] * T.x[5] + b[2] * T.x[8]);
 }
 
-// per-lane accumulators of a pair
-struct Acc {
+// per-lane accumulators of a pair (forward)
+struct FwdAcc {
     v3<double> P[3];      // triangle source: sum of W psi_a w
     double ca[3], cb[3];  // filament source: the two end parts
     v3<float> Pf[3];      // FP32 partial sums, folded into P every few points
@@ -640,9 +643,14 @@ struct PairCtx {
     int nq64;       // queued FP64 points (uniform)
     long long npts; // points of this pair (uniform)
     long long n64;  // points of this pair evaluated in FP64 (uniform)
+    // adjoint: the test function weights nu_a at T's corners, the pair's direction m, a filament's end values
+    double nu[3];
+    v3<double> m;
+    v3<float> mf;
+    double mua, mub;
 };
 
-__device__ __forceinline__ void fold32(Acc& acc) {
+__device__ __forceinline__ void fold32(FwdAcc& acc) {
     for (int k = 0; k < 3; ++k) {
         acc.P[k].x += double(acc.Pf[k].x);
         acc.P[k].y += double(acc.Pf[k].y);
@@ -653,7 +661,7 @@ __device__ __forceinline__ void fold32(Acc& acc) {
 }
 
 // evaluate one point (barycentric l on T, weight W) in FP64
-__device__ __forceinline__ void eval_point64(const PairCtx& pc, Acc& acc, double l0, double l1, double l2, double W) {
+__device__ __forceinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double l0, double l1, double l2, double W) {
     const WarpSh& sh = *pc.sh;
     v3<double> psi = test_weights(pc.a->test_mode, l0, l1, l2);
     if (pc.kind == 0) {
@@ -692,7 +700,7 @@ __device__ __forceinline__ void eval_point64(const PairCtx& pc, Acc& acc, double
 }
 
 // evaluate one point in FP32 (triangle sources in VP_MIXED); false when it lies where FP32 cancels
-__device__ __forceinline__ bool eval_point32(const PairCtx& pc, Acc& acc, float l0, float l1, float l2, float W) {
+__device__ __forceinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float l0, float l1, float l2, float W) {
     if (pc.a->test_mode == 2) return false;  // the dual test's ties are decided in FP64
     const WarpSh& sh = *pc.sh;
     SrcKern<float> S;
@@ -726,8 +734,144 @@ __device__ __forceinline__ bool eval_point32(const PairCtx& pc, Acc& acc, float 
     return true;
 }
 
+// ---- adjoint accumulation of a pair (warp-cooperative path) --------------------------------------------------------
+struct AdjAcc {
+    AdjSums<double> d;  // FP64 sums
+    AdjSums<float> f;   // FP32 partial sums, folded into d every few points
+    int nf;
+};
+
+template <class A, class B>
+__device__ __forceinline__ void adj_add(AdjSums<A>& d, const AdjSums<B>& f) {
+    auto c = [](v3<B> v) { return mk3(A(v.x), A(v.y), A(v.z)); };
+    d.Q += c(f.Q);
+    d.Grf += c(f.Grf);
+    for (int k = 0; k < 3; ++k) {
+        d.Xg[k] += c(f.Xg[k]);
+        d.Gr[k] += c(f.Gr[k]);
+        d.Gd[k] += c(f.Gd[k]);
+        d.L[k] += A(f.L[k]);
+        d.N[k] += A(f.N[k]);
+    }
+    d.O += A(f.O);
+    d.A += A(f.A);
+}
+
+__device__ __forceinline__ void fold32(AdjAcc& acc) {
+    adj_add(acc.d, acc.f);
+    adj_zero(acc.f);
+    acc.nf = 0;
+}
+
+__device__ __forceinline__ SrcKern<double> src64(const WarpSh& sh) {
+    SrcKern<double> S;
+    for (int k = 0; k < 3; ++k) {
+        S.d[k] = ld3(sh.Sd + 3 * k);
+        S.nu[k] = ld3(sh.Snu + 3 * k);
+        S.len[k] = sh.Slen[k];
+    }
+    S.n = ld3(sh.Sn);
+    S.area = sh.Sarea;
+    S.diam = sh.Sdiam;
+    return S;
+}
+
+__device__ __forceinline__ SrcKern<float> src32(const WarpSh& sh) {
+    SrcKern<float> S;
+    for (int k = 0; k < 3; ++k) {
+        S.d[k] = mk3(sh.Sdf[3 * k], sh.Sdf[3 * k + 1], sh.Sdf[3 * k + 2]);
+        S.nu[k] = mk3(sh.Snuf[3 * k], sh.Snuf[3 * k + 1], sh.Snuf[3 * k + 2]);
+        S.len[k] = sh.Slenf[k];
+    }
+    S.n = mk3(sh.Snf[0], sh.Snf[1], sh.Snf[2]);
+    S.area = sh.Sareaf;
+    S.diam = sh.Sdiamf;
+    return S;
+}
+
+// one point in FP64, adjoint: W nu(q) times s = w·m and its derivatives (source sheets), or the filament's
+__device__ __forceinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, double l0, double l1, double l2, double W) {
+    const WarpSh& sh = *pc.sh;
+    v3<double> psi = test_weights(pc.a->test_mode, l0, l1, l2);
+    double Wn = W * (pc.nu[0] * psi.x + pc.nu[1] * psi.y + pc.nu[2] * psi.z);
+    v3<double> ra = l0 * ld3(sh.E + 0) + l1 * ld3(sh.E + 9) + l2 * ld3(sh.E + 18);
+    v3<double> rb = l0 * ld3(sh.E + 3) + l1 * ld3(sh.E + 12) + l2 * ld3(sh.E + 21);
+    if (pc.kind == 0) {
+        v3<double> rc = l0 * ld3(sh.E + 6) + l1 * ld3(sh.E + 15) + l2 * ld3(sh.E + 24);
+        v3<double> r = l0 * ld3(sh.D) + l1 * ld3(sh.D + 3) + l2 * ld3(sh.D + 6);
+        SrcKern<double> S = src64(sh);
+        double fd = pc.a->kernel_far * S.diam;
+        if (dot(r, r) > fd * fd)
+            adj_point_far(acc.d, S, Wn, l0, l1, l2, r, pc.m);
+        else
+            adj_point_exact(acc.d, S, Wn, l0, l1, l2, ra, rb, rc, r, pc.m, pc.side, 1e-12);
+    } else {
+        v3<double> n = ld3(pc.T->n), va, vb, ga, gb;
+        segment_velocity(ra, rb, va, vb);
+        seg_vjp(ra, rb, n, pc.mua, pc.mub, ga, gb);
+        acc.d.Q += Wn * (pc.mua * va + pc.mub * vb);
+        v3<double> gx = ga + gb;
+        acc.d.Xg[0] += (Wn * l0) * gx;
+        acc.d.Xg[1] += (Wn * l1) * gx;
+        acc.d.Xg[2] += (Wn * l2) * gx;
+        acc.d.Gr[0] += Wn * ga;
+        acc.d.Gr[1] += Wn * gb;
+    }
+}
+
+// one point in FP32 under the guard, adjoint; false when it must be evaluated in FP64
+__device__ __forceinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float l0, float l1, float l2, float W) {
+    if (pc.a->test_mode == 2) return false;
+    const WarpSh& sh = *pc.sh;
+    SrcKern<float> S = src32(sh);
+    v3<float> r = l0 * mk3(sh.D32[0], sh.D32[1], sh.D32[2]) + l1 * mk3(sh.D32[3], sh.D32[4], sh.D32[5]) +
+                  l2 * mk3(sh.D32[6], sh.D32[7], sh.D32[8]);
+    v3<float> psi = pc.a->test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);
+    float Wn = W * (float(pc.nu[0]) * psi.x + float(pc.nu[1]) * psi.y + float(pc.nu[2]) * psi.z);
+    float fd = float(pc.a->kernel_far) * S.diam;
+    if (dot(r, r) > fd * fd) {
+        adj_point_far(acc.f, S, Wn, l0, l1, l2, r, pc.mf);
+    } else {
+        const float* E = sh.E32;
+        v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
+        v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
+        v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
+        if (!fp32_guard_ok(S, ra, rb, rc, pc.side, Fp32Guard{ADJ_GUARD})) return false;
+        adj_point_exact(acc.f, S, Wn, l0, l1, l2, ra, rb, rc, r, pc.mf, pc.side, 1e-12f);
+    }
+    if (++acc.nf == 16) fold32(acc);
+    return true;
+}
+
+__device__ __forceinline__ double wsum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ v3<double> wsum3(v3<double> v) { return mk3(wsum_d(v.x), wsum_d(v.y), wsum_d(v.z)); }
+
+__device__ void adj_warp_sum(AdjSums<double>& a) {
+    a.Q = wsum3(a.Q);
+    a.Grf = wsum3(a.Grf);
+    for (int k = 0; k < 3; ++k) {
+        a.Xg[k] = wsum3(a.Xg[k]);
+        a.Gr[k] = wsum3(a.Gr[k]);
+        a.Gd[k] = wsum3(a.Gd[k]);
+        a.L[k] = wsum_d(a.L[k]);
+        a.N[k] = wsum_d(a.N[k]);
+    }
+    a.O = wsum_d(a.O);
+    a.A = wsum_d(a.A);
+}
+
+__device__ __forceinline__ void tri_corners(const TriGeo& g, v3<double>* v) {
+    for (int k = 0; k < 3; ++k) v[k] = ld3(g.x + 3 * k);
+}
+
 // FP64 evaluation of the queued points, 32 at a time (all of them when `all`): rule point qi of the current piece
 // (corners b, fraction frac) or of buffered leaf ql
+template <class Acc>
 __device__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* b, double frac) {
     const RulePt* R = pc.a->rule[rid];
     const double areaT = pc.T->area;
@@ -764,6 +908,7 @@ __device__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* 
 
 // one point per lane (all lanes call this together). FP64: evaluated at once from the FP64 barycentrics. FP32: the
 // FP32 barycentrics are evaluated under the guard; guarded points are queued (rule point i, leaf lf) for drain64.
+template <class Acc>
 __device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, int rid, int i, int lf, const double* b,
                                            const float* bf, double frac) {
     if (!pc.fp32) {
@@ -796,6 +941,7 @@ __device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, in
 }
 
 // a piece carrying a whole tabulated rule: lanes stride over its points
+template <class Acc>
 __device__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, double frac) {
     const int n = pc.a->nrule[rid];
     float bf[10];
@@ -811,6 +957,7 @@ __device__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, doubl
     if (!pc.fp32) pc.n64 += n;
 }
 
+template <class Acc>
 __device__ void flush_leaves(PairCtx& pc, Acc& acc) {
     const int nl = pc.nleaf;
     if (nl == 0) return;
@@ -834,6 +981,7 @@ __device__ void flush_leaves(PairCtx& pc, Acc& acc) {
     pc.nleaf = 0;
 }
 
+template <class Acc>
 __device__ void emit_leaf(PairCtx& pc, Acc& acc, const double* b, double frac) {
     if (pc.lane == 0) {
         for (int k = 0; k < 9; ++k) pc.sh->leaf[pc.nleaf][k] = b[k];
@@ -850,6 +998,7 @@ __device__ __forceinline__ void bmix(double* o, const double* a, double sa, cons
 }
 
 // near_pieces! (assemble.jl:131-142) as a depth-first walk of the quadtree of sub-triangles
+template <class Acc>
 __device__ void near_pieces(PairCtx& pc, Acc& acc, const SrcRef& src, const double* b0, double frac0, int depth) {
     int level = 0;
     unsigned path = 0;  // base-4 digits, most significant first
@@ -893,6 +1042,7 @@ __device__ void near_pieces(PairCtx& pc, Acc& acc, const SrcRef& src, const doub
 }
 
 // vertex_pieces! (assemble.jl:102-116): the vertex rule toward corner k of the piece with corners p, b
+template <class Acc>
 __device__ void vertex_pieces(PairCtx& pc, Acc& acc, const v3<double>* p, int k, const double* b, double frac) {
     int i = (k + 1) % 3, j = (k + 2) % 3;
     v3<double> u = p[i] - p[k], v = p[j] - p[k];
@@ -933,6 +1083,7 @@ __device__ __forceinline__ bool on_edge_split(v3<double> q, v3<double> a, v3<dou
 }
 
 // contact_rule / contact_pieces! (assemble.jl:199-238) for a triangle source S; returns false without contact
+template <class Acc>
 __device__ bool contact_rule(PairCtx& pc, Acc& acc, const TriGeo& S, const bool* shared) {
     const TriGeo& T = *pc.T;
     const NearArgs& a = *pc.a;
@@ -1076,6 +1227,7 @@ __device__ void setup_tri_source(PairCtx& pc, const TriGeo& S) {
 }
 
 // the rule of one triangle pair and its evaluation; returns the tier. Sources: body (wake = 0) or wake triangle.
+template <class Acc>
 __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
     const NearArgs& a = *pc.a;
     const TriGeo& T = *pc.T;
@@ -1144,7 +1296,7 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
     return TIER_NEAR;
 }
 
-__device__ void add_block(PairCtx& pc, Acc& acc, const TriGeo& S, int col0, double* rbt, bool with_rhs) {
+__device__ void add_block(PairCtx& pc, FwdAcc& acc, const TriGeo& S, int col0, double* rbt, bool with_rhs) {
     // reduce the per-lane sums, contract with n_T x gamma_b and add the block to this warp's rows
     fold32(acc);
     double P[9];
@@ -1169,6 +1321,7 @@ __device__ void add_block(PairCtx& pc, Acc& acc, const TriGeo& S, int col0, doub
 }
 
 // vertex_rule (assemble.jl:119-125) toward corner k of the whole test triangle
+template <class Acc>
 __device__ void vertex_rule(PairCtx& pc, Acc& acc, int k) {
     const TriGeo& T = *pc.T;
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
@@ -1673,7 +1826,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) 
         const int col0 = wake ? a.nslot : 0;
         for (int e = 0; e < n; ++e) {
             const int s = rest[e0 + e];
-            Acc acc = {};
+            FwdAcc acc = {};
             pc.kind = 0;
             pc.npts = 0;
             pc.n64 = 0;
@@ -1701,7 +1854,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) 
             }
         }
         __syncwarp();
-        Acc acc = {};
+        FwdAcc acc = {};
         pc.kind = 1;
         pc.npts = 0;
         pc.n64 = 0;

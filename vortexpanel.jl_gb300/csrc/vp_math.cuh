@@ -71,10 +71,13 @@ __device__ T inplane_fraction_rel(const v3<T> q[3], v3<T> n, T area, T tol) {
 
 // edge_log with the distances to the edge's ends given: ln((r_i + r_j + d)^2 / (2(r_i r_j + ri.rj))), the denominator
 // formed without cancellation as |ri x rj|^2 / (r_i r_j - ri.rj) when ri.rj < 0 (source_triangle.jl:39-44)
+// (FP32: where ri.rj >= 0 the same value as log1p(d (r_i + r_j + d) / (r_i r_j + ri.rj)), using
+// (r_i + r_j)^2 - d^2 = 2 (r_i r_j + ri.rj), which keeps its accuracy at a distance where the log's argument nears 1)
 template <class T>
 __device__ __forceinline__ T edge_log_n(v3<T> ri, v3<T> rj, T li, T lj, T d) {
     T p = dot(ri, rj);
     T num = li + lj + d;
+    if (sizeof(T) == 4 && p >= T(0)) return T(log1pf(float(d * num / (li * lj + p))));
     T q = p < T(0) ? (li * lj - p) / (T(2) * norm2(cross(ri, rj))) : T(1) / (T(2) * (li * lj + p));
     return vlog(num * num * q);
 }
@@ -108,6 +111,29 @@ struct Fp32Guard {
     float corner, edge_sin2, plane;
 };
 
+// the guard of sv_exact3_guarded alone: true where the FP32 exact kernel (and its derivatives) may be used
+__device__ __forceinline__ bool fp32_guard_ok(const SrcKern<float>& S, v3<float> ra, v3<float> rb, v3<float> rc,
+                                              int side, const Fp32Guard& g) {
+    float la = vnorm(ra), lb = vnorm(rb), lc = vnorm(rc);
+    if (fminf(la, fminf(lb, lc)) < g.corner * S.diam) return false;
+    const v3<float> R[3] = {ra, rb, rc};
+    const float L[3] = {la, lb, lc};
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        v3<float> ri = R[e], rj = R[(e + 1) % 3];
+        float p = dot(ri, rj);
+        if (p < 0.f && norm2(cross(ri, rj)) < g.edge_sin2 * (L[e] * L[e]) * (L[(e + 1) % 3] * L[(e + 1) % 3]))
+            return false;
+    }
+    if (side == 0) {
+        float P3 = la * lb * lc;
+        float N = dot(ra, cross(rb, rc));
+        float D = P3 + dot(ra, rb) * lc + dot(ra, rc) * lb + dot(rb, rc) * la;
+        if (fabsf(N) < g.plane * P3 && (D < 0.f || fabsf(D) < g.plane * P3)) return false;
+    }
+    return true;
+}
+
 __device__ __forceinline__ bool sv_exact3_guarded(const SrcKern<float>& S, v3<float> ra, v3<float> rb, v3<float> rc,
                                                   int side, const Fp32Guard& g, v3<float>& w) {
     float la = vnorm(ra), lb = vnorm(rb), lc = vnorm(rc);
@@ -126,10 +152,10 @@ __device__ __forceinline__ bool sv_exact3_guarded(const SrcKern<float>& S, v3<fl
             float c2 = norm2(cross(ri, rj));
             if (c2 < g.edge_sin2 * (li * li) * (lj * lj)) return false;
             q = (li * lj - p) / (2.f * c2);
+            wt += logf(num * num * q) * S.nu[e];
         } else {
-            q = 1.f / (2.f * (li * lj + p));
+            wt += log1pf(S.len[e] * num / (li * lj + p)) * S.nu[e];
         }
-        wt += logf(num * num * q) * S.nu[e];
     }
     float Om;
     if (side != 0) {

@@ -339,3 +339,22 @@ def trefftz_drag(wte, mu_w, V):
         v = (dG[:, None] / (4 * math.pi) * np.cross(d, r) / np.einsum("ij,ij->i", r, r)[:, None]).sum(axis=0)
         Dsum += Gk * (n @ v) * l
     return 2 * Dsum / (V @ V)
+
+
+# ---- diagnostics -----------------------------------------------------------------------------------------------------
+
+def eval_points(mode, tri, x, m=None, side=0, kernel_far=10.0, precision="fp64", ctx=None):
+    """The device kernels at points (vp_eval_points): mode 0 velocity w, 1 s = w·m with its x and corner
+    derivatives, 2 the filament's (see include/vortexpanel_gpu.h)"""
+    ctx = ctx or default_context()
+    tri = np.ascontiguousarray(np.asarray(tri, float).reshape(-1, 9))
+    n = tri.shape[0]
+    x = np.ascontiguousarray(np.asarray(x, float).reshape(n, 3))
+    nout = {0: 3, 1: 13, 2: 10}[mode]
+    out = np.zeros((n, nout))
+    mm = None if m is None else np.ascontiguousarray(np.asarray(m, float).reshape(n, 3))
+    prec = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}[precision]
+    check(ctx.h, load().vp_eval_points(ctx.h, mode, prec, n, tri.ctypes.data_as(D), x.ctypes.data_as(D),
+                                       None if mm is None else mm.ctypes.data_as(D), side, kernel_far,
+                                       out.ctypes.data_as(D)))
+    return out
