@@ -75,7 +75,8 @@ def test_reverse_mode_against_fd(vp, oracle, far):
     for i in range(len(xs)):
         t = tris[i].reshape(3, 3)
         s = _s(oracle, t, xs[i], ms[i], far)
-        assert abs(out[i, 0] - s) <= 1e-12 * (abs(s) + 1e-300)
+        # the exact form loses digits to cancellation far from the triangle (about 1e-12 relative at 40 diameters)
+        assert abs(out[i, 0] - s) <= (1e-10 if far == math.inf else 1e-12) * (abs(s) + 1e-300)
         h = 1e-6 * np.linalg.norm(t[1] - t[0])
         scale = max(np.abs(out[i, 1:]).max(), 1e-300)
         for k in range(3):
