@@ -3,6 +3,8 @@
 #include "vp_adjoint_common.cuh"
 #include "vp_internal.h"
 
+#include <mutex>
+
 namespace {
 
 template <class T>
@@ -121,5 +123,71 @@ extern "C" int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const
     cudaFree(dm);
     cudaFree(dout);
     if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("vp_eval_points: ") + cudaGetErrorString(e));
+    return VP_OK;
+}
+
+// ---------------------------------------------------------------------------------------------------------------------
+// vp_eval_points_static: the same evaluation as vp_eval_points with no device allocation. Inputs and outputs are
+// staged through one file-scope device array sized for VP_STATIC_POINTS_MAX points; its address is looked up once per
+// device with cudaGetSymbolAddress on the first call for that device, so that first call has to be made before any
+// stream capture on the device. Calls that overlap in time on one device (from two streams or two host threads) share
+// the array and race: the caller serialises them. No part of the array has to start at zero: points_kernel writes
+// every output slot of the n points it is given, and the inputs are copied in before the launch.
+namespace {
+
+constexpr size_t kStaticTri = size_t(9) * VP_STATIC_POINTS_MAX;   // triangle (or filament) rows
+constexpr size_t kStaticVec = size_t(3) * VP_STATIC_POINTS_MAX;   // x and m
+constexpr size_t kStaticOut = size_t(13) * VP_STATIC_POINTS_MAX;  // widest output (mode 1)
+// offsets in doubles; each block starts on a 256-byte boundary (VP_STATIC_POINTS_MAX is a multiple of 32)
+constexpr size_t kOffX = kStaticTri, kOffM = kOffX + kStaticVec, kOffOut = kOffM + kStaticVec;
+constexpr size_t kStaticDoubles = kOffOut + kStaticOut;
+static_assert(VP_STATIC_POINTS_MAX % 32 == 0, "blocks must stay 256-byte aligned");
+
+static __device__ __align__(256) double g_points_scratch[kStaticDoubles];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+double* g_scratch_addr[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int vp_eval_points_static(vp_ctx* ctx, int mode, int precision, int n, const double* tri, const double* x,
+                                     const double* m, int side, double kernel_far, double* out) {
+    if (!ctx || !tri || !x || !out || n <= 0 || mode < 0 || mode > 2) return vp_fail(ctx, VP_ERR_ARG, "bad argument");
+    if (mode > 0 && !m) return vp_fail(ctx, VP_ERR_ARG, "m is needed");
+    if (n > VP_STATIC_POINTS_MAX)
+        return vp_fail(ctx, VP_ERR_ARG, "vp_eval_points_static: n = " + std::to_string(n) + " is above " +
+                                            std::to_string(VP_STATIC_POINTS_MAX));
+    if (ctx->device < 0 || ctx->device >= kMaxDevices) return vp_fail(ctx, VP_ERR_ARG, "device index");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    double* base;
+    {
+        std::lock_guard<std::mutex> lk(g_scratch_mu);
+        if (!g_scratch_addr[ctx->device]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_points_scratch);
+            if (e != cudaSuccess)
+                return vp_fail(ctx, VP_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_scratch_addr[ctx->device] = static_cast<double*>(p);
+        }
+        base = g_scratch_addr[ctx->device];
+    }
+    const int nout = mode == 0 ? 3 : (mode == 1 ? 13 : 10);
+    double *dt = base, *dx = base + kOffX, *dm = m ? base + kOffM : nullptr, *dout = base + kOffOut;
+    cudaError_t e = vp_h2d(ctx, dt, tri, sizeof(double) * 9 * size_t(n));
+    if (e == cudaSuccess) e = vp_h2d(ctx, dx, x, sizeof(double) * 3 * size_t(n));
+    if (e == cudaSuccess && m) e = vp_h2d(ctx, dm, m, sizeof(double) * 3 * size_t(n));
+    if (e == cudaSuccess) {
+        if (precision == VP_FP64)
+            points_kernel<double><<<(n + 127) / 128, 128, 0, ctx->stream>>>(mode, n, dt, dx, dm, side, kernel_far, dout);
+        else
+            points_kernel<float><<<(n + 127) / 128, 128, 0, ctx->stream>>>(mode, n, dt, dx, dm, side, kernel_far, dout);
+        ctx->launches++;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = vp_d2h(ctx, out, dout, sizeof(double) * nout * size_t(n));
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess)
+        return vp_fail(ctx, VP_ERR_CUDA, std::string("vp_eval_points_static: ") + cudaGetErrorString(e));
     return VP_OK;
 }

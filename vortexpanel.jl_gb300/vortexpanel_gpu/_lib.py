@@ -52,6 +52,8 @@ SIGNATURES = [
                                          ctypes.POINTER(ctypes.c_longlong), ctypes.c_int]),
     ("vp_eval_points", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, D, D, D, ctypes.c_int,
                                       ctypes.c_double, D]),
+    ("vp_eval_points_static", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, D, D, D,
+                                             ctypes.c_int, ctypes.c_double, D]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]

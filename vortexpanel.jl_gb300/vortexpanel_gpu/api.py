@@ -358,3 +358,22 @@ def eval_points(mode, tri, x, m=None, side=0, kernel_far=10.0, precision="fp64",
                                        None if mm is None else mm.ctypes.data_as(D), side, kernel_far,
                                        out.ctypes.data_as(D)))
     return out
+
+
+STATIC_POINTS_MAX = 2048  # VP_STATIC_POINTS_MAX in include/vortexpanel_gpu.h
+
+
+def eval_points_static(mode, tri, x, m=None, side=0, kernel_far=10.0, precision="fp64", ctx=None):
+    """eval_points through vp_eval_points_static: no device allocation, at most STATIC_POINTS_MAX points a call;
+    calls that overlap in time on one device race on its staging array"""
+    ctx = ctx or default_context()
+    tri = np.ascontiguousarray(np.asarray(tri, float).reshape(-1, 9))
+    n = tri.shape[0]
+    x = np.ascontiguousarray(np.asarray(x, float).reshape(n, 3))
+    out = np.zeros((n, {0: 3, 1: 13, 2: 10}[mode]))
+    mm = None if m is None else np.ascontiguousarray(np.asarray(m, float).reshape(n, 3))
+    prec = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}[precision]
+    check(ctx.h, load().vp_eval_points_static(ctx.h, mode, prec, n, tri.ctypes.data_as(D), x.ctypes.data_as(D),
+                                              None if mm is None else mm.ctypes.data_as(D), side, kernel_far,
+                                              out.ctypes.data_as(D)))
+    return out
