@@ -1,0 +1,127 @@
+"""Adjoint gradients through the C ABI (vp_solve_transposed, vp_adjoint) against central finite differences of the
+GPU's FP64 forward path (assemble + factorize + solve + loads), step 1e-6 chord, on a small lifting wing with its
+rigid wake: dCL/dx and dCDi/dx at seeded random nodes, trailing edge and tip nodes among them, and d/dalpha."""
+import dataclasses
+import math
+
+import numpy as np
+import pytest
+
+from vortexpanel_gpu import api, meshes
+from vortexpanel_gpu.adjoint import wing_gradients
+
+pytestmark = pytest.mark.gpu
+
+
+def _corner_angles(g):
+    x, t = g.x, g.tris
+    out = []
+    for k in range(3):
+        u = x[t[:, (k + 1) % 3]] - x[t[:, k]]
+        v = x[t[:, (k + 2) % 3]] - x[t[:, k]]
+        c = np.einsum("ij,ij->i", u, v) / (np.linalg.norm(u, axis=1) * np.linalg.norm(v, axis=1))
+        out.append(np.degrees(np.arccos(np.clip(c, -1, 1))))
+    return np.concatenate(out)
+
+
+@pytest.fixture(scope="module")
+def case():
+    """The wing with its nodes moved in x and y by up to 2e-3 chord: the extruded wing's quads have corners of
+    exactly 90 degrees, where the vertex rule switches from one piece to wedges (assemble.jl:102-125), so that the
+    discrete loads jump under a rounding-level move and finite differences across the switch mean nothing"""
+    w = meshes.wing(12, 6, aspect=6.0)
+    rng = np.random.default_rng(20)
+    x = w.g.x.copy()
+    x[:, :2] += rng.uniform(-2e-3, 2e-3, (len(x), 2)) * w.chord
+    w = dataclasses.replace(w, g=dataclasses.replace(w.g, x=x))
+    te = w.dm.wake_te
+    w = dataclasses.replace(w, dm=dataclasses.replace(w.dm, wake_te=meshes.WakeTE(te.node, x[te.node].copy(), te.lines,
+                                                                                   te.closed)))
+    ang = _corner_angles(w.g)
+    # no corner within 0.01 degrees of a switch of the vertex rule (90, and 150 for corner_angle = 75), wedges present
+    assert np.abs(ang - 90).min() > 1e-2 and np.abs(ang - 150).min() > 1e-2 and (ang > 90.5).any()
+    wake = meshes.build_wake(w.g, w.dm, (1.0, 0.0, 0.0), length=1.0)
+    W = meshes.wake_rows(w.dm, wake.te)
+    return w, wake, W
+
+
+def _moved(w, wake, x):
+    """the wing with its nodes at x; the wake rows keep their offsets from the trailing edge nodes"""
+    wte = w.dm.wake_te
+    te = meshes.WakeTE(wte.node, x[wte.node].copy(), wte.lines, wte.closed)
+    d = np.array([1.0, 0.0, 0.0])
+    wk = dataclasses.replace(wake, x=te.x[wake.te] + wake.rows[wake.row][:, None] * d)
+    return dataclasses.replace(w, g=dataclasses.replace(w.g, x=x), dm=dataclasses.replace(w.dm, wake_te=te)), wk
+
+
+def _loads(w, wake, W, a):
+    V = np.array([math.cos(a), 0.0, math.sin(a)])
+    eL = np.array([-math.sin(a), 0.0, math.cos(a)])
+    els = api.build_elements(w.g)
+    sig = api.source_strengths(els, V)
+    A, b, _ = api.assemble(w.g, w.dm, els, sig, V, wake=wake)
+    s = api.solve_galerkin(api.factorize_galerkin(w.dm, A, W=W), b)
+    S = w.span * w.chord
+    cp = api.pressure_coefficient(api.gradient_velocity(els, w.dm, s["mu"], V), V)
+    return float(api.pressure_force(els, cp)[0] @ eL / S), float(api.trefftz_drag(w.dm.wake_te, w.dm.K @ s["q"], V) / S)
+
+
+def _nodes(w):
+    rng = np.random.default_rng(1)
+    te = int(w.dm.wake_te.node[len(w.dm.wake_te.node) // 2])
+    tip = int(np.argmax(w.g.x[:, 1]))
+    return sorted(set(rng.choice(w.g.nnode, 6, replace=False).tolist()) | {te, tip})
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gradients_against_finite_differences(case, precision):
+    w, wake, W = case
+    a = math.radians(5.0)
+    out = wing_gradients(w, wake, W, a, precision=precision)
+    CL0, CDi0 = _loads(w, wake, W, a)
+    assert abs(out["CL"] - CL0) <= 1e-6 and abs(out["CDi"] - CDi0) <= 1e-6
+    h = 1e-6 * w.chord
+    for name, k in (("CL", 0), ("CDi", 1)):
+        grad = out["d" + name + "_dx"]
+        scale = np.abs(grad).max()
+        for n in _nodes(w):
+            for c in range(3):
+                xp, xm = w.g.x.copy(), w.g.x.copy()
+                xp[n, c] += h
+                xm[n, c] -= h
+                fp = _loads(*_moved(w, wake, xp), W, a)[k]
+                fm = _loads(*_moved(w, wake, xm), W, a)[k]
+                fd = (fp - fm) / (2 * h)
+                assert abs(grad[n, c] - fd) <= 1e-5 * scale, (name, precision, n, c, grad[n, c], fd, scale)
+        fd = (_loads(w, wake, W, a + 1e-6)[k] - _loads(w, wake, W, a - 1e-6)[k]) / 2e-6
+        da = out["d" + name + "_dalpha"]
+        assert abs(da - fd) <= 1e-5 * max(abs(fd), 1e-3), (name, precision, da, fd)
+
+
+def test_mixed_gradients_match_fp64(case):
+    w, wake, W = case
+    a = math.radians(3.0)
+    g64 = wing_gradients(w, wake, W, a, precision="fp64")
+    g32 = wing_gradients(w, wake, W, a, precision="mixed")
+    for name in ("CL", "CDi"):
+        d = g64["d" + name + "_dx"]
+        assert np.abs(g32["d" + name + "_dx"] - d).max() <= 1e-5 * np.abs(d).max(), name
+        assert abs(g32["d" + name + "_dalpha"] - g64["d" + name + "_dalpha"]) <= 1e-5 * abs(g64["d" + name + "_dalpha"])
+
+
+def test_transposed_solve(case):
+    """M' xi = g through vp_solve_transposed: xi' (M q) = g' q for the solved q of any right hand side"""
+    from vortexpanel_gpu.adjoint import solve_transposed
+    w, wake, W = case
+    V = np.array([1.0, 0.0, 0.1])
+    els = api.build_elements(w.g)
+    A, b, _ = api.assemble(w.g, w.dm, els, api.source_strengths(els, V), V, wake=wake)
+    for precision in ("fp64", "mixed"):
+        F = api.factorize_galerkin(w.dm, A, W=W, precision=precision)
+        rng = np.random.default_rng(4)
+        g = rng.standard_normal(w.dm.nq)
+        g -= g.mean()  # orthogonal to the body's constant mode
+        xi = solve_transposed(F, g)
+        q = api.solve_galerkin(F, b)["q"]
+        # [g; 0]' [q; lambda] = [xi; eta]' M [q; lambda] = xi' (C' b)
+        assert abs(g @ q - xi @ (w.dm.C.T @ b)) <= 1e-9 * np.abs(g).sum() * np.abs(q).max()

@@ -68,13 +68,17 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
     }
     T z = dot(r, S.n);
     T nm = dot(S.n, m) * i4pi;
+    T N = dot(r0, cross(r1, r2));
+    T D = l[0] * l[1] * l[2] + dot(r0, r1) * l[2] + dot(r0, r2) * l[1] + dot(r1, r2) * l[0];
     if (fabs(z) <= plane_tol * S.diam) {
         v3<T> q[3] = {-r0, -r1, -r2};
         sh.Om = side == 0 ? T(0) : T(side) * T(2) * vp_pi<T>() * inplane_fraction_rel(q, S.n, S.area, plane_tol);
     } else {
-        T N = dot(r0, cross(r1, r2));
-        T D = l[0] * l[1] * l[2] + dot(r0, r1) * l[2] + dot(r0, r2) * l[1] + dot(r1, r2) * l[0];
         sh.Om = T(2) * vatan2(N, D);
+    }
+    // 2 atan2(N, D) is smooth across the plane away from the triangle's edges (N = 0, D != 0): in the plane its
+    // derivative along the normal is the one-sided limit of the general formula, which the in-plane branch keeps
+    if (N * N + D * D > T(0)) {
         T h = T(2) / (N * N + D * D);
         T Nb = nm * D * h, Db = -nm * N * h;
         gr[0] += Nb * cross(r1, r2);

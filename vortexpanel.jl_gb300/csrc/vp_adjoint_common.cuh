@@ -30,13 +30,15 @@ __device__ __forceinline__ void adj_zero(AdjSums<T>& s) {
     s.A = T(0);
 }
 
-// add one point: weight Wn = W nu(q), barycentrics l, offsets r_a (exact) or r (multipole), direction m
+// add one point: weight Wn = W nu(q), barycentrics l, offsets r_a (exact) or r (multipole), direction m. Returns
+// s = w·m; *gxo (if given) receives ds/dx.
 template <class T>
-__device__ __forceinline__ void adj_point_exact(AdjSums<T>& acc, const SrcKern<T>& S, T Wn, T l0, T l1, T l2, v3<T> r0,
-                                                v3<T> r1, v3<T> r2, v3<T> r, v3<T> m, int side, T plane_tol) {
+__device__ __forceinline__ T adj_point_exact(AdjSums<T>& acc, const SrcKern<T>& S, T Wn, T l0, T l1, T l2, v3<T> r0,
+                                             v3<T> r1, v3<T> r2, v3<T> r, v3<T> m, int side, T plane_tol,
+                                             v3<T>* gxo = nullptr) {
     v3<T> g0, g1, g2;
     ExactShape<T> sh;
-    sv_exact_vjp(S, r0, r1, r2, r, m, side, plane_tol, g0, g1, g2, sh);
+    T sv = sv_exact_vjp(S, r0, r1, r2, r, m, side, plane_tol, g0, g1, g2, sh);
     const T i4pi = T(1) / (T(4) * vp_pi<T>());
     v3<T> w = (sh.L[0] * S.nu[0] + sh.L[1] * S.nu[1] + sh.L[2] * S.nu[2] + sh.Om * S.n) * i4pi;
     acc.Q += Wn * w;
@@ -52,14 +54,16 @@ __device__ __forceinline__ void adj_point_exact(AdjSums<T>& acc, const SrcKern<T
         acc.N[e] += Wn * sh.dLdlen[e];
     }
     acc.O += Wn * sh.Om;
+    if (gxo) *gxo = gx;
+    return sv;
 }
 
 template <class T>
-__device__ __forceinline__ void adj_point_far(AdjSums<T>& acc, const SrcKern<T>& S, T Wn, T l0, T l1, T l2, v3<T> r,
-                                              v3<T> m) {
+__device__ __forceinline__ T adj_point_far(AdjSums<T>& acc, const SrcKern<T>& S, T Wn, T l0, T l1, T l2, v3<T> r,
+                                           v3<T> m, v3<T>* gxo = nullptr) {
     v3<T> gr, gd[3];
     T ga;
-    sv_far_vjp(S, r, m, gr, gd, ga);
+    T sv = sv_far_vjp(S, r, m, gr, gd, ga);
     acc.Q += Wn * sv_far(S, r);
     acc.Xg[0] += (Wn * l0) * gr;
     acc.Xg[1] += (Wn * l1) * gr;
@@ -67,56 +71,35 @@ __device__ __forceinline__ void adj_point_far(AdjSums<T>& acc, const SrcKern<T>&
     acc.Grf += Wn * gr;
     for (int a = 0; a < 3; ++a) acc.Gd[a] += Wn * gd[a];
     acc.A += Wn * ga;
+    if (gxo) *gxo = gr;
+    return sv;
 }
 
-// the derivative of sum W nu s (at fixed m) with respect to the source's corners v (3), added to g (3)
+// The sums a source collects over all its (test triangle, point) evaluations, with m = n_T x Gamma_S + sigma_S n_T the
+// pair's direction (Gamma_S = sum_b mu_b gamma_b the source sheet's vortex density): exact form Gr (ds/dr_a at fixed
+// shape), Lm_e = sum L_e m, Nm_e = sum dL_e/dlen_e (nu_e·m), Om = sum Omega m; multipole form Grf, Gd, A (as AdjSums);
+// Gb = sum w x n_T and Sb = sum w·n_T (the derivatives with respect to Gamma_S and sigma_S). Every sum carries the
+// point's weight W nu(q).
 template <class T>
-__device__ inline void adj_source_shape(const v3<T>* v, const AdjSums<T>& a, v3<T> m, v3<T>* gout) {
-    const T i4pi = T(1) / (T(4) * vp_pi<T>());
-    v3<T> g[3];
-    // exact form: r_a = x - v_a
-    for (int k = 0; k < 3; ++k) g[k] = T(-1) * a.Gr[k];
-    // multipole form: r = x - c, d_b = v_b - c, c the centroid
-    v3<T> sGd = a.Gd[0] + a.Gd[1] + a.Gd[2];
-    for (int k = 0; k < 3; ++k) g[k] += (T(-1) / T(3)) * a.Grf + a.Gd[k] - (T(1) / T(3)) * sGd;
-    // shape: edges e_e = v_{e+1} - v_e, lengths, normals nu_e = (e_e x n) / len_e, n = nA / |nA|, area = |nA| / 2
-    v3<T> u = v[1] - v[0], w2 = v[2] - v[0];
-    v3<T> nA = cross(u, w2);
-    T A2 = vnorm(nA);
-    v3<T> n = nA / A2;
-    v3<T> nbar = (a.O * i4pi) * m;
-    v3<T> ebar[3];
-    for (int e = 0; e < 3; ++e) {
-        v3<T> ed = v[(e + 1) % 3] - v[e];
-        T len = vnorm(ed);
-        v3<T> nu = cross(ed, n) / len;
-        v3<T> nubar = (a.L[e] * i4pi) * m;
-        T lenbar = -dot(nu, nubar) / len + a.N[e] * dot(nu, m) * i4pi;
-        ebar[e] = cross(n, nubar) / len + (lenbar / len) * ed;
-        nbar += cross(nubar, ed) / len;
-    }
-    v3<T> nAbar = (nbar - dot(nbar, n) * n) / A2 + (T(0.5) * a.A) * n;  // area = |nA| / 2
-    v3<T> ubar = cross(w2, nAbar), w2bar = cross(nAbar, u);
-    g[1] += ubar;
-    g[2] += w2bar;
-    g[0] -= ubar + w2bar;
-    for (int e = 0; e < 3; ++e) {
-        g[(e + 1) % 3] += ebar[e];
-        g[e] -= ebar[e];
-    }
-    for (int k = 0; k < 3; ++k) gout[k] += g[k];
-}
+struct SrcAdj {
+    v3<T> Gr[3], Lm[3], Om, Grf, Gd[3], Gb;
+    T Nm[3], A, Sb;
+};
 
-// FP64 form on corners given as 9 doubles
-__device__ inline void adj_source_shape(const double* xS, const AdjSums<double>& a, v3<double> m, double* gS) {
-    v3<double> v[3] = {mk3(xS[0], xS[1], xS[2]), mk3(xS[3], xS[4], xS[5]), mk3(xS[6], xS[7], xS[8])};
-    v3<double> g[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
-    adj_source_shape(v, a, m, g);
+template <class T>
+__device__ __forceinline__ void src_zero(SrcAdj<T>& s) {
+    v3<T> z = mk3(T(0), T(0), T(0));
     for (int k = 0; k < 3; ++k) {
-        gS[3 * k] += g[k].x;
-        gS[3 * k + 1] += g[k].y;
-        gS[3 * k + 2] += g[k].z;
+        s.Gr[k] = z;
+        s.Lm[k] = z;
+        s.Gd[k] = z;
+        s.Nm[k] = T(0);
     }
+    s.Om = z;
+    s.Grf = z;
+    s.Gb = z;
+    s.A = T(0);
+    s.Sb = T(0);
 }
 
 // derivative of a vector of the unit normal (nbar) and of the area (Abar) of triangle v (3) with respect to its
@@ -145,38 +128,118 @@ __device__ inline void area_vector_grad(const v3<T>* v, v3<T> V, T c, v3<T>* g) 
     g[0] -= ubar + w2bar;
 }
 
-// The derivative of one pair's f = sum W nu w·m, m = n_T x gamma_S + sigma_S n_T, from its sums a:
-// the test triangle's corners (gT), the source's (gS), and d f / d alpha through sigma_S = -V·n_S (dal), for a source
-// sheet with corner values mu (gamma_S = sum_b mu_b gamma_b, gamma_b = -e_b / 2A, e_b the edge opposite corner b) and
-// source strength sigma (body sources: with_sigma).
+// The derivative of a source's sums a with respect to its corners v, added to gout: through the offsets to the
+// corners and the centroid, the edge normals, edge lengths, unit normal and area (the shape, as SourceTriangle builds
+// it: src/kernels/source_triangle.jl:8-26), through Gamma_S = -sum_b mu_b e_b / 2A (e_b the edge opposite corner b)
+// and, for a body source (with_sigma), through sigma_S = -V·n_S; d/dalpha of sigma_S = -dV·n_S is added to *dal.
+template <class T>
+__device__ inline void src_adj_grad(const v3<T>* v, const SrcAdj<T>& a, const T* mu, bool with_sigma, v3<T> V,
+                                    v3<T> dV, v3<T>* gout, T* dal) {
+    const T i4pi = T(1) / (T(4) * vp_pi<T>());
+    v3<T> g[3];
+    // exact form: r_a = x - v_a
+    for (int k = 0; k < 3; ++k) g[k] = T(-1) * a.Gr[k];
+    // multipole form: r = x - c, d_b = v_b - c, c the centroid
+    v3<T> sGd = a.Gd[0] + a.Gd[1] + a.Gd[2];
+    for (int k = 0; k < 3; ++k) g[k] += (T(-1) / T(3)) * a.Grf + a.Gd[k] - (T(1) / T(3)) * sGd;
+    // shape: edges ed_e = v_{e+1} - v_e, lengths, normals nu_e = (ed_e x n) / len_e, n = nA / |nA|, area = |nA| / 2
+    v3<T> nA = cross(v[1] - v[0], v[2] - v[0]);
+    T A2 = vnorm(nA);
+    v3<T> n = nA / A2;
+    v3<T> nbar = i4pi * a.Om;
+    T Abar = a.A;
+    for (int e = 0; e < 3; ++e) {
+        v3<T> ed = v[(e + 1) % 3] - v[e];
+        T len = vnorm(ed);
+        v3<T> nu = cross(ed, n) / len;
+        v3<T> nubar = i4pi * a.Lm[e];
+        T lenbar = -dot(nu, nubar) / len + a.Nm[e] * i4pi;
+        v3<T> ebar = cross(n, nubar) / len + (lenbar / len) * ed;
+        nbar += cross(nubar, ed) / len;
+        g[(e + 1) % 3] += ebar;
+        g[e] -= ebar;
+    }
+    // Gamma_S = -Et / 2A, Et = sum_b mu_b e_b
+    if (mu) {
+        T AS = A2 / T(2);
+        v3<T> Et = mu[0] * (v[2] - v[1]) + mu[1] * (v[0] - v[2]) + mu[2] * (v[1] - v[0]);
+        v3<T> Ebar = (T(-1) / (T(2) * AS)) * a.Gb;
+        Abar += dot(a.Gb, Et) / (T(2) * AS * AS);
+        g[2] += mu[0] * Ebar;
+        g[1] -= mu[0] * Ebar;
+        g[0] += mu[1] * Ebar;
+        g[2] -= mu[1] * Ebar;
+        g[1] += mu[2] * Ebar;
+        g[0] -= mu[2] * Ebar;
+    }
+    if (with_sigma) {
+        nbar += (T(-1) * a.Sb) * V;
+        *dal += -dot(dV, n) * a.Sb;
+    }
+    normal_area_grad(v, nbar, Abar, g);
+    for (int k = 0; k < 3; ++k) gout[k] += g[k];
+}
+
+// a pair's AdjSums (one direction m) as a source's sums; the test normal nT gives Gb and Sb
+template <class T>
+__device__ inline SrcAdj<T> src_of_pair(const v3<T>* xS, const AdjSums<T>& a, v3<T> m, v3<T> nT) {
+    SrcAdj<T> s;
+    v3<T> nA = cross(xS[1] - xS[0], xS[2] - xS[0]);
+    v3<T> n = nA / vnorm(nA);
+    for (int e = 0; e < 3; ++e) {
+        v3<T> ed = xS[(e + 1) % 3] - xS[e];
+        v3<T> nu = cross(ed, n) / vnorm(ed);
+        s.Gr[e] = a.Gr[e];
+        s.Lm[e] = a.L[e] * m;
+        s.Nm[e] = a.N[e] * dot(nu, m);
+        s.Gd[e] = a.Gd[e];
+    }
+    s.Om = a.O * m;
+    s.Grf = a.Grf;
+    s.A = a.A;
+    s.Gb = cross(a.Q, nT);
+    s.Sb = dot(a.Q, nT);
+    return s;
+}
+
+// the derivative of sum W nu s (at fixed m) with respect to the source's corners v (3), added to g (3)
+template <class T>
+__device__ inline void adj_source_shape(const v3<T>* v, const AdjSums<T>& a, v3<T> m, v3<T>* gout) {
+    SrcAdj<T> s = src_of_pair(v, a, m, mk3(T(0), T(0), T(0)));
+    T dal = T(0);
+    src_adj_grad(v, s, (const T*)nullptr, false, m, m, gout, &dal);
+}
+
+// FP64 form on corners given as 9 doubles
+__device__ inline void adj_source_shape(const double* xS, const AdjSums<double>& a, v3<double> m, double* gS) {
+    v3<double> v[3] = {mk3(xS[0], xS[1], xS[2]), mk3(xS[3], xS[4], xS[5]), mk3(xS[6], xS[7], xS[8])};
+    v3<double> g[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
+    adj_source_shape(v, a, m, g);
+    for (int k = 0; k < 3; ++k) {
+        gS[3 * k] += g[k].x;
+        gS[3 * k + 1] += g[k].y;
+        gS[3 * k + 2] += g[k].z;
+    }
+}
+
+// The test side of f = sum W nu s, s = w·m, m = n_T x Gamma_S + sigma_S n_T: the points' positions (Xg, by corner), the
+// unit normal (U = sum W nu ds/dn_T = sum W nu (Gamma_S x w + sigma_S w)) and the area (f / A_T, W = w_q A_T)
+template <class T>
+__device__ inline void test_adj_grad(const v3<T>* xT, const v3<T>* Xg, v3<T> U, T f, v3<T>* gT) {
+    v3<T> nA = cross(xT[1] - xT[0], xT[2] - xT[0]);
+    T AT = vnorm(nA) / T(2);
+    for (int k = 0; k < 3; ++k) gT[k] += Xg[k];
+    normal_area_grad(xT, U, f / AT, gT);
+}
+
+// One pair's derivatives from its sums a: the test triangle's corners (gT), the source's (gS) and d/dalpha (dal),
+// for a source sheet with corner values mu and Gamma_S = gam, source strength sig (body sources: with_sigma).
 template <class T>
 __device__ inline void adj_pair_grad(const v3<T>* xT, const v3<T>* xS, const AdjSums<T>& a, v3<T> m, v3<T> gam, T sig,
-                                     const T* mu, bool with_sigma, v3<T> V, v3<T> eL, v3<T>* gT, v3<T>* gS, T* dal) {
+                                     const T* mu, bool with_sigma, v3<T> V, v3<T> dV, v3<T>* gT, v3<T>* gS, T* dal) {
     v3<T> nT = cross(xT[1] - xT[0], xT[2] - xT[0]);
-    T AT = vnorm(nT) / T(2);
-    nT = nT / (T(2) * AT);
-    T f = dot(a.Q, m);
-    for (int k = 0; k < 3; ++k) gT[k] += a.Xg[k];
-    normal_area_grad(xT, cross(gam, a.Q) + sig * a.Q, f / AT, gT);
-    adj_source_shape(xS, a, m, gS);
-    v3<T> nA = cross(xS[1] - xS[0], xS[2] - xS[0]);
-    T AS = vnorm(nA) / T(2);
-    v3<T> nS = nA / (T(2) * AS);
-    v3<T> gbar = cross(a.Q, nT);
-    v3<T> Et = mu[0] * (xS[2] - xS[1]) + mu[1] * (xS[0] - xS[2]) + mu[2] * (xS[1] - xS[0]);
-    v3<T> Ebar = (T(-1) / (T(2) * AS)) * gbar;
-    T Abar = dot(gbar, Et) / (T(2) * AS * AS);
-    gS[2] += mu[0] * Ebar;
-    gS[1] -= mu[0] * Ebar;
-    gS[0] += mu[1] * Ebar;
-    gS[2] -= mu[1] * Ebar;
-    gS[1] += mu[2] * Ebar;
-    gS[0] -= mu[2] * Ebar;
-    v3<T> nbarS = mk3(T(0), T(0), T(0));
-    if (with_sigma) {
-        T sbar = dot(a.Q, nT);
-        nbarS = T(-1) * sbar * V;
-        *dal += -dot(eL, nS) * sbar;
-    }
-    normal_area_grad(xS, nbarS, Abar, gS);
+    nT = nT / vnorm(nT);
+    test_adj_grad(xT, a.Xg, cross(gam, a.Q) + sig * a.Q, dot(a.Q, m), gT);
+    SrcAdj<T> s = src_of_pair(xS, a, m, nT);
+    src_adj_grad(xS, s, mu, with_sigma, V, dV, gS, dal);
 }

@@ -1,0 +1,687 @@
+// The adjoint pair derivatives: for fixed adjoint values nu (one per row slot) and unknowns mu (one per column), the
+// derivative of F = nu' (A(x) mu - b(x)) with respect to the body nodes, the wake nodes and the angle of attack
+// (through V∞(alpha) and sigma = -V∞·n), with the quadrature of the assembly kept fixed. With the adjoint solution
+// nu = C xi of the transposed bordered system, dJ/dx = dJ/dx|_q - dF/dx (src/assembly/assemble.jl:377-447 is the
+// forward map; the reference differentiates it with ForwardDiff duals through the same pair rules).
+//
+// A pair (T, S) contributes f = sum_q W_q nu(q) w_S(x_q)·m, m = n_T x Gamma_S + sigma_S n_T, where nu(q) = sum_a
+// nu_a psi_a(q) and Gamma_S = sum_b mu_b gamma_b; the freestream adds (V∞·n_T A_T) sum_a nu_a ti_a. Per point the
+// kernels evaluate s = w·m with its reverse-mode derivatives (vp_adjoint.cuh) and collect:
+//   - on the test side, per test triangle (TA, 13 doubles): the derivative with respect to the points' positions by
+//     corner (9), with respect to n_T (3) and f itself (for the area);
+//   - on the source side, per source triangle (SA, 41 doubles): the sums of SrcAdj (vp_adjoint_common.cuh), which
+//     a last kernel turns into derivatives with respect to the source's corners once per source.
+// Kernels (one CUDA stream):
+//   1. far tier: one CTA per (128-source tile, chunk of test tiles), one thread per source keeping its sums in
+//      registers across the chunk; test-side sums reduced over the CTA per test and added with FP64 atomics;
+//   2. non-far pairs: one warp per test triangle, every pair's rule built and walked as in the assembly (the same
+//      templates with the adjoint accumulator), per-pair warp sums, test side in registers, source side added to SA;
+//      the tip filaments and the freestream term;
+//   3. finish: one thread per triangle turns TA and SA into node derivatives.
+#include "vp_pairs.cuh"
+
+namespace {
+
+constexpr int NSA = 41;  // SrcAdj fields
+constexpr int NTA = 13;  // test side: Xg (9), U (3), f (1)
+
+// SrcAdj in a flat order: Gr (9), Lm (9), Om (3), Grf (3), Gd (9), Gb (3), Nm (3), A, Sb
+template <class T>
+__device__ __forceinline__ void sa_flat(const SrcAdj<T>& s, T* f) {
+    for (int k = 0; k < 3; ++k) {
+        f[3 * k] = s.Gr[k].x; f[3 * k + 1] = s.Gr[k].y; f[3 * k + 2] = s.Gr[k].z;
+        f[9 + 3 * k] = s.Lm[k].x; f[10 + 3 * k] = s.Lm[k].y; f[11 + 3 * k] = s.Lm[k].z;
+        f[24 + 3 * k] = s.Gd[k].x; f[25 + 3 * k] = s.Gd[k].y; f[26 + 3 * k] = s.Gd[k].z;
+        f[36 + k] = s.Nm[k];
+    }
+    f[18] = s.Om.x; f[19] = s.Om.y; f[20] = s.Om.z;
+    f[21] = s.Grf.x; f[22] = s.Grf.y; f[23] = s.Grf.z;
+    f[33] = s.Gb.x; f[34] = s.Gb.y; f[35] = s.Gb.z;
+    f[39] = s.A;
+    f[40] = s.Sb;
+}
+
+__device__ __forceinline__ SrcAdj<double> sa_unflat(const double* f) {
+    SrcAdj<double> s;
+    for (int k = 0; k < 3; ++k) {
+        s.Gr[k] = mk3(f[3 * k], f[3 * k + 1], f[3 * k + 2]);
+        s.Lm[k] = mk3(f[9 + 3 * k], f[10 + 3 * k], f[11 + 3 * k]);
+        s.Gd[k] = mk3(f[24 + 3 * k], f[25 + 3 * k], f[26 + 3 * k]);
+        s.Nm[k] = f[36 + k];
+    }
+    s.Om = mk3(f[18], f[19], f[20]);
+    s.Grf = mk3(f[21], f[22], f[23]);
+    s.Gb = mk3(f[33], f[34], f[35]);
+    s.A = f[39];
+    s.Sb = f[40];
+    return s;
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// far tier
+
+struct AdjFarArgs {
+    int ntest, nq, ntiles_test, tiles_per_chunk;
+    const double* tq;    // test far points (ntest x NQMAX x 3)
+    const double* tw;    // w_q A_T psi_a (ntest x NQMAX x 3)
+    const TriGeo* tgeo;
+    const CentF* tcent;
+    const double* lam;   // far rule barycentrics (nq x 3)
+    const double* nu;    // row slot values
+    int nset;
+    int nsrc[2], ntile[2];
+    const void* soa[2];  // NFIELD x pad (T), as the assembly's far kernel
+    const void* gam[2];  // Gamma_S, 3 x pad (T)
+    int pad[2];
+    const CentF* scent[2];
+    const TriGeo* sgeo[2];
+    double* SA[2];
+    double* TA;
+    float ratio32;
+    double ratio, kernel_far;
+};
+
+template <class T>
+struct AdjFarTest {
+    T xh[NQMAX][3], xl[NQMAX][3];
+    T Wn[NQMAX];  // w_q A_T nu(q)
+    T n[3];
+    CentF cf;
+    double c64[3];
+    double diam64;
+    int t;  // -1: past the end
+};
+
+template <class T, int TT>
+__global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
+    __shared__ AdjFarTest<T> ts[TT];
+    __shared__ T lam[NQMAX][3];
+    __shared__ T red[TT][FAR_NT / 32][NTA];
+    const T i4pi = T(1) / (T(4) * vp_pi<T>());
+    int bx = blockIdx.x, set = 0;
+    if (bx >= a.ntile[0]) {
+        set = 1;
+        bx -= a.ntile[0];
+    }
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int s = bx * FAR_NT + tid;
+    const bool sv = s < a.nsrc[set];
+    const T* soa = (const T*)a.soa[set];
+    const int pad = a.pad[set];
+    SrcKern<T> S;
+    v3<T> ch = mk3(T(0), T(0), T(0)), cl = ch, G = ch;
+    T sig = T(0);
+    CentF scf{};
+    if (sv) {
+#define F(f) soa[size_t(f) * pad + s]
+        ch = mk3(F(0), F(1), F(2));
+        cl = mk3(F(3), F(4), F(5));
+        S.diam = F(6);
+        S.area = F(7);
+        sig = F(8);
+        for (int k = 0; k < 3; ++k) {
+            S.d[k] = mk3(F(9 + 3 * k), F(10 + 3 * k), F(11 + 3 * k));
+            S.nu[k] = mk3(F(18 + 3 * k), F(19 + 3 * k), F(20 + 3 * k));
+            S.len[k] = F(27 + k);
+        }
+        S.n = mk3(F(30), F(31), F(32));
+#undef F
+        const T* g = (const T*)a.gam[set];
+        G = mk3(g[s], g[size_t(pad) + s], g[2 * size_t(pad) + s]);
+        scf = a.scent[set][s];
+    }
+    SrcAdj<T> acc;
+    src_zero(acc);
+    if (tid < 3 * a.nq) lam[tid / 3][tid % 3] = T(a.lam[tid]);
+    const T fd = T(a.kernel_far) * (sv ? S.diam : T(0));
+    const int tile0 = blockIdx.y * a.tiles_per_chunk;
+    const int tile1 = min(tile0 + a.tiles_per_chunk, a.ntiles_test);
+    for (int tile = tile0; tile < tile1; ++tile) {
+        __syncthreads();
+        for (int i = tid; i < TT; i += FAR_NT) {
+            const int t = tile * TT + i;
+            AdjFarTest<T>& q = ts[i];
+            q.t = t < a.ntest ? t : -1;
+            if (q.t >= 0) {
+                const TriGeo& g = a.tgeo[t];
+                const double nv[3] = {a.nu[g.slot[0]], a.nu[g.slot[1]], a.nu[g.slot[2]]};
+                for (int p = 0; p < a.nq; ++p) {
+                    const double* tq = a.tq + (size_t(t) * NQMAX + p) * 3;
+                    const double* tw = a.tw + (size_t(t) * NQMAX + p) * 3;
+                    for (int k = 0; k < 3; ++k) {
+                        T h = T(tq[k]);
+                        q.xh[p][k] = h;
+                        q.xl[p][k] = T(tq[k] - double(h));
+                    }
+                    q.Wn[p] = T(nv[0] * tw[0] + nv[1] * tw[1] + nv[2] * tw[2]);
+                }
+                for (int k = 0; k < 3; ++k) {
+                    q.n[k] = T(g.n[k]);
+                    q.c64[k] = g.c[k];
+                }
+                q.diam64 = g.diam;
+                q.cf = a.tcent[t];
+            }
+        }
+        __syncthreads();
+#pragma unroll 1
+        for (int i = 0; i < TT; ++i) {
+            const AdjFarTest<T>& q = ts[i];
+            bool far = false;
+            if (sv && q.t >= 0) {
+                if (sizeof(T) == 8) {
+                    far = far_exact64(q.c64, q.diam64, a.sgeo[set][s].c, a.sgeo[set][s].diam, a.ratio);
+                } else {
+                    int f = far_test32(q.cf, scf, a.ratio32);
+                    if (f < 0) f = far_exact64(q.c64, q.diam64, a.sgeo[set][s].c, a.sgeo[set][s].diam, a.ratio);
+                    far = f == 1;
+                }
+            }
+            v3<T> Xg[3] = {mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0))};
+            v3<T> U = mk3(T(0), T(0), T(0));
+            T fs = T(0);
+            if (far) {
+                const v3<T> nT = mk3(q.n[0], q.n[1], q.n[2]);
+                const v3<T> m = cross(nT, G) + sig * nT;
+                for (int p = 0; p < a.nq; ++p) {
+                    v3<T> r = mk3((q.xh[p][0] - ch.x) + (q.xl[p][0] - cl.x), (q.xh[p][1] - ch.y) + (q.xl[p][1] - cl.y),
+                                  (q.xh[p][2] - ch.z) + (q.xl[p][2] - cl.z));
+                    const T Wn = q.Wn[p];
+                    v3<T> w, gx;
+                    T sval;
+                    if (dot(r, r) > fd * fd) {
+                        v3<T> gr, gd[3];
+                        T ga;
+                        sval = sv_far_vjp(S, r, m, gr, gd, ga);
+                        w = sv_far(S, r);
+                        acc.Grf += Wn * gr;
+                        for (int k = 0; k < 3; ++k) acc.Gd[k] += Wn * gd[k];
+                        acc.A += Wn * ga;
+                        gx = gr;
+                    } else {
+                        v3<T> g0, g1, g2;
+                        ExactShape<T> sh;
+                        sval = sv_exact_vjp(S, r - S.d[0], r - S.d[1], r - S.d[2], r, m, 0, T(1e-12), g0, g1, g2, sh);
+                        w = (sh.L[0] * S.nu[0] + sh.L[1] * S.nu[1] + sh.L[2] * S.nu[2] + sh.Om * S.n) * i4pi;
+                        acc.Gr[0] += Wn * g0;
+                        acc.Gr[1] += Wn * g1;
+                        acc.Gr[2] += Wn * g2;
+                        for (int e = 0; e < 3; ++e) {
+                            acc.Lm[e] += (Wn * sh.L[e]) * m;
+                            acc.Nm[e] += Wn * sh.dLdlen[e] * dot(S.nu[e], m);
+                        }
+                        acc.Om += (Wn * sh.Om) * m;
+                        gx = g0 + g1 + g2;
+                    }
+                    acc.Gb += Wn * cross(w, nT);
+                    acc.Sb += Wn * dot(w, nT);
+                    for (int k = 0; k < 3; ++k) Xg[k] += (Wn * lam[p][k]) * gx;
+                    U += Wn * (cross(G, w) + sig * w);
+                    fs += Wn * sval;
+                }
+            }
+            // the test side of this test: sum over the warp, then over the CTA's warps below
+            T v[NTA] = {Xg[0].x, Xg[0].y, Xg[0].z, Xg[1].x, Xg[1].y, Xg[1].z, Xg[2].x, Xg[2].y, Xg[2].z, U.x, U.y, U.z, fs};
+            if (__any_sync(0xffffffffu, far)) {
+#pragma unroll
+                for (int k = 0; k < NTA; ++k)
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+            }
+            if (lane == 0)
+#pragma unroll
+                for (int k = 0; k < NTA; ++k) red[i][wid][k] = v[k];
+        }
+        __syncthreads();
+        for (int k = tid; k < TT * NTA; k += FAR_NT) {
+            const int i = k / NTA, f = k - i * NTA;
+            if (ts[i].t < 0) continue;
+            T v = T(0);
+            for (int w = 0; w < FAR_NT / 32; ++w) v += red[i][w][f];
+            if (v != T(0)) atomicAdd(a.TA + size_t(ts[i].t) * NTA + f, double(v));
+        }
+    }
+    if (sv) {
+        T f[NSA];
+        sa_flat(acc, f);
+        double* dst = a.SA[set] + size_t(s) * NSA;
+#pragma unroll
+        for (int k = 0; k < NSA; ++k)
+            if (f[k] != T(0)) atomicAdd(dst + k, double(f[k]));
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// non-far pairs, tip filaments and freestream: one warp per test triangle
+
+struct AdjExtra {
+    const double* nu;     // row slot values
+    const double* mu;     // column values (body slots, then wake nodes)
+    const double* gam_b;  // Gamma_S of the body triangles (3 each)
+    const double* gam_w;  // and of the wake triangles
+    double V[3], dV[3];
+    double* SA[2];
+    double* TA;
+    double* gx;           // body node derivatives (3 each)
+    double* gwx;          // wake node derivatives (3 each)
+    double* dal;
+};
+
+// this lane's rule-geometry derivative (direction lane < 18) to the test triangle's nodes and the source's
+__device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjExtra& x, const TriGeo& T, const TriGeo* S, bool wake) {
+    const int d = pc.lane;
+    if (d < 18 && pc.gdir != 0.0) {
+        if (d < 9)
+            atomicAdd(x.gx + 3 * T.node[d / 3] + d % 3, pc.gdir);
+        else if (S)
+            atomicAdd((wake ? x.gwx + 3 * S->slot[(d - 9) / 3] : x.gx + 3 * S->node[(d - 9) / 3]) + (d - 9) % 3, pc.gdir);
+    }
+    pc.gdir = 0;
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, AdjExtra x) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int idx = blockIdx.x * NEAR_WARPS + w;
+    if (idx >= a.ntests) return;
+    const int t = a.tests[idx];
+    const TriGeo& T = a.tri[t];
+    PairCtx pc;
+    pc.a = &a;
+    pc.T = &T;
+    pc.sh = &shm[w];
+    pc.lane = lane;
+    pc.nleaf = 0;
+    pc.nq64 = 0;
+    pc.fp32 = 0;
+    for (int k = 0; k < 3; ++k) {
+        pc.nu[k] = x.nu[T.slot[k]];
+        pc.Xc[k] = ld3(T.x + 3 * k) - ld3(T.c);
+        pc.Xcf[k] = mk3(float(pc.Xc[k].x), float(pc.Xc[k].y), float(pc.Xc[k].z));
+    }
+    pc.dep = 0;
+    pc.gdir = 0;
+    const v3<double> nT = ld3(T.n);
+    v3<double> Xg[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
+    v3<double> U = mk3(0.0, 0.0, 0.0);
+    double fs = 0, dal = 0;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+    const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int set = 0; set < 2; ++set) {
+        const bool wake = set == 1;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
+        const long long e1 = wake ? a.wf_ptr[t + 1] : a.nf_ptr[t + 1];
+        const int* list = wake ? a.wf_src : a.nf_src;
+        for (long long e = e0; e < e1; ++e) {
+            const int s = list[e];
+            const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
+            const double* gp = (wake ? x.gam_w : x.gam_b) + 3 * size_t(s);
+            const v3<double> G = mk3(gp[0], gp[1], gp[2]);
+            const double sig = wake ? 0.0 : S.sigma;
+            pc.m = cross(nT, G) + sig * nT;
+            pc.mf = mk3(float(pc.m.x), float(pc.m.y), float(pc.m.z));
+            AdjAcc acc = {};
+            pc.kind = 0;
+            pc.npts = 0;
+            pc.n64 = 0;
+            pc.nleaf = 0;
+            pc.nq64 = 0;
+            int tier = tri_pair(pc, acc, t, s, wake);
+            flush_gdir(pc, x, T, &S, wake);
+            fold32(acc);
+            adj_warp_sum(acc.d);
+            const AdjSums<double>& d = acc.d;
+            for (int k = 0; k < 3; ++k) Xg[k] += d.Xg[k];
+            U += cross(G, d.Q) + sig * d.Q;
+            fs += dot(d.Q, pc.m);
+            // the source side: lane k adds field k
+            v3<double> xS[3];
+            tri_corners(S, xS);
+            SrcAdj<double> sa = src_of_pair(xS, d, pc.m, nT);
+            double f[NSA];
+            sa_flat(sa, f);
+            double* dst = x.SA[set] + size_t(s) * NSA;
+            double mine = 0, mine2 = 0;
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k == lane) mine = f[k];
+#pragma unroll
+            for (int k = 32; k < NSA; ++k)
+                if (k - 32 == lane) mine2 = f[k];
+            if (mine != 0.0) atomicAdd(dst + lane, mine);
+            if (lane < NSA - 32 && mine2 != 0.0) atomicAdd(dst + 32 + lane, mine2);
+            __syncwarp();
+            P[tier] += 1;
+            Q[tier] += pc.npts;
+            Q64 += pc.n64;
+        }
+    }
+    // tip filaments (assemble.jl:344-354), FP64: f = sum W nu (mu_a va + mu_b vb)·n_T
+    for (int fi = 0; fi < a.nfil; ++fi) {
+        const int ia = a.fil[2 * fi], ib = a.fil[2 * fi + 1];
+        v3<double> fa = ld3(a.wx + 3 * ia), fb = ld3(a.wx + 3 * ib);
+        if (lane == 0) {
+            for (int k = 0; k < 3; ++k) {
+                pc.sh->E[9 * k + 0] = T.x[3 * k + 0] - fa.x;
+                pc.sh->E[9 * k + 1] = T.x[3 * k + 1] - fa.y;
+                pc.sh->E[9 * k + 2] = T.x[3 * k + 2] - fa.z;
+                pc.sh->E[9 * k + 3] = T.x[3 * k + 0] - fb.x;
+                pc.sh->E[9 * k + 4] = T.x[3 * k + 1] - fb.y;
+                pc.sh->E[9 * k + 5] = T.x[3 * k + 2] - fb.z;
+            }
+        }
+        __syncwarp();
+        AdjAcc acc = {};
+        pc.kind = 1;
+        pc.npts = 0;
+        pc.n64 = 0;
+        pc.side = 0;
+        pc.fp32 = 0;
+        pc.mua = x.mu[a.nslot + ia];
+        pc.mub = x.mu[a.nslot + ib];
+        const double L = vnorm(fb - fa);
+        int tier;
+        if (vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, L)) {
+            tier = TIER_FAR;
+            emit_rule(pc, acc, R_FAR, corners, 1.0);
+        } else {
+            int kv = -1;
+            for (int k = 0; k < 3 && kv < 0; ++k)
+                if (fmin(vnorm(ld3(T.x + 3 * k) - fa), vnorm(ld3(T.x + 3 * k) - fb)) <= 1e-12 * T.diam) kv = k;
+            if (kv >= 0) {
+                tier = TIER_VERTEX;
+                vertex_rule(pc, acc, kv);
+            } else {
+                tier = TIER_NEAR;
+                SrcRef src{1, nullptr, fa, fb};
+                near_pieces(pc, acc, src, corners, 1.0, a.near_depth);
+                flush_leaves(pc, acc);
+            }
+        }
+        flush_gdir(pc, x, T, nullptr, false);
+        adj_warp_sum(acc.d);
+        const AdjSums<double>& d = acc.d;
+        for (int k = 0; k < 3; ++k) Xg[k] += d.Xg[k];
+        U += d.Q;
+        fs += dot(d.Q, nT);
+        if (lane < 3) {
+            const double ga[3] = {d.Gr[0].x, d.Gr[0].y, d.Gr[0].z}, gb[3] = {d.Gr[1].x, d.Gr[1].y, d.Gr[1].z};
+            atomicAdd(x.gwx + 3 * ia + lane, -ga[lane]);
+            atomicAdd(x.gwx + 3 * ib + lane, -gb[lane]);
+        }
+        __syncwarp();
+        P[tier] += 1;
+        Q[tier] += pc.npts;
+        Q64 += pc.n64;
+    }
+    // freestream (assemble.jl:422): (V·n_T) A_T sum_a nu_a ti_a
+    {
+        const double c = (pc.nu[0] * a.tint[0] + pc.nu[1] * a.tint[1] + pc.nu[2] * a.tint[2]) * T.area;
+        const v3<double> V = mk3(x.V[0], x.V[1], x.V[2]), dV = mk3(x.dV[0], x.dV[1], x.dV[2]);
+        U += c * V;
+        fs += c * dot(V, nT);
+        dal += c * dot(dV, nT);
+    }
+    const double v[NTA] = {Xg[0].x, Xg[0].y, Xg[0].z, Xg[1].x, Xg[1].y, Xg[1].z, Xg[2].x, Xg[2].y, Xg[2].z,
+                           U.x,     U.y,     U.z,     fs};
+    double mine = 0;
+#pragma unroll
+    for (int k = 0; k < NTA; ++k)
+        if (k == lane) mine = v[k];
+    if (lane < NTA && mine != 0.0) atomicAdd(x.TA + size_t(t) * NTA + lane, mine);
+    if (lane == 0) {
+        atomicAdd(x.dal, dal);
+        for (int k = 0; k < 6; ++k) {
+            if (P[k]) atomicAdd(a.stats + k, P[k]);
+            if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
+        }
+        if (Q64) atomicAdd(a.stats + 12, Q64);
+    }
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// finish: node derivatives from the per-triangle sums, one thread per triangle (body, then wake)
+
+struct AdjFinish {
+    const TriGeo* tri;
+    const TriGeo* wtri;
+    int ntri, nwtri, nslot;
+    const double* TA;
+    const double* SA[2];
+    const double* mu;
+    double V[3], dV[3];
+    double* gx;   // body node derivatives (3 each)
+    double* gwx;  // wake node derivatives
+    double* dal;
+};
+
+__global__ void adj_finish_kernel(AdjFinish f) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double dal = 0;
+    if (i < f.ntri + f.nwtri) {
+        const bool wake = i >= f.ntri;
+        const int s = wake ? i - f.ntri : i;
+        const TriGeo& g = wake ? f.wtri[s] : f.tri[s];
+        v3<double> v[3], gr[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
+        tri_corners(g, v);
+        if (!wake) {
+            const double* ta = f.TA + size_t(s) * NTA;
+            v3<double> Xg[3] = {mk3(ta[0], ta[1], ta[2]), mk3(ta[3], ta[4], ta[5]), mk3(ta[6], ta[7], ta[8])};
+            test_adj_grad(v, Xg, mk3(ta[9], ta[10], ta[11]), ta[12], gr);
+        }
+        const SrcAdj<double> sa = sa_unflat(f.SA[wake ? 1 : 0] + size_t(s) * NSA);
+        double mu[3];
+        for (int k = 0; k < 3; ++k) mu[k] = f.mu[(wake ? f.nslot : 0) + g.slot[k]];
+        src_adj_grad(v, sa, mu, !wake, mk3(f.V[0], f.V[1], f.V[2]), mk3(f.dV[0], f.dV[1], f.dV[2]), gr, &dal);
+        double* dst = wake ? f.gwx : f.gx;
+        for (int k = 0; k < 3; ++k) {
+            const int node = wake ? g.slot[k] : g.node[k];
+            atomicAdd(dst + 3 * node, gr[k].x);
+            atomicAdd(dst + 3 * node + 1, gr[k].y);
+            atomicAdd(dst + 3 * node + 2, gr[k].z);
+        }
+    }
+    dal = warp_sum(dal);
+    if ((threadIdx.x & 31) == 0 && dal != 0.0) atomicAdd(f.dal, dal);
+}
+
+template <class T>
+void fill_gam(const std::vector<TriGeo>& g, int n, const double* mu, int col0, int pad, std::vector<T>& out) {
+    out.assign(size_t(3) * std::max(pad, 1), T(0));
+    for (int s = 0; s < n; ++s)
+        for (int k = 0; k < 3; ++k) {
+            double v = 0;
+            for (int b = 0; b < 3; ++b) v += mu[col0 + g[s].slot[b]] * g[s].gam[3 * b + k];
+            out[size_t(k) * pad + s] = T(v);
+        }
+}
+
+template <class T, int TT>
+int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const double* d_nu, const double* mu,
+                double* d_SA0, double* d_SA1, double* d_TA, DevList& dl) {
+    AdjFarArgs fa{};
+    fa.ntest = in.ntri;
+    fa.nq = ps.nq;
+    fa.ntiles_test = (in.ntri + TT - 1) / TT;
+    fa.tq = ps.d_tq;
+    fa.tw = ps.d_tw;
+    fa.tgeo = ps.d_tg;
+    fa.tcent = ps.d_tc;
+    fa.nu = d_nu;
+    fa.nset = in.nwtri > 0 ? 2 : 1;
+    fa.SA[0] = d_SA0;
+    fa.SA[1] = d_SA1;
+    fa.TA = d_TA;
+    fa.ratio32 = ps.ratio32;
+    fa.ratio = in.o->far_ratio;
+    fa.kernel_far = in.o->kernel_far;
+    int r;
+    {
+        std::vector<double> lam(3 * NQMAX, 0.0);
+        for (int p = 0; p < ps.nq; ++p) {
+            lam[3 * p] = ps.rfar[p].l0;
+            lam[3 * p + 1] = ps.rfar[p].l1;
+            lam[3 * p + 2] = ps.rfar[p].l2;
+        }
+        double* d;
+        if ((r = dl.up(ctx, &d, lam))) return r;
+        fa.lam = d;
+    }
+    const std::vector<TriGeo>* sets[2] = {&ps.tg, &ps.wg};
+    const int nsrc[2] = {in.ntri, in.nwtri};
+    int tiles = 0;
+    for (int set = 0; set < fa.nset; ++set) {
+        std::vector<TriGeo> g(sets[set]->begin(), sets[set]->begin() + nsrc[set]);
+        std::vector<T> soa, gam;
+        fill_soa(g, soa, fa.pad[set]);
+        fill_gam(g, nsrc[set], mu, set == 0 ? 0 : in.nslot, fa.pad[set], gam);
+        T *d_soa, *d_gam;
+        if ((r = dl.up(ctx, &d_soa, soa)) || (r = dl.up(ctx, &d_gam, gam))) return r;
+        fa.soa[set] = d_soa;
+        fa.gam[set] = d_gam;
+        fa.nsrc[set] = nsrc[set];
+        fa.ntile[set] = (nsrc[set] + FAR_NT - 1) / FAR_NT;
+        fa.scent[set] = set == 0 ? ps.d_tc : ps.d_wc;
+        fa.sgeo[set] = set == 0 ? ps.d_tg : ps.d_wg;
+        tiles += fa.ntile[set];
+    }
+    // enough CTAs for a few per SM: split the test tiles into chunks
+    int chunks = std::max(1, std::min(fa.ntiles_test, (6 * ctx->nsm + tiles - 1) / std::max(tiles, 1)));
+    fa.tiles_per_chunk = (fa.ntiles_test + chunks - 1) / chunks;
+    chunks = (fa.ntiles_test + fa.tiles_per_chunk - 1) / fa.tiles_per_chunk;
+    adj_far_kernel<T, TT><<<dim3(tiles, chunks), FAR_NT, 0, ctx->stream>>>(fa);
+    ctx->launches++;
+    VP_CUDA(ctx, cudaGetLastError());
+    return VP_OK;
+}
+
+}  // namespace
+
+int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
+                    const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
+                    const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
+                    const int* fil, const double* nu, const double* mu, const double* dvinf, double* grad_x,
+                    double* grad_wx, double* dalpha, vp_assembly_stats* stats) {
+    auto t0 = std::chrono::steady_clock::now();
+    if (!nu || !mu || !dvinf || !grad_x || !dalpha || (nwnode > 0 && !grad_wx))
+        return vp_fail(ctx, VP_ERR_ARG, "null argument");
+    const PairInput in{o,     nnode, x,     ntri, tris,  corner_slot, nslot, ntouch, touch_pairs,
+                       sigma, vinf,  nwnode, wx,  nwtri, wtris,       nfil,  fil};
+    PairSetup ps;
+    int r = setup_pairs(ctx, in, PH_ADJOINT, PH_ADJOINT, ps);
+    if (r) return r;
+    DevList& dl = ps.dl;
+    const int ncols = ps.ncols;
+    vp_phase_begin(ctx, PH_ADJOINT);
+    double *d_nu, *d_mu, *d_SA0, *d_SA1, *d_TA, *d_gx, *d_gwx, *d_dal, *d_gamb, *d_gamw;
+    unsigned long long* d_stats;
+    std::vector<double> hnu(nu, nu + nslot), hmu(mu, mu + ncols);
+    std::vector<double> gamb(size_t(3) * ntri), gamw(size_t(3) * std::max(nwtri, 1), 0.0);
+    for (int s = 0; s < ntri; ++s)
+        for (int k = 0; k < 3; ++k) {
+            double v = 0;
+            for (int b = 0; b < 3; ++b) v += mu[ps.tg[s].slot[b]] * ps.tg[s].gam[3 * b + k];
+            gamb[3 * size_t(s) + k] = v;
+        }
+    for (int s = 0; s < nwtri; ++s)
+        for (int k = 0; k < 3; ++k) {
+            double v = 0;
+            for (int b = 0; b < 3; ++b) v += mu[nslot + ps.wg[s].slot[b]] * ps.wg[s].gam[3 * b + k];
+            gamw[3 * size_t(s) + k] = v;
+        }
+    if ((r = dl.up(ctx, &d_nu, hnu)) || (r = dl.up(ctx, &d_mu, hmu)) || (r = dl.up(ctx, &d_gamb, gamb)) ||
+        (r = dl.up(ctx, &d_gamw, gamw)) || (r = dl.alloc(ctx, &d_SA0, size_t(NSA) * ntri)) ||
+        (r = dl.alloc(ctx, &d_SA1, size_t(NSA) * std::max(nwtri, 1))) || (r = dl.alloc(ctx, &d_TA, size_t(NTA) * ntri)) ||
+        (r = dl.alloc(ctx, &d_gx, size_t(3) * nnode)) || (r = dl.alloc(ctx, &d_gwx, size_t(3) * std::max(nwnode, 1))) ||
+        (r = dl.alloc(ctx, &d_dal, 1)) || (r = dl.alloc(ctx, &d_stats, 13)))
+        return r;
+    VP_CUDA(ctx, cudaMemsetAsync(d_SA0, 0, sizeof(double) * NSA * ntri, ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_SA1, 0, sizeof(double) * NSA * std::max(nwtri, 1), ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_TA, 0, sizeof(double) * NTA * ntri, ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_gx, 0, sizeof(double) * 3 * nnode, ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_gwx, 0, sizeof(double) * 3 * std::max(nwnode, 1), ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_dal, 0, sizeof(double), ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
+    // far tier
+    r = ps.mixed ? run_adj_far<float, 8>(ctx, ps, in, d_nu, mu, d_SA0, d_SA1, d_TA, dl)
+                 : run_adj_far<double, 4>(ctx, ps, in, d_nu, mu, d_SA0, d_SA1, d_TA, dl);
+    if (r) return r;
+    // non-far pairs, filaments, freestream
+    {
+        std::vector<int> all(ntri);
+        std::iota(all.begin(), all.end(), 0);
+        int* d_tests;
+        if ((r = dl.up(ctx, &d_tests, all))) return r;
+        NearArgs na = near_args(ps, in);
+        na.tests = d_tests;
+        na.ntests = ntri;
+        na.stats = d_stats;
+        AdjExtra ex{};
+        ex.nu = d_nu;
+        ex.mu = d_mu;
+        ex.gam_b = d_gamb;
+        ex.gam_w = d_gamw;
+        for (int k = 0; k < 3; ++k) {
+            ex.V[k] = vinf[k];
+            ex.dV[k] = dvinf[k];
+        }
+        ex.SA[0] = d_SA0;
+        ex.SA[1] = d_SA1;
+        ex.TA = d_TA;
+        ex.gx = d_gx;
+        ex.gwx = d_gwx;
+        ex.dal = d_dal;
+        adj_near_kernel<<<(ntri + NEAR_WARPS - 1) / NEAR_WARPS, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, ex);
+        ctx->launches++;
+        VP_CUDA(ctx, cudaGetLastError());
+    }
+    // node derivatives
+    {
+        AdjFinish f{};
+        f.tri = ps.d_tg;
+        f.wtri = ps.d_wg;
+        f.ntri = ntri;
+        f.nwtri = nwtri;
+        f.nslot = nslot;
+        f.TA = d_TA;
+        f.SA[0] = d_SA0;
+        f.SA[1] = d_SA1;
+        f.mu = d_mu;
+        for (int k = 0; k < 3; ++k) {
+            f.V[k] = vinf[k];
+            f.dV[k] = dvinf[k];
+        }
+        f.gx = d_gx;
+        f.gwx = d_gwx;
+        f.dal = d_dal;
+        const int n = ntri + nwtri;
+        adj_finish_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(f);
+        ctx->launches++;
+        VP_CUDA(ctx, cudaGetLastError());
+    }
+    vp_phase_end(ctx);
+    unsigned long long hs[13];
+    VP_CUDA(ctx, vp_d2h(ctx, grad_x, d_gx, sizeof(double) * 3 * nnode));
+    if (nwnode > 0) VP_CUDA(ctx, vp_d2h(ctx, grad_wx, d_gwx, sizeof(double) * 3 * nwnode));
+    VP_CUDA(ctx, vp_d2h(ctx, dalpha, d_dal, sizeof(double)));
+    VP_CUDA(ctx, vp_d2h(ctx, hs, d_stats, sizeof(hs)));
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("adjoint kernels: ") + cudaGetErrorString(e));
+    if (stats) {
+        const int nq = ps.nq;
+        long long total = (long long)ntri * (ntri + nwtri) + (long long)ntri * nfil;
+        long long nonfar = 0;
+        for (int k = 0; k < 6; ++k) {
+            stats->pairs[k] = (long long)hs[k];
+            stats->points[k] = (long long)hs[6 + k];
+            if (k != TIER_FAR) nonfar += (long long)hs[k];
+        }
+        long long far_fil = (long long)hs[TIER_FAR];
+        long long far_tri = total - nonfar - far_fil;
+        stats->pairs[TIER_FAR] = far_tri + far_fil;
+        stats->points[TIER_FAR] = (long long)hs[6 + TIER_FAR] + far_tri * nq;
+        stats->points_fp64 = (long long)hs[12] + (ps.mixed ? 0 : far_tri * nq);
+        stats->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return VP_OK;
+}

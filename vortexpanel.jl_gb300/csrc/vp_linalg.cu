@@ -746,6 +746,32 @@ extern "C" int vp_solve(vp_ctx* ctx, const vp_factor* F, int nrhs, const double*
     return r;
 }
 
+// the adjoint's transposed solve: M' [xi; eta] = [g; 0]
+extern "C" int vp_solve_transposed(vp_ctx* ctx, const vp_factor* F, int nrhs, const double* g, double* xi) {
+    if (!ctx || !F || !g || !xi || nrhs <= 0) return vp_fail(ctx, VP_ERR_ARG, "null argument");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    const int n = F->n, nq = F->nq;
+    const size_t tot = size_t(n) * nrhs;
+    std::vector<double> hx(tot, 0.0);
+    for (int k = 0; k < nrhs; ++k)
+        for (int i = 0; i < nq; ++i) hx[size_t(k) * n + i] = g[size_t(k) * nq + i];
+    double* x;
+    int r;
+    if ((r = vp_upload(ctx, &x, hx.data(), tot))) return r;
+    vp_phase_begin(ctx, PH_ADJOINT);
+    r = solve_core(ctx, F, nrhs, x, true, nullptr);
+    vp_phase_end(ctx);
+    if (!r) {
+        cudaError_t e = vp_d2h(ctx, hx.data(), x, sizeof(double) * tot);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) r = vp_fail(ctx, VP_ERR_CUDA, cudaGetErrorString(e));
+        for (int k = 0; k < nrhs && !r; ++k)
+            for (int i = 0; i < nq; ++i) xi[size_t(k) * nq + i] = hx[size_t(k) * n + i];
+    }
+    cudaFree(x);
+    return r;
+}
+
 extern "C" int vp_solve_system(vp_ctx* ctx, const vp_factor* F, const vp_system* sys, double* q, double* lambda,
                                double* residual) {
     if (!ctx || !F || !sys) return vp_fail(ctx, VP_ERR_ARG, "null argument");

@@ -54,6 +54,11 @@ SIGNATURES = [
                                       ctypes.c_double, D]),
     ("vp_eval_points_static", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, D, D, D,
                                              ctypes.c_int, ctypes.c_double, D]),
+    ("vp_solve_transposed", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, D, D]),
+    ("vp_adjoint", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
+      ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I, D, D, D, D, D, D,
+      ctypes.POINTER(vp_assembly_stats)]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]
