@@ -28,6 +28,10 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "vortexpanel.jl_gb300"))
 
 METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|<1e-6"
+# algorithmic flops per quadrature point: forward (kernel evaluation ~230 + contraction into the hat block 18) and
+# adjoint (value and reverse-mode derivatives of the kernel ~620 + the sums of the test and source sides ~110)
+FLOP_FWD_POINT = 248
+FLOP_ADJ_POINT = 730
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
 SIZES = {"wing25k": (112, 56), "medium": (56, 28), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
@@ -42,23 +46,15 @@ def workload(name="wing25k"):
     W = meshes.wake_rows(w.dm, wake.te)
     a = math.radians(ALPHA)
     V = np.array([math.cos(a), 0.0, math.sin(a)])
-    eL = np.array([-math.sin(a), 0.0, math.cos(a)])
-    return w, wake, W, V, eL
+    return w, wake, W, V
 
 
-def step(vp, w, wake, W, V, eL, precision, ctx):
-    """one pass of the hot path; returns CL, CDi and the assembly stats"""
-    els = vp.build_elements(w.g)
-    sig = vp.source_strengths(els, V)
-    A, b, stats = vp.assemble(w.g, w.dm, els, sig, V, wake=wake, opts=vp.AssemblyOptions(precision=precision), ctx=ctx)
-    F = vp.factorize_galerkin(w.dm, A, W=W, precision=precision, ctx=ctx)
-    s = vp.solve_galerkin(F, b)
-    S = w.span * w.chord
-    cp = vp.pressure_coefficient(vp.gradient_velocity(els, w.dm, s["mu"], V), V)
-    CL = float(vp.pressure_force(els, cp)[0] @ eL / S)
-    CDi = float(vp.trefftz_drag(w.dm.wake_te, w.dm.K @ s["q"], V) / S)
-    del A, F
-    return CL, CDi, stats, s["cond"]
+def step(vp, w, wake, W, precision, ctx):
+    """one pass of the hot path: assemble + factorize + solve + loads (CL by pressure, CDi by Trefftz) + the adjoint
+    gradients of both with respect to every node and alpha; returns the result dict of wing_gradients"""
+    from vortexpanel_gpu.adjoint import wing_gradients
+
+    return wing_gradients(w, wake, W, math.radians(ALPHA), precision=precision, ctx=ctx)
 
 
 class Clocks:
@@ -124,7 +120,7 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-def cpu_baseline(w, wake, W, V, eL, budget_s=20.0):
+def cpu_baseline(w, wake, W, V, budget_s=20.0):
     """The oracle (C++ restatement of the reference's assembly, OpenMP over test triangles as assemble.jl:395, and the
     reference's LAPACK dgetrf/dgetrs through scipy) on a bounded sample: the rows of a slice of test triangles, and
     the LU of a leading principal block; scaled to the full step (rows linearly, the LU by n^3)."""
@@ -187,7 +183,7 @@ def main():
                     help="wing25k (the measured configuration); medium (56x28 per side) and small (28x14) for profiler captures")
     args = ap.parse_args()
     rank, world, local, dist = dist_setup(args.gpus)
-    w, wake, W, V, eL = workload(args.workload)
+    w, wake, W, V = workload(args.workload)
     config = {"workload": f"wing AR{ASPECT:g} NACA0012 {NCHORD}x{NSPAN}/side ({w.g.ntri} tris, {w.dm.nq} unknowns), "
                           f"rigid wake {len(wake.tris)} tris + {len(wake.filaments)} filaments, alpha {ALPHA:g} deg",
               "ntri": w.g.ntri, "nq": w.dm.nq, "nwake_nodes": wake.nwake, "precision": "mixed",
@@ -196,7 +192,7 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        cb = cpu_baseline(w, wake, W, V, eL)
+        cb = cpu_baseline(w, wake, W, V)
         line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": world, "steps": 1, "warmup": 0,
                 "ms_per_step": cb["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
@@ -209,7 +205,7 @@ def main():
 
     ctx = vp.Context(local)
     for _ in range(args.warmup):
-        step(vp, w, wake, W, V, eL, "mixed", ctx)
+        step(vp, w, wake, W, "mixed", ctx)
     ctx.phase_times(reset=True)
     ctx.transfer_bytes(reset=True)
     if dist:
@@ -218,7 +214,7 @@ def main():
     with Clocks(local) as clk:
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            CL, CDi, stats, cond = step(vp, w, wake, W, V, eL, "mixed", ctx)
+            out = step(vp, w, wake, W, "mixed", ctx)
             walls.append(time.perf_counter() - t0)
     phases, launches = ctx.phase_times(reset=True)
     h2d, d2h = ctx.transfer_bytes(reset=True)
@@ -230,45 +226,53 @@ def main():
         t = torch.tensor([dev_s, e2e_s], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         dev_s, e2e_s = float(t[0]), float(t[1])
+    CL, CDi, stats, cond = out["CL"], out["CDi"], out["stats"], out["cond"]
     # the plain FP64 GPU path on the same workload
     fp = {}
     if args.fp64_steps > 0:
-        step(vp, w, wake, W, V, eL, "fp64", ctx)
+        step(vp, w, wake, W, "fp64", ctx)
         ctx.phase_times(reset=True)
         fw = []
         for _ in range(args.fp64_steps):
             t0 = time.perf_counter()
-            CL64, CDi64, stats64, cond64 = step(vp, w, wake, W, V, eL, "fp64", ctx)
+            o64 = step(vp, w, wake, W, "fp64", ctx)
             fw.append(time.perf_counter() - t0)
         ph64, _ = ctx.phase_times(reset=True)
+        grel = {n: float(np.abs(out[f"d{n}_dx"] - o64[f"d{n}_dx"]).max() / np.abs(o64[f"d{n}_dx"]).max())
+                for n in ("CL", "CDi")}
         fp = {"fp64_s": sum(ph64.values()) / 1e3 / args.fp64_steps, "fp64_e2e_s": sum(fw) / len(fw),
               "fp64_phases_ms": {k: v / args.fp64_steps for k, v in ph64.items()},
-              "CL_fp64": CL64, "CDi_fp64": CDi64, "dCL": abs(CL - CL64), "dCDi": abs(CDi - CDi64)}
+              "CL_fp64": o64["CL"], "CDi_fp64": o64["CDi"], "dCL": abs(CL - o64["CL"]), "dCDi": abs(CDi - o64["CDi"]),
+              "grad_rel_diff_vs_fp64": grel,
+              "dalpha_rel_diff_vs_fp64": {n: abs(out[f"d{n}_dalpha"] - o64[f"d{n}_dalpha"]) / abs(o64[f"d{n}_dalpha"])
+                                          for n in ("CL", "CDi")}}
         fp["speedup_vs_fp64"] = fp["fp64_s"] / dev_s
+        fp["e2e_speedup_vs_fp64"] = fp["fp64_e2e_s"] / e2e_s
     if rank != 0:
         return
     per = {k: v / args.steps for k, v in phases.items()}
-    # roofline of the dominant kernel: FP32 CUDA-core bound (the pair integrals); algorithmic flops per evaluated
-    # point (kernel evaluation + contraction into the hat block) from the device's per-tier point counts
+    # roofline of the dominant kernel: the pair integrals are FP32 CUDA-core bound; algorithmic flops per evaluated
+    # point (kernel evaluation + contraction) from the device's per-tier point counts
     pk, src = peaks()
-    dom = max(("far", "near", "lu"), key=lambda k: per[k])
+    dom = max(("far", "near", "lu", "adj_far", "adj_near"), key=lambda k: per[k])
     sm_max = pk.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal FP32 FMA rate at the max SM clock
-    FLOP_FAR_POINT = 230 + 18
+    pts, apts = stats["points"], out["adjoint_points"]
+    nonfar = lambda p: sum(v for k, v in p.items() if k != "far")  # noqa: E731
     if dom == "far":
-        flops = stats["points"]["far"] * FLOP_FAR_POINT
-        roof = {"kernel": "far_kernel<float,8>", "bound": "fp32", "achieved": flops / (per["far"] / 1e3) / 1e12,
-                "peak": fp32_peak, "unit": "TFLOP/s"}
+        roof = {"kernel": "far_kernel<float,8>", "bound": "fp32", "flops": pts["far"] * FLOP_FWD_POINT}
     elif dom == "near":
-        pts = stats["points"]
-        flops = pts["near"] * FLOP_FAR_POINT
-        roof = {"kernel": "near_kernel", "bound": "fp32", "achieved": flops / (per["near"] / 1e3) / 1e12,
-                "peak": fp32_peak, "unit": "TFLOP/s"}
+        roof = {"kernel": "near_kernel_lanes + near_kernel_rest", "bound": "fp32", "flops": nonfar(pts) * FLOP_FWD_POINT}
+    elif dom == "adj_far":
+        roof = {"kernel": "adj_far_kernel<float,8>", "bound": "fp32", "flops": 2 * apts["far"] * FLOP_ADJ_POINT}
+    elif dom == "adj_near":
+        roof = {"kernel": "adj_near_kernel", "bound": "fp32", "flops": 2 * nonfar(apts) * FLOP_ADJ_POINT}
     else:
         n = w.dm.nq + 1
-        roof = {"kernel": "lu (cluster panels + sgemm)", "bound": "tensor",
-                "achieved": 2 / 3 * n ** 3 / (per["lu"] / 1e3) / 1e12, "peak": pk.get("bf16_tflops", 1900.0),
-                "unit": "TFLOP/s"}
+        roof = {"kernel": "lu (cluster panels + sgemm)", "bound": "tensor", "flops": 2 / 3 * n ** 3}
+    roof["achieved"] = roof.pop("flops") / (per[dom] / 1e3) / 1e12
+    roof["peak"] = fp32_peak if roof["bound"] == "fp32" else pk.get("bf16_tflops", 1900.0)
+    roof["unit"] = "TFLOP/s"
     roof["frac"] = roof["achieved"] / roof["peak"]
     roof["peak_source"] = "nominal (152 SMs x 128 FP32 lanes x 2 x max SM clock)" if roof["bound"] == "fp32" else src
     roof["traffic"] = None
@@ -280,10 +284,10 @@ def main():
             "gpu_launches": launches // args.steps * args.steps, "phases_ms": per,
             "CL": CL, "CDi": CDi, "cond": cond, "tiers": stats, "roofline": roof, "clocks": clk.summary(),
             "fp64_point_share": stats["points_fp64"] / max(1, sum(stats["points"].values())),
-            "adjoint": "not included yet"}
+            "adjoint_points": out["adjoint_points"]}
     line.update(fp)
     if not args.no_cpu_baseline:
-        cb = cpu_baseline(w, wake, W, V, eL)
+        cb = cpu_baseline(w, wake, W, V)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     print(json.dumps(line))
 

@@ -808,6 +808,7 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
     }
     int* d_tiles;
     if ((r = dl.up(ctx, &d_tiles, all))) return r;
+    vp_phase_begin(ctx, PH_FAR);
     for (size_t c = 0; c < colours.size(); ++c) {
         fa.tiles = d_tiles + off[c];
         int nb = off[c + 1] - off[c];
@@ -816,6 +817,7 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
             ctx->launches++;
         }
     }
+    vp_phase_end(ctx);
     VP_CUDA(ctx, cudaGetLastError());
     return VP_OK;
 }
@@ -910,9 +912,7 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
             }
         }
         std::vector<int> cs(corner_slot, corner_slot + 3 * ntri);
-        vp_phase_begin(ctx, PH_FAR);
         r = mixed ? run_far<float, 8>(ctx, fa, tg, cs, nslot, dl) : run_far<double, 4>(ctx, fa, tg, cs, nslot, dl);
-        vp_phase_end(ctx);
         if (r) { vp_system_free(sys); return r; }
     }
 

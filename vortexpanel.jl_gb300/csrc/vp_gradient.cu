@@ -549,7 +549,9 @@ int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const dou
     int chunks = std::max(1, std::min(fa.ntiles_test, (6 * ctx->nsm + tiles - 1) / std::max(tiles, 1)));
     fa.tiles_per_chunk = (fa.ntiles_test + chunks - 1) / chunks;
     chunks = (fa.ntiles_test + fa.tiles_per_chunk - 1) / fa.tiles_per_chunk;
+    vp_phase_begin(ctx, PH_ADJ_FAR);
     adj_far_kernel<T, TT><<<dim3(tiles, chunks), FAR_NT, 0, ctx->stream>>>(fa);
+    vp_phase_end(ctx);
     ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
     return VP_OK;
@@ -602,6 +604,7 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     VP_CUDA(ctx, cudaMemsetAsync(d_gwx, 0, sizeof(double) * 3 * std::max(nwnode, 1), ctx->stream));
     VP_CUDA(ctx, cudaMemsetAsync(d_dal, 0, sizeof(double), ctx->stream));
     VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
+    vp_phase_end(ctx);
     // far tier
     r = ps.mixed ? run_adj_far<float, 8>(ctx, ps, in, d_nu, mu, d_SA0, d_SA1, d_TA, dl)
                  : run_adj_far<double, 4>(ctx, ps, in, d_nu, mu, d_SA0, d_SA1, d_TA, dl);
@@ -631,10 +634,13 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         ex.gx = d_gx;
         ex.gwx = d_gwx;
         ex.dal = d_dal;
+        vp_phase_begin(ctx, PH_ADJ_NEAR);
         adj_near_kernel<<<(ntri + NEAR_WARPS - 1) / NEAR_WARPS, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, ex);
+        vp_phase_end(ctx);
         ctx->launches++;
         VP_CUDA(ctx, cudaGetLastError());
     }
+    vp_phase_begin(ctx, PH_ADJOINT);
     // node derivatives
     {
         AdjFinish f{};

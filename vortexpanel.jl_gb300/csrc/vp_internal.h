@@ -18,7 +18,10 @@ enum {
     PH_LU,          // LU factorization
     PH_COND,        // condition estimate
     PH_SOLVE,       // triangular solves and refinement
-    PH_ADJOINT,     // adjoint pair derivatives
+    PH_ADJOINT,     // adjoint: element data, classification and the node derivatives (finish)
+    PH_ADJ_FAR,     // adjoint far tier
+    PH_ADJ_NEAR,    // adjoint non-far pairs, filaments, freestream
+    PH_ADJ_SOLVE,   // transposed solve
     PH_COUNT
 };
 

@@ -758,7 +758,7 @@ extern "C" int vp_solve_transposed(vp_ctx* ctx, const vp_factor* F, int nrhs, co
     double* x;
     int r;
     if ((r = vp_upload(ctx, &x, hx.data(), tot))) return r;
-    vp_phase_begin(ctx, PH_ADJOINT);
+    vp_phase_begin(ctx, PH_ADJ_SOLVE);
     r = solve_core(ctx, F, nrhs, x, true, nullptr);
     vp_phase_end(ctx);
     if (!r) {

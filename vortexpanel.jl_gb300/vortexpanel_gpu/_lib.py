@@ -118,7 +118,8 @@ class Context:
         self.h = h
         self.device = device
 
-    PHASES = ("setup", "classify", "far", "near", "reduce", "lu", "cond", "solve", "adjoint")
+    PHASES = ("setup", "classify", "far", "near", "reduce", "lu", "cond", "solve", "adj_setup", "adj_far", "adj_near",
+              "adj_solve")
 
     def phase_times(self, reset=False):
         """Device milliseconds per phase since the last reset, and the number of the library's kernel launches"""

@@ -235,7 +235,8 @@ def wing_gradients(w, wake, W, alpha, precision="mixed", opts=None, ctx=None, ti
     out = dict(CL=CL, CDi=CDi, q=q, stats=stats, cond=s["cond"])
     for name, gx, al, k in (("CL", gCL, aCL, 0), ("CDi", gCDi, aCDi, 1)):
         nu = dm.C @ xi[:, k]
-        fx, fw, fa, _ = pair_derivatives(g, dm, sig, V, dV, nu, mu_cols, opts=opts, wake=wake, ctx=ctx)
+        fx, fw, fa, st = pair_derivatives(g, dm, sig, V, dV, nu, mu_cols, opts=opts, wake=wake, ctx=ctx)
+        out["adjoint_points"] = dict(zip(("self", "edge", "vertex", "contact", "near", "far"), list(st.points)))
         grad = gx - fx
         if wake is not None and len(fw):
             np.add.at(grad, dm.wake_te.node[wake.te], -fw)
