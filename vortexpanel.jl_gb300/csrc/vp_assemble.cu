@@ -207,64 +207,12 @@ __global__ void __launch_bounds__(FAR_NT) far_kernel(FarArgs a) {
 // are queued and evaluated 32 at a time in FP64), reduces them per pair in a fixed order and adds the blocks to A
 // pair by pair. Pairs of the other tiers are returned (a lane mask) for the warp-cooperative path.
 struct NearChunkSh {
-    uint8_t leaf[32][64];  // leaf codes: level << 6 | path (level base-4 digits, most significant first)
-    float E32[32][27];     // x_T,k - v_S,a
-    float D32[32][9];      // x_T,k - c_S
-    float S32[32][26];     // d (9), nu (9), len (3), n (3), area, diam
+    NearPlanSh pl;         // the pairs' leaves and FP32 frames
     double acc[32][9];     // per pair: sum of W psi_a w (FP64 evaluations)
     float accf[32][9];     // per pair: the same sums of the FP32 evaluations
     int off[33];           // points before each pair
     int qp[64], qk[64];    // queued FP64 points: pair, point within the pair
 };
-
-__device__ __forceinline__ void leaf_corners32(int code, float* b) {
-    // the corners of a quadtree node in the test triangle's barycentrics (dyadic, exact in FP32)
-    int level = code >> 6, path = code & 63;
-    float c[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    for (int l = 0; l < level; ++l) {
-        int digit = (path >> (2 * (level - 1 - l))) & 3;
-        float m12[3], m23[3], m31[3];
-        for (int z = 0; z < 3; ++z) {
-            m12[z] = 0.5f * (c[z] + c[3 + z]);
-            m23[z] = 0.5f * (c[3 + z] + c[6 + z]);
-            m31[z] = 0.5f * (c[6 + z] + c[z]);
-        }
-        float n[9];
-        for (int z = 0; z < 3; ++z) {
-            if (digit == 0) { n[z] = c[z]; n[3 + z] = m12[z]; n[6 + z] = m31[z]; }
-            else if (digit == 1) { n[z] = m12[z]; n[3 + z] = c[3 + z]; n[6 + z] = m23[z]; }
-            else if (digit == 2) { n[z] = m31[z]; n[3 + z] = m23[z]; n[6 + z] = c[6 + z]; }
-            else { n[z] = m12[z]; n[3 + z] = m23[z]; n[6 + z] = m31[z]; }
-        }
-        for (int z = 0; z < 9; ++z) c[z] = n[z];
-    }
-    for (int z = 0; z < 9; ++z) b[z] = c[z];
-}
-
-// per-lane contributions W psi_a w_c (9 values), keyed by pair (non-decreasing over the lanes, 32+ for none):
-// segmented sums in a fixed order, added to the pairs' FP64 accumulators
-template <class V>
-__device__ __forceinline__ void seg_accumulate(NearChunkSh& ns, int lane, int key, V* v) {
-    const unsigned FULL = 0xffffffffu;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        int ky = __shfl_up_sync(FULL, key, o);
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-            V y = __shfl_up_sync(FULL, v[k], o);
-            if (lane >= o && ky == key) v[k] += y;
-        }
-    }
-    int kn = __shfl_down_sync(FULL, key, 1);
-    bool last = lane == 31 || kn != key;
-    if (last && key < 32) {
-        if (sizeof(V) == 4)
-            for (int k = 0; k < 9; ++k) ns.accf[key][k] += float(v[k]);
-        else
-            for (int k = 0; k < 9; ++k) ns.acc[key][k] += double(v[k]);
-    }
-    __syncwarp();
-}
 
 // the FP64 evaluation of point k of pair p (queued by the FP32 guard): contributions in v
 __device__ void near_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S, const NearChunkSh& ns, int p, int k,
@@ -272,14 +220,14 @@ __device__ void near_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S
     const int nr = a.nrule[R_NEAR];
     int leaf = k / nr, q = k - leaf * nr;
     float bf[9];
-    leaf_corners32(ns.leaf[p][leaf], bf);
+    leaf_corners32(ns.pl.leaf[p][leaf], bf);
     double b[9];
     for (int z = 0; z < 9; ++z) b[z] = double(bf[z]);
     RulePt m = a.rule[R_NEAR][q];
     double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
     double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
     double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
-    int level = ns.leaf[p][leaf] >> 6;
+    int level = ns.pl.leaf[p][leaf] >> 6;
     double W = (m.w * ldexp(1.0, -2 * level)) * T.area;
     v3<double> x = mk3(l0 * T.x[0] + l1 * T.x[3] + l2 * T.x[6], l0 * T.x[1] + l1 * T.x[4] + l2 * T.x[7],
                        l0 * T.x[2] + l1 * T.x[5] + l2 * T.x[8]);
@@ -322,137 +270,8 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
     const bool valid = lane < cnt;
     const int s = valid ? list[lane] : 0;
     const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
-    // 1. the tier of this lane's pair
-    bool near = valid && a.test_mode != 2 && a.near_depth <= 3 && !(!wake && s == t);
-    if (near && !wake) {
-        for (int k = 0; k < 3; ++k)
-            if (T.node[k] == S.node[0] || T.node[k] == S.node[1] || T.node[k] == S.node[2]) near = false;
-        if (near && a.ntouch > 0) {
-            long long key = (long long)t * a.ntri + s;
-            int lo = 0, hi = a.ntouch;
-            while (lo < hi) {
-                int mid = (lo + hi) >> 1;
-                if (a.touch[mid] < key) lo = mid + 1;
-                else hi = mid;
-            }
-            if (lo < a.ntouch && a.touch[lo] == key) near = false;
-        }
-    }
-    // FP32 frame of this pair: S's corner 0 at the origin (differences taken in FP64); e32 bounds the FP32 rounding
-    v3<float> sv[3], tv[3];
-    float e32 = 0.f;
-    if (near) {
-        for (int q = 0; q < 3; ++q) {
-            sv[q] = mk3(float(S.x[3 * q] - S.x[0]), float(S.x[3 * q + 1] - S.x[1]), float(S.x[3 * q + 2] - S.x[2]));
-            tv[q] = mk3(float(T.x[3 * q] - S.x[0]), float(T.x[3 * q + 1] - S.x[1]), float(T.x[3 * q + 2] - S.x[2]));
-            e32 = fmaxf(e32, fmaxf(vnorm(sv[q]), vnorm(tv[q])));
-        }
-        e32 *= 1e-4f;
-    }
-    if (near) {  // contact_rule (assemble.jl:199-207) finds no contact beyond shared corners
-        const double tol = a.contact_rel * fmin(T.diam, S.diam);
-        const float tolf = float(tol);
-        // FP32 pass: 1 contact, 0 none, -1 undecided (then the FP64 test decides)
-        int res;
-        {
-            v3<float> dc = (sv[1] + sv[2]) * (1.f / 3.f) - (tv[0] + tv[1] + tv[2]) * (1.f / 3.f);
-            int far_reach = lt32(float(T.reach + S.reach + tol), vnorm(dc), e32);
-            if (far_reach == 1) {
-                res = 0;
-            } else {
-                bool any_true = false, any_undec = far_reach < 0;
-                for (int k = 0; k < 3; ++k) {
-                    int c = lt32(dist_tri_v(sv[0], sv[1], sv[2], tv[k]), tolf, e32);
-                    if (c == 1) any_true = true;
-                    else if (c < 0) any_undec = true;
-                }
-                for (int k = 0; k < 3 && !any_true; ++k) {
-                    v3<float> ta = tv[k], tc = tv[(k + 1) % 3];
-                    v3<float> ev = tc - ta;
-                    float L = vnorm(ev);
-                    for (int q = 0; q < 3; ++q) {
-                        float t = dot(sv[q] - ta, ev) / dot(ev, ev);
-                        t = fminf(fmaxf(t, 0.f), 1.f);
-                        float d = vnorm(sv[q] - (ta + t * ev));
-                        int c1 = lt32(d, tolf, e32) , c2 = lt32(tolf, t * L, 2.f * e32), c3 = lt32(tolf, (1.f - t) * L, 2.f * e32);
-                        if (d == tolf) c1 = -1;
-                        if (c1 == 1 && c2 == 1 && c3 == 1) any_true = true;
-                        else if (c1 != 0 && c2 != 0 && c3 != 0) any_undec = true;
-                    }
-                }
-                res = any_true ? 1 : (any_undec ? -1 : 0);
-                if (far_reach < 0 && res == 1) res = -1;  // contact needs the reach test passed
-            }
-        }
-        if (res < 0) {  // the reference's FP64 test
-            res = 0;
-            if (!(vnorm(ld3(S.c) - ld3(T.c)) > T.reach + S.reach + tol)) {
-                bool extra = false;
-                for (int k = 0; k < 3 && !extra; ++k)
-                    if (dist_tri(S.x, ld3(T.x + 3 * k)) <= tol) extra = true;
-                for (int k = 0; k < 3 && !extra; ++k)
-                    for (int q = 0; q < 3 && !extra; ++q) {
-                        double tt;
-                        if (on_edge_split(ld3(S.x + 3 * q), ld3(T.x + 3 * k), ld3(T.x + 3 * ((k + 1) % 3)), tol, tt))
-                            extra = true;
-                    }
-                res = extra ? 1 : 0;
-            }
-        }
-        if (res == 1) near = false;
-    }
-    // 2. near_pieces' leaves (assemble.jl:131-142), decided in FP32 unless a node is too close to the threshold
     int nleaf = 0;
-    if (near) {
-        const int depth = a.near_depth;
-        const float ratiof = float(a.near_ratio);
-        int level = 0;
-        unsigned path = 0;
-        for (int guard = 0; guard < 1024; ++guard) {
-            float bf[9];
-            leaf_corners32((level << 6) | int(path), bf);
-            v3<float> p1 = bf[0] * tv[0] + bf[1] * tv[1] + bf[2] * tv[2];
-            v3<float> p2 = bf[3] * tv[0] + bf[4] * tv[1] + bf[5] * tv[2];
-            v3<float> p3 = bf[6] * tv[0] + bf[7] * tv[1] + bf[8] * tv[2];
-            float size = fmaxf(vnorm(p2 - p1), fmaxf(vnorm(p3 - p2), vnorm(p1 - p3)));
-            float d = dist_tri_v(sv[0], sv[1], sv[2], (p1 + p2 + p3) * (1.f / 3.f));
-            int split = level < depth ? lt32(d, ratiof * size, 2.f * e32) : 0;
-            if (split < 0) {  // the reference's FP64 test at this node
-                double b[9];
-                for (int z = 0; z < 9; ++z) b[z] = double(bf[z]);
-                v3<double> q1 = tpoint(T, b), q2 = tpoint(T, b + 3), q3 = tpoint(T, b + 6);
-                double sz = fmax(vnorm(q2 - q1), fmax(vnorm(q3 - q2), vnorm(q1 - q3)));
-                split = dist_tri(S.x, (q1 + q2 + q3) / 3.0) < a.near_ratio * sz ? 1 : 0;
-            }
-            if (split) {
-                level++;
-                path *= 4;
-                continue;
-            }
-            ns.leaf[lane][nleaf++] = uint8_t((level << 6) | path);
-            while (level > 0 && (path & 3) == 3) {
-                path >>= 2;
-                level--;
-            }
-            if (level == 0) break;
-            path++;
-        }
-        for (int k = 0; k < 3; ++k)
-            for (int q = 0; q < 3; ++q)
-                for (int z = 0; z < 3; ++z) ns.E32[lane][9 * k + 3 * q + z] = float(T.x[3 * k + z] - S.x[3 * q + z]);
-        for (int k = 0; k < 3; ++k)
-            for (int z = 0; z < 3; ++z) ns.D32[lane][3 * k + z] = float(T.x[3 * k + z] - S.c[z]);
-        for (int k = 0; k < 9; ++k) {
-            ns.S32[lane][k] = float(S.x[k] - S.c[k % 3]);
-            ns.S32[lane][9 + k] = float(S.nu[k]);
-        }
-        for (int k = 0; k < 3; ++k) {
-            ns.S32[lane][18 + k] = float(S.len[k]);
-            ns.S32[lane][21 + k] = float(S.n[k]);
-        }
-        ns.S32[lane][24] = float(S.area);
-        ns.S32[lane][25] = float(S.diam);
-    }
+    bool near = near_plan(pc, ns.pl, t, S, s, valid, wake, nleaf);
     for (int k = 0; k < 9; ++k) {
         ns.acc[lane][k] = 0.0;
         ns.accf[lane][k] = 0.f;
@@ -500,7 +319,7 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
             p = lo;
             k = i - ns.off[p];
             int leaf = k / nr, q = k - leaf * nr;
-            int code = ns.leaf[p][leaf];
+            int code = ns.pl.leaf[p][leaf];
             float b[9];
             leaf_corners32(code, b);
             float4 m = a.rulef[R_NEAR][q];
@@ -508,9 +327,9 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
             float l1 = m.x * b[1] + m.y * b[4] + m.z * b[7];
             float l2 = m.x * b[2] + m.y * b[5] + m.z * b[8];
             float W = m.w * ldexpf(1.f, -2 * (code >> 6)) * areaT;
-            const float* E = ns.E32[p];
-            const float* Dp = ns.D32[p];
-            const float* Sf = ns.S32[p];
+            const float* E = ns.pl.E32[p];
+            const float* Dp = ns.pl.D32[p];
+            const float* Sf = ns.pl.S32[p];
             SrcKern<float> K;
             for (int z = 0; z < 3; ++z) {
                 K.d[z] = mk3(Sf[3 * z], Sf[3 * z + 1], Sf[3 * z + 2]);
@@ -544,7 +363,7 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
                 need = true;
             }
         }
-        if (a.mixed) seg_accumulate(ns, lane, p, vals);  // flagged points add zero here, their FP64 value when drained
+        if (a.mixed) seg_accumulate<9>(ns.accf, ns.acc, lane, p, vals);  // flagged points add zero here, their FP64 value when drained
         unsigned m = __ballot_sync(FULL, need);
         if (m) {
             int pos = nq + __popc(m & ((1u << lane) - 1u));
@@ -564,7 +383,7 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
                 const TriGeo& Sq = wake ? a.wtri[list[qpair]] : a.tri[list[qpair]];
                 near_point64(a, T, Sq, ns, qpair, ns.qk[lane], qv);
             }
-            seg_accumulate(ns, lane, qpair, qv);
+            seg_accumulate<9>(ns.accf, ns.acc, lane, qpair, qv);
             const int rest = nq - take;
             int mp = 0, mk = 0;
             if (lane < rest) {

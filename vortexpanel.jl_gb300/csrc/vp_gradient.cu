@@ -251,9 +251,6 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
     }
 }
 
-// ------------------------------------------------------------------------------------------------------------------
-// non-far pairs, tip filaments and freestream: one warp per test triangle
-
 struct AdjExtra {
     const double* nu;     // row slot values
     const double* mu;     // column values (body slots, then wake nodes)
@@ -267,6 +264,323 @@ struct AdjExtra {
     double* dal;
 };
 
+// ------------------------------------------------------------------------------------------------------------------
+// near-tier pairs, one per lane: the plan of the assembly's lanes kernel (tiers and quadtree leaves), every leaf point
+// of a chunk of 32 pairs evaluated across the lanes (FP32 under the adjoint's guard, or queued for FP64), per-pair
+// segmented sums, and each lane finishing its own pair: the source side added to SA, the test side summed over the
+// warp once per test triangle. The pairs of the other tiers are listed for the warp-cooperative kernel.
+
+constexpr int NSUM = 41;  // AdjSums: Q (3), Xg (9), Gr (9), Grf (3), Gd (9), L (3), N (3), O, A
+
+template <class T>
+__device__ __forceinline__ void sums_flat(const AdjSums<T>& a, T* f) {
+    f[0] = a.Q.x; f[1] = a.Q.y; f[2] = a.Q.z;
+    for (int k = 0; k < 3; ++k) {
+        f[3 + 3 * k] = a.Xg[k].x; f[4 + 3 * k] = a.Xg[k].y; f[5 + 3 * k] = a.Xg[k].z;
+        f[12 + 3 * k] = a.Gr[k].x; f[13 + 3 * k] = a.Gr[k].y; f[14 + 3 * k] = a.Gr[k].z;
+        f[24 + 3 * k] = a.Gd[k].x; f[25 + 3 * k] = a.Gd[k].y; f[26 + 3 * k] = a.Gd[k].z;
+        f[33 + k] = a.L[k];
+        f[36 + k] = a.N[k];
+    }
+    f[21] = a.Grf.x; f[22] = a.Grf.y; f[23] = a.Grf.z;
+    f[39] = a.O;
+    f[40] = a.A;
+}
+
+__device__ __forceinline__ AdjSums<double> sums_unflat(const double* f) {
+    AdjSums<double> a;
+    a.Q = mk3(f[0], f[1], f[2]);
+    for (int k = 0; k < 3; ++k) {
+        a.Xg[k] = mk3(f[3 + 3 * k], f[4 + 3 * k], f[5 + 3 * k]);
+        a.Gr[k] = mk3(f[12 + 3 * k], f[13 + 3 * k], f[14 + 3 * k]);
+        a.Gd[k] = mk3(f[24 + 3 * k], f[25 + 3 * k], f[26 + 3 * k]);
+        a.L[k] = f[33 + k];
+        a.N[k] = f[36 + k];
+    }
+    a.Grf = mk3(f[21], f[22], f[23]);
+    a.O = f[39];
+    a.A = f[40];
+    return a;
+}
+
+struct AdjChunkSh {
+    NearPlanSh pl;
+    double acc[32][NSUM];  // per pair: the sums of its FP64 points
+    float accf[32][NSUM];  // and of its FP32 points
+    double m64[32][3];     // the pair's direction m
+    int off[33];           // points before each pair
+    int qp[64], qk[64];    // queued FP64 points: pair, point within the pair
+};
+
+// the FP64 adjoint evaluation of point k of pair p (queued by the FP32 guard)
+__device__ void adj_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S, const AdjChunkSh& ns, const double* nu,
+                            int p, int k, double* v) {
+    const int nr = a.nrule[R_NEAR];
+    int leaf = k / nr, q = k - leaf * nr;
+    float bf[9];
+    leaf_corners32(ns.pl.leaf[p][leaf], bf);
+    double b[9];
+    for (int z = 0; z < 9; ++z) b[z] = double(bf[z]);
+    RulePt m = a.rule[R_NEAR][q];
+    double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
+    double l1 = m.l0 * b[1] + m.l1 * b[4] + m.l2 * b[7];
+    double l2 = m.l0 * b[2] + m.l1 * b[5] + m.l2 * b[8];
+    int level = ns.pl.leaf[p][leaf] >> 6;
+    double W = (m.w * ldexp(1.0, -2 * level)) * T.area;
+    v3<double> psi = test_weights(a.test_mode, l0, l1, l2);
+    double Wn = W * (nu[0] * psi.x + nu[1] * psi.y + nu[2] * psi.z);
+    v3<double> R[3];
+    for (int c = 0; c < 3; ++c)
+        R[c] = mk3(l0 * (T.x[0] - S.x[3 * c]) + l1 * (T.x[3] - S.x[3 * c]) + l2 * (T.x[6] - S.x[3 * c]),
+                   l0 * (T.x[1] - S.x[3 * c + 1]) + l1 * (T.x[4] - S.x[3 * c + 1]) + l2 * (T.x[7] - S.x[3 * c + 1]),
+                   l0 * (T.x[2] - S.x[3 * c + 2]) + l1 * (T.x[5] - S.x[3 * c + 2]) + l2 * (T.x[8] - S.x[3 * c + 2]));
+    v3<double> x = mk3(l0 * T.x[0] + l1 * T.x[3] + l2 * T.x[6], l0 * T.x[1] + l1 * T.x[4] + l2 * T.x[7],
+                       l0 * T.x[2] + l1 * T.x[5] + l2 * T.x[8]);
+    v3<double> r = x - ld3(S.c);
+    SrcKern<double> K;
+    for (int z = 0; z < 3; ++z) {
+        K.d[z] = mk3(S.x[3 * z] - S.c[0], S.x[3 * z + 1] - S.c[1], S.x[3 * z + 2] - S.c[2]);
+        K.nu[z] = ld3(S.nu + 3 * z);
+        K.len[z] = S.len[z];
+    }
+    K.n = ld3(S.n);
+    K.area = S.area;
+    K.diam = S.diam;
+    const v3<double> mm = mk3(ns.m64[p][0], ns.m64[p][1], ns.m64[p][2]);
+    AdjSums<double> as;
+    adj_zero(as);
+    double fd = a.kernel_far * K.diam;
+    if (dot(r, r) > fd * fd)
+        adj_point_far(as, K, Wn, l0, l1, l2, r, mm);
+    else
+        adj_point_exact(as, K, Wn, l0, l1, l2, R[0], R[1], R[2], r, mm, 0, 1e-12);
+    sums_flat(as, v);
+}
+
+// one chunk of up to 32 sources of test t; returns the lanes whose pairs are not in the near tier
+__device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, int t, const int* list, int cnt,
+                              bool wake, v3<double>* Xg, v3<double>& U, double& fs, unsigned long long* P,
+                              unsigned long long* Q, unsigned long long& Q64) {
+    const NearArgs& a = *pc.a;
+    const TriGeo& T = *pc.T;
+    const int lane = pc.lane;
+    const unsigned FULL = 0xffffffffu;
+    const bool valid = lane < cnt;
+    const int s = valid ? list[lane] : 0;
+    const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
+    int nleaf = 0;
+    bool near = near_plan(pc, ns.pl, t, S, s, valid, wake, nleaf);
+    const v3<double> nT = ld3(T.n);
+    v3<double> G = mk3(0.0, 0.0, 0.0);
+    double sig = 0;
+    if (near) {
+        const double* gp = (wake ? x.gam_w : x.gam_b) + 3 * size_t(s);
+        G = mk3(gp[0], gp[1], gp[2]);
+        sig = wake ? 0.0 : S.sigma;
+        v3<double> m = cross(nT, G) + sig * nT;
+        ns.m64[lane][0] = m.x;
+        ns.m64[lane][1] = m.y;
+        ns.m64[lane][2] = m.z;
+    }
+    for (int k = 0; k < NSUM; ++k) {
+        ns.acc[lane][k] = 0.0;
+        ns.accf[lane][k] = 0.f;
+    }
+    const int nr = a.nrule[R_NEAR];
+    int incl = near ? nleaf * nr : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(FULL, incl, o);
+        if (lane >= o) incl += y;
+    }
+    ns.off[lane + 1] = incl;
+    if (lane == 0) ns.off[0] = 0;
+    const int total = __shfl_sync(FULL, incl, 31);
+    const unsigned nearmask = __ballot_sync(FULL, near);
+    __syncwarp();
+    const float kf = float(a.kernel_far), areaT = float(T.area);
+    const float nu0 = float(pc.nu[0]), nu1 = float(pc.nu[1]), nu2 = float(pc.nu[2]);
+    int nq = 0;
+    unsigned long long n64 = 0;
+    for (int i0 = 0; i0 < total; i0 += 32) {
+        const int i = i0 + lane;
+        const bool v = i < total;
+        int p = 32 + lane, k = 0;
+        float vals[NSUM];
+#pragma unroll
+        for (int z = 0; z < NSUM; ++z) vals[z] = 0.f;
+        bool need = false;
+        if (v) {
+            int lo = 0, hi = 31;
+            while (lo < hi) {
+                int mid = (lo + hi + 1) >> 1;
+                if (ns.off[mid] <= i) lo = mid;
+                else hi = mid - 1;
+            }
+            p = lo;
+            k = i - ns.off[p];
+            need = !a.mixed;
+        }
+        if (v && a.mixed) {
+            int leaf = k / nr, q = k - leaf * nr;
+            int code = ns.pl.leaf[p][leaf];
+            float b[9];
+            leaf_corners32(code, b);
+            float4 m = a.rulef[R_NEAR][q];
+            float l0 = m.x * b[0] + m.y * b[3] + m.z * b[6];
+            float l1 = m.x * b[1] + m.y * b[4] + m.z * b[7];
+            float l2 = m.x * b[2] + m.y * b[5] + m.z * b[8];
+            float W = m.w * ldexpf(1.f, -2 * (code >> 6)) * areaT;
+            float Wn = W * (a.test_mode == 0 ? nu0 * l0 + nu1 * l1 + nu2 * l2 : nu0 + nu1 + nu2);
+            const float* E = ns.pl.E32[p];
+            const float* Dp = ns.pl.D32[p];
+            const float* Sf = ns.pl.S32[p];
+            SrcKern<float> K;
+            for (int z = 0; z < 3; ++z) {
+                K.d[z] = mk3(Sf[3 * z], Sf[3 * z + 1], Sf[3 * z + 2]);
+                K.nu[z] = mk3(Sf[9 + 3 * z], Sf[10 + 3 * z], Sf[11 + 3 * z]);
+                K.len[z] = Sf[18 + z];
+            }
+            K.n = mk3(Sf[21], Sf[22], Sf[23]);
+            K.area = Sf[24];
+            K.diam = Sf[25];
+            const v3<float> mf = mk3(float(ns.m64[p][0]), float(ns.m64[p][1]), float(ns.m64[p][2]));
+            v3<float> r = l0 * mk3(Dp[0], Dp[1], Dp[2]) + l1 * mk3(Dp[3], Dp[4], Dp[5]) + l2 * mk3(Dp[6], Dp[7], Dp[8]);
+            AdjSums<float> as;
+            adj_zero(as);
+            float fd = kf * K.diam;
+            if (dot(r, r) > fd * fd) {
+                adj_point_far(as, K, Wn, l0, l1, l2, r, mf);
+            } else {
+                v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
+                v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
+                v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
+                if (fp32_guard_ok(K, ra, rb, rc, 0, Fp32Guard{ADJ_GUARD}))
+                    adj_point_exact(as, K, Wn, l0, l1, l2, ra, rb, rc, r, mf, 0, 1e-12f);
+                else
+                    need = true;
+            }
+            if (!need) sums_flat(as, vals);
+        }
+        if (a.mixed) seg_accumulate<NSUM>(ns.accf, ns.acc, lane, p, vals);
+        unsigned mq = __ballot_sync(FULL, need);
+        if (mq) {
+            int pos = nq + __popc(mq & ((1u << lane) - 1u));
+            if (need) {
+                ns.qp[pos] = p;
+                ns.qk[pos] = k;
+            }
+            nq += __popc(mq);
+            __syncwarp();
+        }
+        while (nq >= 32 || (nq > 0 && i0 + 32 >= total)) {
+            const int take = nq < 32 ? nq : 32;
+            int qpair = 32 + lane;
+            double qv[NSUM];
+#pragma unroll
+            for (int z = 0; z < NSUM; ++z) qv[z] = 0.0;
+            if (lane < take) {
+                qpair = ns.qp[lane];
+                const TriGeo& Sq = wake ? a.wtri[list[qpair]] : a.tri[list[qpair]];
+                adj_point64(a, T, Sq, ns, pc.nu, qpair, ns.qk[lane], qv);
+            }
+            seg_accumulate<NSUM>(ns.accf, ns.acc, lane, qpair, qv);
+            const int rest = nq - take;
+            int mp = 0, mk = 0;
+            if (lane < rest) {
+                mp = ns.qp[take + lane];
+                mk = ns.qk[take + lane];
+            }
+            __syncwarp();
+            if (lane < rest) {
+                ns.qp[lane] = mp;
+                ns.qk[lane] = mk;
+            }
+            __syncwarp();
+            nq = rest;
+            n64 += take;
+        }
+    }
+    __syncwarp();
+    // each lane finishes its own pair
+    if (near) {
+        double f[NSUM];
+        for (int z = 0; z < NSUM; ++z) f[z] = ns.acc[lane][z] + double(ns.accf[lane][z]);
+        const AdjSums<double> d = sums_unflat(f);
+        const v3<double> m = mk3(ns.m64[lane][0], ns.m64[lane][1], ns.m64[lane][2]);
+        for (int k = 0; k < 3; ++k) Xg[k] += d.Xg[k];
+        U += cross(G, d.Q) + sig * d.Q;
+        fs += dot(d.Q, m);
+        v3<double> xS[3];
+        tri_corners(S, xS);
+        const SrcAdj<double> sa = src_of_pair(xS, d, m, nT);
+        double g[NSA];
+        sa_flat(sa, g);
+        double* dst = x.SA[wake ? 1 : 0] + size_t(s) * NSA;
+        for (int z = 0; z < NSA; ++z)
+            if (g[z] != 0.0) atomicAdd(dst + z, g[z]);
+    }
+    __syncwarp();
+    P[TIER_NEAR] += __popc(nearmask);
+    Q[TIER_NEAR] += (unsigned long long)total;
+    Q64 += n64;
+    return __ballot_sync(FULL, valid && !near);
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, AdjExtra x) {
+    extern __shared__ __align__(16) unsigned char adj_smem[];
+    AdjChunkSh& ns = reinterpret_cast<AdjChunkSh*>(adj_smem)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
+    const int idx = blockIdx.x * NEAR_WARPS + (threadIdx.x >> 5);
+    if (idx >= a.ntests) return;
+    const int t = a.tests[idx];
+    const TriGeo& T = a.tri[t];
+    PairCtx pc;
+    pc.a = &a;
+    pc.T = &T;
+    pc.sh = nullptr;
+    pc.lane = lane;
+    for (int k = 0; k < 3; ++k) pc.nu[k] = x.nu[T.slot[k]];
+    v3<double> Xg[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
+    v3<double> U = mk3(0.0, 0.0, 0.0);
+    double fs = 0;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+    for (int set = 0; set < 2; ++set) {
+        const bool wake = set == 1;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
+        const long long e1 = wake ? a.wf_ptr[t + 1] : a.nf_ptr[t + 1];
+        const int* src = wake ? a.wf_src : a.nf_src;
+        int* rest = wake ? a.wrest_src : a.rest_src;
+        int nrest = 0;
+        for (long long c0 = e0; c0 < e1; c0 += 32) {
+            const int cnt = int(e1 - c0 < 32 ? e1 - c0 : 32);
+            unsigned m = adj_chunk(pc, ns, x, t, src + c0, cnt, wake, Xg, U, fs, P, Q, Q64);
+            if ((m >> lane) & 1u) rest[e0 + nrest + __popc(m & ((1u << lane) - 1u))] = src[c0 + lane];
+            nrest += __popc(m);
+        }
+        if (lane == 0) a.rest_cnt[2 * t + set] = nrest;
+    }
+    // the test side, summed over the warp's pairs
+    double v[NTA] = {Xg[0].x, Xg[0].y, Xg[0].z, Xg[1].x, Xg[1].y, Xg[1].z, Xg[2].x, Xg[2].y, Xg[2].z, U.x, U.y, U.z, fs};
+#pragma unroll
+    for (int k = 0; k < NTA; ++k) v[k] = warp_sum(v[k]);
+    double mine = 0;
+#pragma unroll
+    for (int k = 0; k < NTA; ++k)
+        if (k == lane) mine = v[k];
+    if (lane < NTA && mine != 0.0) atomicAdd(x.TA + size_t(t) * NTA + lane, mine);
+    for (int k = 0; k < 6; ++k) {
+        unsigned long long pk = P[k], qk = Q[k];
+        if (lane == 0 && pk) atomicAdd(a.stats + k, pk);
+        if (lane == 0 && qk) atomicAdd(a.stats + 6 + k, qk);
+    }
+    if (lane == 0 && Q64) atomicAdd(a.stats + 12, Q64);
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// non-far pairs, tip filaments and freestream: one warp per test triangle
+
+
 // this lane's rule-geometry derivative (direction lane < 18) to the test triangle's nodes and the source's
 __device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjExtra& x, const TriGeo& T, const TriGeo* S, bool wake) {
     const int d = pc.lane;
@@ -279,6 +593,7 @@ __device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjExtra& x, const
     pc.gdir = 0;
 }
 
+// the pairs the lanes kernel left (self, touching, contact), the tip filaments and the freestream
 __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, AdjExtra x) {
     __shared__ WarpSh shm[NEAR_WARPS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -310,8 +625,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
     for (int set = 0; set < 2; ++set) {
         const bool wake = set == 1;
         const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
-        const long long e1 = wake ? a.wf_ptr[t + 1] : a.nf_ptr[t + 1];
-        const int* list = wake ? a.wf_src : a.nf_src;
+        const long long e1 = e0 + a.rest_cnt[2 * t + set];
+        const int* list = wake ? a.wrest_src : a.rest_src;
         for (long long e = e0; e < e1; ++e) {
             const int s = list[e];
             const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
@@ -634,10 +949,22 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         ex.gx = d_gx;
         ex.gwx = d_gwx;
         ex.dal = d_dal;
+        int *d_rest, *d_wrest, *d_rcnt;
+        if ((r = dl.alloc(ctx, &d_rest, size_t(std::max(ps.nfptr[ntri], 1LL)))) ||
+            (r = dl.alloc(ctx, &d_wrest, size_t(std::max(ps.wfptr[ntri], 1LL)))) ||
+            (r = dl.alloc(ctx, &d_rcnt, size_t(2) * ntri)))
+            return r;
+        na.rest_src = d_rest;
+        na.wrest_src = d_wrest;
+        na.rest_cnt = d_rcnt;
+        const size_t smem = sizeof(AdjChunkSh) * NEAR_WARPS;
+        VP_CUDA(ctx, cudaFuncSetAttribute(adj_lanes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
+        const int nb = (ntri + NEAR_WARPS - 1) / NEAR_WARPS;
         vp_phase_begin(ctx, PH_ADJ_NEAR);
-        adj_near_kernel<<<(ntri + NEAR_WARPS - 1) / NEAR_WARPS, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, ex);
+        adj_lanes_kernel<<<nb, 32 * NEAR_WARPS, smem, ctx->stream>>>(na, ex);
+        adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, ex);
         vp_phase_end(ctx);
-        ctx->launches++;
+        ctx->launches += 2;
         VP_CUDA(ctx, cudaGetLastError());
     }
     vp_phase_begin(ctx, PH_ADJOINT);

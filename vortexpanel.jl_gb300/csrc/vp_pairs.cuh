@@ -1371,6 +1371,204 @@ __device__ void vertex_rule(PairCtx& pc, Acc& acc, int k) {
     }
 }
 
+// ---- the near tier, one pair per lane: the plan shared by the assembly and the adjoint -------------------------------
+// A warp takes up to 32 sources of its test triangle at once. Each lane decides its own pair's tier (FP32 with the
+// reference's FP64 test where FP32 cannot decide, exactly as pair_rule / wake_pair_rule) and, for a pair in the near
+// tier, walks near_pieces' quadtree to its leaves (assemble.jl:131-142), stored as codes, with the pair's FP32 frame.
+struct NearPlanSh {
+    uint8_t leaf[32][64];  // leaf codes: level << 6 | path (level base-4 digits, most significant first)
+    float E32[32][27];     // x_T,k - v_S,a
+    float D32[32][9];      // x_T,k - c_S
+    float S32[32][26];     // d (9), nu (9), len (3), n (3), area, diam
+};
+
+__device__ __forceinline__ void leaf_corners32(int code, float* b) {
+    // the corners of a quadtree node in the test triangle's barycentrics (dyadic, exact in FP32)
+    int level = code >> 6, path = code & 63;
+    float c[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    for (int l = 0; l < level; ++l) {
+        int digit = (path >> (2 * (level - 1 - l))) & 3;
+        float m12[3], m23[3], m31[3];
+        for (int z = 0; z < 3; ++z) {
+            m12[z] = 0.5f * (c[z] + c[3 + z]);
+            m23[z] = 0.5f * (c[3 + z] + c[6 + z]);
+            m31[z] = 0.5f * (c[6 + z] + c[z]);
+        }
+        float n[9];
+        for (int z = 0; z < 3; ++z) {
+            if (digit == 0) { n[z] = c[z]; n[3 + z] = m12[z]; n[6 + z] = m31[z]; }
+            else if (digit == 1) { n[z] = m12[z]; n[3 + z] = c[3 + z]; n[6 + z] = m23[z]; }
+            else if (digit == 2) { n[z] = m31[z]; n[3 + z] = m23[z]; n[6 + z] = c[6 + z]; }
+            else { n[z] = m12[z]; n[3 + z] = m23[z]; n[6 + z] = m31[z]; }
+        }
+        for (int z = 0; z < 9; ++z) c[z] = n[z];
+    }
+    for (int z = 0; z < 9; ++z) b[z] = c[z];
+}
+
+// per-lane contributions (N values), keyed by pair (non-decreasing over the lanes, 32+ for none): segmented sums in a
+// fixed order, added to the pairs' accumulators (accf for FP32 contributions, acc for FP64 ones)
+template <int N, class V>
+__device__ __forceinline__ void seg_accumulate(float (*accf)[N], double (*acc)[N], int lane, int key, V* v) {
+    const unsigned FULL = 0xffffffffu;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int ky = __shfl_up_sync(FULL, key, o);
+#pragma unroll
+        for (int k = 0; k < N; ++k) {
+            V y = __shfl_up_sync(FULL, v[k], o);
+            if (lane >= o && ky == key) v[k] += y;
+        }
+    }
+    int kn = __shfl_down_sync(FULL, key, 1);
+    bool last = lane == 31 || kn != key;
+    if (last && key < 32) {
+        if (sizeof(V) == 4)
+            for (int k = 0; k < N; ++k) accf[key][k] += float(v[k]);
+        else
+            for (int k = 0; k < N; ++k) acc[key][k] += double(v[k]);
+    }
+    __syncwarp();
+}
+
+// returns whether this lane's pair (source s, S; valid: the lane has one) is in the near tier; nleaf: its leaves
+__device__ bool near_plan(PairCtx& pc, NearPlanSh& pl, int t, const TriGeo& S, int s, bool valid, bool wake, int& nleaf) {
+    const NearArgs& a = *pc.a;
+    const TriGeo& T = *pc.T;
+    const int lane = pc.lane;
+    // 1. the tier of this lane's pair
+    bool near = valid && a.test_mode != 2 && a.near_depth <= 3 && !(!wake && s == t);
+    if (near && !wake) {
+        for (int k = 0; k < 3; ++k)
+            if (T.node[k] == S.node[0] || T.node[k] == S.node[1] || T.node[k] == S.node[2]) near = false;
+        if (near && a.ntouch > 0) {
+            long long key = (long long)t * a.ntri + s;
+            int lo = 0, hi = a.ntouch;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (a.touch[mid] < key) lo = mid + 1;
+                else hi = mid;
+            }
+            if (lo < a.ntouch && a.touch[lo] == key) near = false;
+        }
+    }
+    // FP32 frame of this pair: S's corner 0 at the origin (differences taken in FP64); e32 bounds the FP32 rounding
+    v3<float> sv[3], tv[3];
+    float e32 = 0.f;
+    if (near) {
+        for (int q = 0; q < 3; ++q) {
+            sv[q] = mk3(float(S.x[3 * q] - S.x[0]), float(S.x[3 * q + 1] - S.x[1]), float(S.x[3 * q + 2] - S.x[2]));
+            tv[q] = mk3(float(T.x[3 * q] - S.x[0]), float(T.x[3 * q + 1] - S.x[1]), float(T.x[3 * q + 2] - S.x[2]));
+            e32 = fmaxf(e32, fmaxf(vnorm(sv[q]), vnorm(tv[q])));
+        }
+        e32 *= 1e-4f;
+    }
+    if (near) {  // contact_rule (assemble.jl:199-207) finds no contact beyond shared corners
+        const double tol = a.contact_rel * fmin(T.diam, S.diam);
+        const float tolf = float(tol);
+        // FP32 pass: 1 contact, 0 none, -1 undecided (then the FP64 test decides)
+        int res;
+        {
+            v3<float> dc = (sv[1] + sv[2]) * (1.f / 3.f) - (tv[0] + tv[1] + tv[2]) * (1.f / 3.f);
+            int far_reach = lt32(float(T.reach + S.reach + tol), vnorm(dc), e32);
+            if (far_reach == 1) {
+                res = 0;
+            } else {
+                bool any_true = false, any_undec = far_reach < 0;
+                for (int k = 0; k < 3; ++k) {
+                    int c = lt32(dist_tri_v(sv[0], sv[1], sv[2], tv[k]), tolf, e32);
+                    if (c == 1) any_true = true;
+                    else if (c < 0) any_undec = true;
+                }
+                for (int k = 0; k < 3 && !any_true; ++k) {
+                    v3<float> ta = tv[k], tc = tv[(k + 1) % 3];
+                    v3<float> ev = tc - ta;
+                    float L = vnorm(ev);
+                    for (int q = 0; q < 3; ++q) {
+                        float t = dot(sv[q] - ta, ev) / dot(ev, ev);
+                        t = fminf(fmaxf(t, 0.f), 1.f);
+                        float d = vnorm(sv[q] - (ta + t * ev));
+                        int c1 = lt32(d, tolf, e32) , c2 = lt32(tolf, t * L, 2.f * e32), c3 = lt32(tolf, (1.f - t) * L, 2.f * e32);
+                        if (d == tolf) c1 = -1;
+                        if (c1 == 1 && c2 == 1 && c3 == 1) any_true = true;
+                        else if (c1 != 0 && c2 != 0 && c3 != 0) any_undec = true;
+                    }
+                }
+                res = any_true ? 1 : (any_undec ? -1 : 0);
+                if (far_reach < 0 && res == 1) res = -1;  // contact needs the reach test passed
+            }
+        }
+        if (res < 0) {  // the reference's FP64 test
+            res = 0;
+            if (!(vnorm(ld3(S.c) - ld3(T.c)) > T.reach + S.reach + tol)) {
+                bool extra = false;
+                for (int k = 0; k < 3 && !extra; ++k)
+                    if (dist_tri(S.x, ld3(T.x + 3 * k)) <= tol) extra = true;
+                for (int k = 0; k < 3 && !extra; ++k)
+                    for (int q = 0; q < 3 && !extra; ++q) {
+                        double tt;
+                        if (on_edge_split(ld3(S.x + 3 * q), ld3(T.x + 3 * k), ld3(T.x + 3 * ((k + 1) % 3)), tol, tt))
+                            extra = true;
+                    }
+                res = extra ? 1 : 0;
+            }
+        }
+        if (res == 1) near = false;
+    }
+    // 2. near_pieces' leaves (assemble.jl:131-142), decided in FP32 unless a node is too close to the threshold
+    if (near) {
+        const int depth = a.near_depth;
+        const float ratiof = float(a.near_ratio);
+        int level = 0;
+        unsigned path = 0;
+        for (int guard = 0; guard < 1024; ++guard) {
+            float bf[9];
+            leaf_corners32((level << 6) | int(path), bf);
+            v3<float> p1 = bf[0] * tv[0] + bf[1] * tv[1] + bf[2] * tv[2];
+            v3<float> p2 = bf[3] * tv[0] + bf[4] * tv[1] + bf[5] * tv[2];
+            v3<float> p3 = bf[6] * tv[0] + bf[7] * tv[1] + bf[8] * tv[2];
+            float size = fmaxf(vnorm(p2 - p1), fmaxf(vnorm(p3 - p2), vnorm(p1 - p3)));
+            float d = dist_tri_v(sv[0], sv[1], sv[2], (p1 + p2 + p3) * (1.f / 3.f));
+            int split = level < depth ? lt32(d, ratiof * size, 2.f * e32) : 0;
+            if (split < 0) {  // the reference's FP64 test at this node
+                double b[9];
+                for (int z = 0; z < 9; ++z) b[z] = double(bf[z]);
+                v3<double> q1 = tpoint(T, b), q2 = tpoint(T, b + 3), q3 = tpoint(T, b + 6);
+                double sz = fmax(vnorm(q2 - q1), fmax(vnorm(q3 - q2), vnorm(q1 - q3)));
+                split = dist_tri(S.x, (q1 + q2 + q3) / 3.0) < a.near_ratio * sz ? 1 : 0;
+            }
+            if (split) {
+                level++;
+                path *= 4;
+                continue;
+            }
+            pl.leaf[lane][nleaf++] = uint8_t((level << 6) | path);
+            while (level > 0 && (path & 3) == 3) {
+                path >>= 2;
+                level--;
+            }
+            if (level == 0) break;
+            path++;
+        }
+        for (int k = 0; k < 3; ++k)
+            for (int q = 0; q < 3; ++q)
+                for (int z = 0; z < 3; ++z) pl.E32[lane][9 * k + 3 * q + z] = float(T.x[3 * k + z] - S.x[3 * q + z]);
+        for (int k = 0; k < 3; ++k)
+            for (int z = 0; z < 3; ++z) pl.D32[lane][3 * k + z] = float(T.x[3 * k + z] - S.c[z]);
+        for (int k = 0; k < 9; ++k) {
+            pl.S32[lane][k] = float(S.x[k] - S.c[k % 3]);
+            pl.S32[lane][9 + k] = float(S.nu[k]);
+        }
+        for (int k = 0; k < 3; ++k) {
+            pl.S32[lane][18 + k] = float(S.len[k]);
+            pl.S32[lane][21 + k] = float(S.n[k]);
+        }
+        pl.S32[lane][24] = float(S.area);
+        pl.S32[lane][25] = float(S.diam);
+    }
+    return near;
+}
+
 // ------------------------------------------------------------------------------------------------------------------
 // host: tiles and colours
 
