@@ -284,7 +284,8 @@ def main():
             "gpu_launches": launches // args.steps * args.steps, "phases_ms": per,
             "CL": CL, "CDi": CDi, "cond": cond, "tiers": stats, "roofline": roof, "clocks": clk.summary(),
             "fp64_point_share": stats["points_fp64"] / max(1, sum(stats["points"].values())),
-            "adjoint_points": out["adjoint_points"]}
+            "adjoint_points": out["adjoint_points"],
+            "adjoint_fp64_point_share": out["adjoint_points_fp64"] / max(1, sum(out["adjoint_points"].values()))}
     line.update(fp)
     if not args.no_cpu_baseline:
         cb = cpu_baseline(w, wake, W, V)

@@ -237,6 +237,7 @@ def wing_gradients(w, wake, W, alpha, precision="mixed", opts=None, ctx=None, ti
         nu = dm.C @ xi[:, k]
         fx, fw, fa, st = pair_derivatives(g, dm, sig, V, dV, nu, mu_cols, opts=opts, wake=wake, ctx=ctx)
         out["adjoint_points"] = dict(zip(("self", "edge", "vertex", "contact", "near", "far"), list(st.points)))
+        out["adjoint_points_fp64"] = st.points_fp64
         grad = gx - fx
         if wake is not None and len(fw):
             np.add.at(grad, dm.wake_te.node[wake.te], -fw)
