@@ -151,6 +151,24 @@ int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const double* tr
 int vp_eval_points_static(vp_ctx* ctx, int mode, int precision, int n, const double* tri, const double* x,
                           const double* m, int side, double kernel_far, double* out);
 
+/* Free wake (src/freewake/step.jl, src/assembly/explicit.jl). Blobs are given as 7 doubles each: x (3), alpha (3),
+ * core delta. precision VP_FP64, or VP_MIXED for FP32 arithmetic with FP64 accumulation.
+ *   vp_blob_velocities  <- FreeWake.blob_velocities(blobs, X)                         src/freewake/step.jl:176-187
+ *                          the Rosenhead-Moore sum (src/kernels/blob.jl:21-25) of every blob at every point X.
+ *   vp_body_velocity    <- Post.body_velocity(els, sigma, gamma, xs; kernel_far)       src/post/Post.jl:92-112
+ *                          sigma_s w_s + gamma_s x w_s of every triangle (corners 9, sigma 1, gamma 3 each) at X.
+ *   vp_explicit_rhs     <- Assembly.explicit_rhs(els, dm, ExplicitSources(...); opts) src/assembly/explicit.jl:31-85
+ *                          -int psi_i n.u dA of known sheets (corners 9, corner doublets 3 each), filaments (ends 6,
+ *                          end circulations 2 each) and particles, one value per slot (rhs, nslot). */
+int vp_blob_velocities(vp_ctx* ctx, int precision, int nblob, const double* blobs, int npts, const double* X,
+                       double* U);
+int vp_body_velocity(vp_ctx* ctx, int precision, int ntri, const double* corners, const double* sigma,
+                     const double* gamma, double kernel_far, int npts, const double* X, double* U);
+int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri,
+                    const int* tris, const int* corner_slot, int nslot, int nsheet, const double* sheet_x,
+                    const double* sheet_mu, int nseg, const double* seg_x, const double* seg_gamma, int nblob,
+                    const double* blobs, double* rhs);
+
 /* Condition estimate and size of a factorization. */
 int vp_factor_info(const vp_factor* F, int* n, double* cond);
 void vp_factor_free(vp_factor* F);

@@ -6,7 +6,7 @@
 int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
                      const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                      const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
-                     const int* fil, vp_system** out, vp_assembly_stats* stats);
+                     const int* fil, vp_system** out, vp_assembly_stats* stats, int body_sources);
 int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
                     const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                     const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
@@ -140,7 +140,7 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
     if (!ctx) return VP_ERR_ARG;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
     return vp_assemble_impl(ctx, opts, nnode, x, ntri, tris, corner_slot, nslot, ntouch, touch_pairs, sigma, vinf,
-                            nwnode, wx, nwtri, wtris, nfil, fil, out, stats);
+                            nwnode, wx, nwtri, wtris, nfil, fil, out, stats, 1);
 }
 
 int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,

@@ -643,15 +643,16 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
 
 }  // namespace
 
+// body_sources = 0: the columns of the wake's sheets and filaments alone (explicit_rhs); A's body columns stay zero
 int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
                      const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                      const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
-                     const int* fil, vp_system** out, vp_assembly_stats* stats) {
+                     const int* fil, vp_system** out, vp_assembly_stats* stats, int body_sources) {
     auto t0 = std::chrono::steady_clock::now();
     if (!out) return vp_fail(ctx, VP_ERR_ARG, "null argument");
     *out = nullptr;
     const PairInput in{o,     nnode, x,     ntri, tris,  corner_slot, nslot, ntouch, touch_pairs,
-                       sigma, vinf,  nwnode, wx,  nwtri, wtris,       nfil,  fil};
+                       sigma, vinf,  nwnode, wx,  nwtri, wtris,       nfil,  fil,   body_sources != 0};
     PairSetup ps;
     int r = setup_pairs(ctx, in, PH_SETUP, PH_CLASSIFY, ps);
     if (r) return r;
@@ -696,7 +697,7 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         fa.ratio = o->far_ratio;
         fa.kernel_far = o->kernel_far;
         const std::vector<TriGeo>* sets[2] = {&tg, &wg};
-        int nsrc[2] = {ntri, nwtri};
+        int nsrc[2] = {body_sources ? ntri : 0, nwtri};
         for (int set = 0; set < fa.nset; ++set) {
             std::vector<TriGeo> g(sets[set]->begin(), sets[set]->begin() + nsrc[set]);
             SrcTiles st = make_src_tiles(g);

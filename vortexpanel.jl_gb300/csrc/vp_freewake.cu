@@ -1,0 +1,401 @@
+// The free wake's device work (src/freewake/step.jl, src/assembly/explicit.jl, src/post/Post.jl:92-112):
+//   - blob velocities: the direct Rosenhead-Moore sum of every blob at every wake point (blob_velocities,
+//     step.jl:176-187), a tiled N-body kernel: one thread per point, the blobs staged through shared memory in tiles;
+//   - body velocity: sigma_s w_s + gamma_s x w_s of every body triangle at every wake point (body_velocity), one
+//     thread per point over shared-memory tiles of triangles, the exact kernel within kernel_far diameters and the
+//     multipole beyond;
+//   - explicit right hand side (explicit_rhs, explicit.jl:31-85): the wake's known sheets and filaments through the
+//     assembly's own tiers (their columns assembled with the body as test triangles only, times their doublets), and
+//     the particles with the far rule or, closer than far_ratio, the near rule.
+#include "vp_pairs.cuh"
+
+int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
+                     const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
+                     const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
+                     const int* fil, vp_system** out, vp_assembly_stats* stats, int body_sources);
+
+namespace {
+
+constexpr int NB_THREADS = 256;  // points per CTA of the N-body and body-velocity kernels
+constexpr int NB_TILE = 256;     // blobs per shared-memory tile
+
+// blob_velocity (blob.jl:21-25): (1/4pi) alpha x r / (|r|^2 + delta^2)^(3/2), r = x - xp
+template <class T>
+__device__ __forceinline__ v3<T> blob_vel(v3<T> r, v3<T> al, T d2core) {
+    T d2 = dot(r, r) + d2core;
+    T s = T(1) / (T(4) * vp_pi<T>() * d2 * vsqrt(d2));
+    return s * cross(al, r);
+}
+
+// blobs: x (3), alpha (3), delta (1) per blob. FP32: every tile summed in FP32, the tiles in FP64.
+template <class T>
+__global__ void __launch_bounds__(NB_THREADS) blob_kernel(int nblob, const double* __restrict__ blobs, int npts,
+                                                        const double* __restrict__ X, double* __restrict__ U) {
+    __shared__ T sb[NB_TILE][8];
+    const int i = blockIdx.x * NB_THREADS + threadIdx.x;
+    const bool valid = i < npts;
+    v3<double> x = valid ? mk3(X[3 * i], X[3 * i + 1], X[3 * i + 2]) : mk3(0.0, 0.0, 0.0);
+    const v3<T> xt = mk3(T(x.x), T(x.y), T(x.z));
+    v3<double> acc = mk3(0.0, 0.0, 0.0);
+    for (int b0 = 0; b0 < nblob; b0 += NB_TILE) {
+        const int nb = min(NB_TILE, nblob - b0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < nb; k += NB_THREADS) {
+            const double* p = blobs + 7 * size_t(b0 + k);
+            for (int z = 0; z < 6; ++z) sb[k][z] = T(p[z]);
+            sb[k][6] = T(p[6] * p[6]);
+        }
+        __syncthreads();
+        v3<T> part = mk3(T(0), T(0), T(0));
+#pragma unroll 4
+        for (int k = 0; k < nb; ++k) {
+            v3<T> r = xt - mk3(sb[k][0], sb[k][1], sb[k][2]);
+            part += blob_vel(r, mk3(sb[k][3], sb[k][4], sb[k][5]), sb[k][6]);
+        }
+        acc += mk3(double(part.x), double(part.y), double(part.z));
+    }
+    if (valid) {
+        U[3 * i] = acc.x;
+        U[3 * i + 1] = acc.y;
+        U[3 * i + 2] = acc.z;
+    }
+}
+
+// body triangles as sources: corners (9), sigma, gamma (3) -> the kernel's data in FP64
+struct BodySrc {
+    double c[3], d[9], nu[9], len[3], n[3], area, diam, sigma, gam[3];
+};
+
+template <class T>
+__device__ __forceinline__ SrcKern<T> kern_from(const BodySrc& s) {
+    SrcKern<T> K;
+    for (int k = 0; k < 3; ++k) {
+        K.d[k] = mk3(T(s.d[3 * k]), T(s.d[3 * k + 1]), T(s.d[3 * k + 2]));
+        K.nu[k] = mk3(T(s.nu[3 * k]), T(s.nu[3 * k + 1]), T(s.nu[3 * k + 2]));
+        K.len[k] = T(s.len[k]);
+    }
+    K.n = mk3(T(s.n[0]), T(s.n[1]), T(s.n[2]));
+    K.area = T(s.area);
+    K.diam = T(s.diam);
+    return K;
+}
+
+// source_velocity (source_triangle.jl:134-138) off the body: exact within kernel_far diameters, multipole beyond.
+// FP32 (mixed): the exact form under the FP32 guard, FP64 where the guard refuses.
+template <class T>
+__global__ void __launch_bounds__(NB_THREADS) body_kernel(int nsrc, const BodySrc* __restrict__ src, double kernel_far,
+                                                        int npts, const double* __restrict__ X, double* __restrict__ U) {
+    __shared__ BodySrc ss[32];
+    const int i = blockIdx.x * NB_THREADS + threadIdx.x;
+    const bool valid = i < npts;
+    const v3<double> x = valid ? mk3(X[3 * i], X[3 * i + 1], X[3 * i + 2]) : mk3(0.0, 0.0, 0.0);
+    v3<double> acc = mk3(0.0, 0.0, 0.0);
+    const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+    for (int s0 = 0; s0 < nsrc; s0 += 32) {
+        const int ns = min(32, nsrc - s0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < ns * int(sizeof(BodySrc) / 8); k += NB_THREADS)
+            reinterpret_cast<double*>(ss)[k] = reinterpret_cast<const double*>(src + s0)[k];
+        __syncthreads();
+        if (!valid) continue;
+        for (int k = 0; k < ns; ++k) {
+            const BodySrc& s = ss[k];
+            const v3<double> r64 = x - mk3(s.c[0], s.c[1], s.c[2]);
+            const double fd = kernel_far * s.diam;
+            v3<double> w;
+            bool done = false;
+            if (sizeof(T) == 4) {
+                const SrcKern<float> K = kern_from<float>(s);
+                const v3<float> r = mk3(float(r64.x), float(r64.y), float(r64.z));
+                v3<float> wf;
+                if (dot(r64, r64) > fd * fd) {
+                    wf = sv_far(K, r);
+                    done = true;
+                } else {
+                    done = sv_exact3_guarded(K, r - K.d[0], r - K.d[1], r - K.d[2], 0, g, wf);
+                }
+                if (done) w = mk3(double(wf.x), double(wf.y), double(wf.z));
+            }
+            if (!done) {
+                const SrcKern<double> K = kern_from<double>(s);
+                w = sv_rel(K, r64, 0, kernel_far, 1e-12);
+            }
+            acc += s.sigma * w + cross(mk3(s.gam[0], s.gam[1], s.gam[2]), w);
+        }
+    }
+    if (valid) {
+        U[3 * i] = acc.x;
+        U[3 * i + 1] = acc.y;
+        U[3 * i + 2] = acc.z;
+    }
+}
+
+// the particles' part of explicit_rhs: one warp per test triangle, the lanes over the particles; far particles with
+// the far rule's points, near ones with near_rule's quadtree about the particle (explicit.jl:63-76), evaluated by the
+// lane alone. Rows are added with atomics (a slot's rows come from several test triangles).
+struct BlobRhsArgs {
+    const TriGeo* tri;
+    int ntri, nblob;
+    const double* blobs;  // x (3), alpha (3), delta
+    const RulePt* rfar;
+    int nfar;
+    const RulePt* rnear;
+    int nnear;
+    int test_mode, near_depth;
+    double far_ratio, near_ratio;
+    double* rhs;
+};
+
+template <class T>
+__device__ __forceinline__ void blob_rows(const BlobRhsArgs& a, const TriGeo& Tr, const double* b, double l0, double l1,
+                                          double l2, double W, const double* bl, double* rows) {
+    v3<double> x = mk3(l0 * Tr.x[0] + l1 * Tr.x[3] + l2 * Tr.x[6], l0 * Tr.x[1] + l1 * Tr.x[4] + l2 * Tr.x[7],
+                       l0 * Tr.x[2] + l1 * Tr.x[5] + l2 * Tr.x[8]);
+    v3<double> r = x - mk3(bl[0], bl[1], bl[2]);
+    v3<T> u = blob_vel(mk3(T(r.x), T(r.y), T(r.z)), mk3(T(bl[3]), T(bl[4]), T(bl[5])), T(bl[6] * bl[6]));
+    double un = (double(u.x) * Tr.n[0] + double(u.y) * Tr.n[1] + double(u.z) * Tr.n[2]) * W;
+    v3<double> psi = test_weights(a.test_mode, l0, l1, l2);
+    rows[0] -= un * psi.x;
+    rows[1] -= un * psi.y;
+    rows[2] -= un * psi.z;
+    (void)b;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) blob_rhs_kernel(BlobRhsArgs a) {
+    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (w >= a.ntri) return;
+    const TriGeo& Tr = a.tri[w];
+    double rows[3] = {0, 0, 0};
+    for (int k = lane; k < a.nblob; k += 32) {
+        const double* bl = a.blobs + 7 * size_t(k);
+        const double dx = bl[0] - Tr.c[0], dy = bl[1] - Tr.c[1], dz = bl[2] - Tr.c[2];
+        if (sqrt(dx * dx + dy * dy + dz * dz) > a.far_ratio * fmax(Tr.diam, bl[6])) {
+            for (int q = 0; q < a.nfar; ++q) {
+                const RulePt& m = a.rfar[q];
+                blob_rows<T>(a, Tr, nullptr, m.l0, m.l1, m.l2, m.w * Tr.area, bl, rows);
+            }
+            continue;
+        }
+        // near_rule about the particle (assemble.jl:69-91 with distance_to(b, p) = |p - x_b|): depth-first quadtree
+        int level = 0;
+        unsigned path = 0;
+        for (int guard = 0; guard < (1 << 20); ++guard) {
+            double c[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+            for (int l = 0; l < level; ++l) {
+                int digit = (path >> (2 * (level - 1 - l))) & 3;
+                double m12[3], m23[3], m31[3], nb[9];
+                for (int z = 0; z < 3; ++z) {
+                    m12[z] = 0.5 * (c[z] + c[3 + z]);
+                    m23[z] = 0.5 * (c[3 + z] + c[6 + z]);
+                    m31[z] = 0.5 * (c[6 + z] + c[z]);
+                }
+                for (int z = 0; z < 3; ++z) {
+                    if (digit == 0) { nb[z] = c[z]; nb[3 + z] = m12[z]; nb[6 + z] = m31[z]; }
+                    else if (digit == 1) { nb[z] = m12[z]; nb[3 + z] = c[3 + z]; nb[6 + z] = m23[z]; }
+                    else if (digit == 2) { nb[z] = m31[z]; nb[3 + z] = m23[z]; nb[6 + z] = c[6 + z]; }
+                    else { nb[z] = m12[z]; nb[3 + z] = m23[z]; nb[6 + z] = m31[z]; }
+                }
+                for (int z = 0; z < 9; ++z) c[z] = nb[z];
+            }
+            v3<double> p1 = tpoint(Tr, c), p2 = tpoint(Tr, c + 3), p3 = tpoint(Tr, c + 6);
+            double size = fmax(vnorm(p2 - p1), fmax(vnorm(p3 - p2), vnorm(p1 - p3)));
+            v3<double> pc = (p1 + p2 + p3) / 3.0 - mk3(bl[0], bl[1], bl[2]);
+            if (level < a.near_depth && vnorm(pc) < a.near_ratio * size) {
+                level++;
+                path *= 4;
+                continue;
+            }
+            const double frac = ldexp(1.0, -2 * level);
+            for (int q = 0; q < a.nnear; ++q) {
+                const RulePt& m = a.rnear[q];
+                double l0 = m.l0 * c[0] + m.l1 * c[3] + m.l2 * c[6];
+                double l1 = m.l0 * c[1] + m.l1 * c[4] + m.l2 * c[7];
+                double l2 = m.l0 * c[2] + m.l1 * c[5] + m.l2 * c[8];
+                blob_rows<T>(a, Tr, c, l0, l1, l2, m.w * frac * Tr.area, bl, rows);
+            }
+            while (level > 0 && (path & 3) == 3) {
+                path >>= 2;
+                level--;
+            }
+            if (level == 0) break;
+            path++;
+        }
+    }
+    for (int k = 0; k < 3; ++k) {
+        double v = warp_sum(rows[k]);
+        if (lane == k && v != 0.0) atomicAdd(a.rhs + Tr.slot[k], v);
+    }
+}
+
+int points_grid(int n) { return (n + NB_THREADS - 1) / NB_THREADS; }
+
+}  // namespace
+
+extern "C" int vp_blob_velocities(vp_ctx* ctx, int precision, int nblob, const double* blobs, int npts, const double* X,
+                                  double* U) {
+    if (!ctx || npts < 0 || nblob < 0 || (npts > 0 && (!X || !U)) || (nblob > 0 && !blobs))
+        return vp_fail(ctx, VP_ERR_ARG, "bad argument");
+    if (npts == 0) return VP_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    if (nblob == 0) {
+        for (size_t k = 0; k < 3 * size_t(npts); ++k) U[k] = 0.0;
+        return VP_OK;
+    }
+    DevList dl;
+    double *db, *dx, *du;
+    int r;
+    std::vector<double> hb(blobs, blobs + 7 * size_t(nblob));
+    std::vector<double> hx(X, X + 3 * size_t(npts));
+    if ((r = dl.up(ctx, &db, hb)) || (r = dl.up(ctx, &dx, hx)) || (r = dl.alloc(ctx, &du, 3 * size_t(npts)))) return r;
+    if (precision == VP_FP64)
+        blob_kernel<double><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(nblob, db, npts, dx, du);
+    else
+        blob_kernel<float><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(nblob, db, npts, dx, du);
+    ctx->launches++;
+    VP_CUDA(ctx, cudaGetLastError());
+    VP_CUDA(ctx, vp_d2h(ctx, U, du, sizeof(double) * 3 * npts));
+    VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return VP_OK;
+}
+
+extern "C" int vp_body_velocity(vp_ctx* ctx, int precision, int ntri, const double* corners, const double* sigma,
+                                const double* gamma, double kernel_far, int npts, const double* X, double* U) {
+    if (!ctx || ntri < 0 || npts < 0 || (ntri > 0 && (!corners || !sigma || !gamma)) || (npts > 0 && (!X || !U)) ||
+        !(kernel_far > 0))
+        return vp_fail(ctx, VP_ERR_ARG, "bad argument");
+    if (npts == 0) return VP_OK;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    std::vector<BodySrc> hs(std::max(ntri, 1));
+    for (int t = 0; t < ntri; ++t) {
+        TriGeo g;
+        const double* c = corners + 9 * size_t(t);
+        if (!make_tri(c, c + 3, c + 6, g)) return vp_fail(ctx, VP_ERR_DEGENERATE, "degenerate triangle " + std::to_string(t));
+        BodySrc& s = hs[t];
+        for (int k = 0; k < 3; ++k) {
+            s.c[k] = g.c[k];
+            s.len[k] = g.len[k];
+            s.n[k] = g.n[k];
+            s.gam[k] = gamma[3 * size_t(t) + k];
+        }
+        for (int k = 0; k < 9; ++k) {
+            s.d[k] = g.x[k] - g.c[k % 3];
+            s.nu[k] = g.nu[k];
+        }
+        s.area = g.area;
+        s.diam = g.diam;
+        s.sigma = sigma[t];
+    }
+    DevList dl;
+    BodySrc* ds;
+    double *dx, *du;
+    int r;
+    std::vector<double> hx(X, X + 3 * size_t(npts));
+    if ((r = dl.up(ctx, &ds, hs)) || (r = dl.up(ctx, &dx, hx)) || (r = dl.alloc(ctx, &du, 3 * size_t(npts)))) return r;
+    if (precision == VP_FP64)
+        body_kernel<double><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(ntri, ds, kernel_far, npts, dx, du);
+    else
+        body_kernel<float><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(ntri, ds, kernel_far, npts, dx, du);
+    ctx->launches++;
+    VP_CUDA(ctx, cudaGetLastError());
+    VP_CUDA(ctx, vp_d2h(ctx, U, du, sizeof(double) * 3 * npts));
+    VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return VP_OK;
+}
+
+extern "C" int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri,
+                               const int* tris, const int* corner_slot, int nslot, int nsheet, const double* sheet_x,
+                               const double* sheet_mu, int nseg, const double* seg_x, const double* seg_gamma,
+                               int nblob, const double* blobs, double* rhs) {
+    if (!ctx || !o || !x || !tris || !corner_slot || !rhs || nsheet < 0 || nseg < 0 || nblob < 0 ||
+        (nsheet > 0 && (!sheet_x || !sheet_mu)) || (nseg > 0 && (!seg_x || !seg_gamma)) || (nblob > 0 && !blobs))
+        return vp_fail(ctx, VP_ERR_ARG, "bad argument");
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    int r;
+    DevList dl;
+    double* d_rhs;
+    if ((r = dl.alloc(ctx, &d_rhs, size_t(nslot)))) return r;
+    VP_CUDA(ctx, cudaMemsetAsync(d_rhs, 0, sizeof(double) * nslot, ctx->stream));
+    // sheets and filaments: their own nodes (unshared), their columns assembled with the body's test triangles
+    const int nw = 3 * nsheet + 2 * nseg;
+    if (nw > 0) {
+        std::vector<double> wx(3 * size_t(nw)), mu(nw);
+        std::vector<int> wt(3 * size_t(std::max(nsheet, 1)), 0), fl(2 * size_t(std::max(nseg, 1)), 0);
+        for (int s = 0; s < nsheet; ++s)
+            for (int k = 0; k < 3; ++k) {
+                for (int z = 0; z < 3; ++z) wx[3 * (3 * size_t(s) + k) + z] = sheet_x[9 * size_t(s) + 3 * k + z];
+                mu[3 * s + k] = sheet_mu[3 * size_t(s) + k];
+                wt[3 * size_t(s) + k] = 3 * s + k;
+            }
+        for (int f = 0; f < nseg; ++f)
+            for (int k = 0; k < 2; ++k) {
+                const int node = 3 * nsheet + 2 * f + k;
+                for (int z = 0; z < 3; ++z) wx[3 * size_t(node) + z] = seg_x[6 * size_t(f) + 3 * k + z];
+                mu[node] = seg_gamma[2 * size_t(f) + k];
+                fl[2 * size_t(f) + k] = node;
+            }
+        std::vector<double> sig(ntri, 0.0);
+        const double vzero[3] = {0, 0, 0};
+        vp_system* sys = nullptr;
+        r = vp_assemble_impl(ctx, o, nnode, x, ntri, tris, corner_slot, nslot, 0, nullptr, sig.data(), vzero, nw,
+                             wx.data(), nsheet, wt.data(), nseg, fl.data(), &sys, nullptr, 0);
+        if (r) return r;
+        double* d_mu;
+        if ((r = dl.up(ctx, &d_mu, mu))) {
+            vp_system_free(sys);
+            return r;
+        }
+        const double mone = -1.0, zero = 0.0;
+        // A is row-major nslot x (nslot + nw): its wake block, read column-major, is nw x nslot with leading dim ncols
+        cublasStatus_t bs = cublasDgemv(ctx->blas, CUBLAS_OP_T, nw, nslot, &mone, sys->A + nslot, sys->ncols, d_mu, 1,
+                                        &zero, d_rhs, 1);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        vp_system_free(sys);
+        if (bs != CUBLAS_STATUS_SUCCESS) return vp_fail(ctx, VP_ERR_CUDA, "cublasDgemv");
+        if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("explicit_rhs: ") + cudaGetErrorString(e));
+    }
+    // particles
+    if (nblob > 0) {
+        std::vector<TriGeo> tg(ntri);
+        for (int t = 0; t < ntri; ++t) {
+            if (!make_tri(x + 3 * tris[3 * t], x + 3 * tris[3 * t + 1], x + 3 * tris[3 * t + 2], tg[t]))
+                return vp_fail(ctx, VP_ERR_DEGENERATE, "degenerate triangle " + std::to_string(t));
+            for (int k = 0; k < 3; ++k) {
+                tg[t].node[k] = tris[3 * t + k];
+                tg[t].slot[k] = corner_slot[3 * t + k];
+            }
+        }
+        std::vector<RulePt> rfar = triangle_rule(o->far_points), rnear = triangle_rule(o->near_points);
+        std::vector<double> hb(blobs, blobs + 7 * size_t(nblob));
+        TriGeo* d_tg;
+        RulePt *d_rf, *d_rn;
+        double* d_b;
+        if ((r = dl.up(ctx, &d_tg, tg)) || (r = dl.up(ctx, &d_rf, rfar)) || (r = dl.up(ctx, &d_rn, rnear)) ||
+            (r = dl.up(ctx, &d_b, hb)))
+            return r;
+        BlobRhsArgs a{};
+        a.tri = d_tg;
+        a.ntri = ntri;
+        a.nblob = nblob;
+        a.blobs = d_b;
+        a.rfar = d_rf;
+        a.nfar = (int)rfar.size();
+        a.rnear = d_rn;
+        a.nnear = (int)rnear.size();
+        a.test_mode = o->test;
+        a.near_depth = o->near_depth;
+        a.far_ratio = o->far_ratio;
+        a.near_ratio = o->near_ratio;
+        a.rhs = d_rhs;
+        const int nb = (ntri * 32 + 127) / 128;
+        if (o->precision == VP_FP64)
+            blob_rhs_kernel<double><<<nb, 128, 0, ctx->stream>>>(a);
+        else
+            blob_rhs_kernel<float><<<nb, 128, 0, ctx->stream>>>(a);
+        ctx->launches++;
+        VP_CUDA(ctx, cudaGetLastError());
+    }
+    VP_CUDA(ctx, vp_d2h(ctx, rhs, d_rhs, sizeof(double) * nslot));
+    VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return VP_OK;
+}

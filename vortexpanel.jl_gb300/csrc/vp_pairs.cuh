@@ -1724,6 +1724,7 @@ struct PairInput {
     const int* wtris;
     int nfil;
     const int* fil;
+    bool body_sources = true;  // false: only the wake's sheets and filaments are sources (explicit_rhs)
 };
 
 struct PairSetup {
@@ -1887,12 +1888,14 @@ int setup_pairs(vp_ctx* ctx, const PairInput& in, int ph_setup, int ph_classify,
     ps.wfptr.assign(ntri + 1, 0);
     std::vector<int> cnt(ntri);
     ps.ratio32 = float(o->far_ratio);
-    classify_kernel<<<ntri, 256, 0, ctx->stream>>>(0, ntri, ps.d_tc, ps.d_tg, ntri, ps.d_tc, ps.d_tg, ps.ratio32,
-                                                   o->far_ratio, d_cnt, nullptr, nullptr);
-    ctx->launches++;
-    VP_CUDA(ctx, vp_d2h(ctx, cnt.data(), d_cnt, sizeof(int) * ntri));
-    VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
-    for (int t = 0; t < ntri; ++t) ps.nfptr[t + 1] = ps.nfptr[t] + cnt[t];
+    if (in.body_sources) {
+        classify_kernel<<<ntri, 256, 0, ctx->stream>>>(0, ntri, ps.d_tc, ps.d_tg, ntri, ps.d_tc, ps.d_tg, ps.ratio32,
+                                                       o->far_ratio, d_cnt, nullptr, nullptr);
+        ctx->launches++;
+        VP_CUDA(ctx, vp_d2h(ctx, cnt.data(), d_cnt, sizeof(int) * ntri));
+        VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int t = 0; t < ntri; ++t) ps.nfptr[t + 1] = ps.nfptr[t] + cnt[t];
+    }
     if (nwtri > 0) {
         classify_kernel<<<ntri, 256, 0, ctx->stream>>>(0, ntri, ps.d_tc, ps.d_tg, nwtri, ps.d_wc, ps.d_wg, ps.ratio32,
                                                        o->far_ratio, d_cnt, nullptr, nullptr);
@@ -1905,9 +1908,11 @@ int setup_pairs(vp_ctx* ctx, const PairInput& in, int ph_setup, int ph_classify,
         (r = dl.alloc(ctx, &ps.d_nf, size_t(std::max(ps.nfptr[ntri], 1LL)))) ||
         (r = dl.alloc(ctx, &ps.d_wf, size_t(std::max(ps.wfptr[ntri], 1LL)))))
         return r;
-    classify_kernel<<<ntri, 256, 0, ctx->stream>>>(1, ntri, ps.d_tc, ps.d_tg, ntri, ps.d_tc, ps.d_tg, ps.ratio32,
-                                                   o->far_ratio, nullptr, ps.d_nfptr, ps.d_nf);
-    ctx->launches++;
+    if (in.body_sources) {
+        classify_kernel<<<ntri, 256, 0, ctx->stream>>>(1, ntri, ps.d_tc, ps.d_tg, ntri, ps.d_tc, ps.d_tg, ps.ratio32,
+                                                       o->far_ratio, nullptr, ps.d_nfptr, ps.d_nf);
+        ctx->launches++;
+    }
     if (nwtri > 0) {
         classify_kernel<<<ntri, 256, 0, ctx->stream>>>(1, ntri, ps.d_tc, ps.d_tg, nwtri, ps.d_wc, ps.d_wg, ps.ratio32,
                                                        o->far_ratio, nullptr, ps.d_wfptr, ps.d_wf);

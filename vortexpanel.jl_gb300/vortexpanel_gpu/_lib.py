@@ -59,6 +59,12 @@ SIGNATURES = [
      [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
       ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I, D, D, D, D, D, D,
       ctypes.POINTER(vp_assembly_stats)]),
+    ("vp_blob_velocities", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, ctypes.c_int, D, D]),
+    ("vp_body_velocity", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, D, D, ctypes.c_double,
+                                        ctypes.c_int, D, D]),
+    ("vp_explicit_rhs", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D,
+                                       ctypes.c_int, I, I, ctypes.c_int, ctypes.c_int, D, D, ctypes.c_int, D, D,
+                                       ctypes.c_int, D, D]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]
