@@ -120,6 +120,29 @@ def peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
+def nbody(vp, ctx, n=400_000, reps=3):
+    """The free wake's blob N-body kernel on a synthetic cloud of n blobs at their own n positions (positions uniform
+    in [0,8] x [-4,4] x [-1,1], strengths N(0,1)^3 1e-3, core 0.05, seed 1), mixed precision: interactions per second
+    and its roofline (28 FP32 flops per interaction) from the kernel's device time"""
+    from vortexpanel_gpu import freewake
+
+    rng = np.random.default_rng(1)
+    x = rng.uniform([0, -4, -1], [8, 4, 1], (n, 3))
+    blobs = np.hstack([x, 1e-3 * rng.standard_normal((n, 3)), np.full((n, 1), 0.05)])
+    freewake.blob_velocities(blobs[:1000], x[:1000], precision="mixed", ctx=ctx)
+    ctx.phase_times(reset=True)
+    for _ in range(reps):
+        freewake.blob_velocities(blobs, x, precision="mixed", ctx=ctx)
+    ph, _ = ctx.phase_times(reset=True)
+    t = ph["wake"] / 1e3 / reps
+    pk, _ = peaks()
+    peak = 152 * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    ach = 28 * n * n / t / 1e12
+    return {"blobs": n, "points": n, "ms": t * 1e3, "interactions_per_s": n * n / t,
+            "roofline": {"kernel": "blob_kernel<float>", "bound": "fp32", "achieved": ach, "peak": peak,
+                         "unit": "TFLOP/s", "frac": ach / peak, "peak_source": "nominal"}}
+
+
 def cpu_baseline(w, wake, W, V, budget_s=20.0):
     """The oracle (C++ restatement of the reference's assembly, OpenMP over test triangles as assemble.jl:395, and the
     reference's LAPACK dgetrf/dgetrs through scipy) on a bounded sample: the rows of a slice of test triangles, and
@@ -287,6 +310,7 @@ def main():
             "adjoint_points": out["adjoint_points"],
             "adjoint_fp64_point_share": out["adjoint_points_fp64"] / max(1, sum(out["adjoint_points"].values()))}
     line.update(fp)
+    line["nbody"] = nbody(vp, ctx)
     if not args.no_cpu_baseline:
         cb = cpu_baseline(w, wake, W, V)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

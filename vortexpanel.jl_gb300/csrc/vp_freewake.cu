@@ -248,10 +248,12 @@ extern "C" int vp_blob_velocities(vp_ctx* ctx, int precision, int nblob, const d
     std::vector<double> hb(blobs, blobs + 7 * size_t(nblob));
     std::vector<double> hx(X, X + 3 * size_t(npts));
     if ((r = dl.up(ctx, &db, hb)) || (r = dl.up(ctx, &dx, hx)) || (r = dl.alloc(ctx, &du, 3 * size_t(npts)))) return r;
+    vp_phase_begin(ctx, PH_WAKE);
     if (precision == VP_FP64)
         blob_kernel<double><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(nblob, db, npts, dx, du);
     else
         blob_kernel<float><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(nblob, db, npts, dx, du);
+    vp_phase_end(ctx);
     ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
     VP_CUDA(ctx, vp_d2h(ctx, U, du, sizeof(double) * 3 * npts));
@@ -292,10 +294,12 @@ extern "C" int vp_body_velocity(vp_ctx* ctx, int precision, int ntri, const doub
     int r;
     std::vector<double> hx(X, X + 3 * size_t(npts));
     if ((r = dl.up(ctx, &ds, hs)) || (r = dl.up(ctx, &dx, hx)) || (r = dl.alloc(ctx, &du, 3 * size_t(npts)))) return r;
+    vp_phase_begin(ctx, PH_WAKE);
     if (precision == VP_FP64)
         body_kernel<double><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(ntri, ds, kernel_far, npts, dx, du);
     else
         body_kernel<float><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(ntri, ds, kernel_far, npts, dx, du);
+    vp_phase_end(ctx);
     ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
     VP_CUDA(ctx, vp_d2h(ctx, U, du, sizeof(double) * 3 * npts));

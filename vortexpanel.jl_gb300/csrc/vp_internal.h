@@ -22,6 +22,7 @@ enum {
     PH_ADJ_FAR,     // adjoint far tier
     PH_ADJ_NEAR,    // adjoint non-far pairs, filaments, freestream
     PH_ADJ_SOLVE,   // transposed solve
+    PH_WAKE,        // free wake: blob sums, body velocity, explicit right hand side of particles
     PH_COUNT
 };
 

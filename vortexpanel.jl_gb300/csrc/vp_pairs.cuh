@@ -489,7 +489,7 @@ __device__ __forceinline__ void fold32(FwdAcc& acc) {
 }
 
 // evaluate one point (barycentric l on T, weight W) in FP64
-__device__ __forceinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double l0, double l1, double l2, double W) {
+__device__ __noinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double l0, double l1, double l2, double W) {
     const WarpSh& sh = *pc.sh;
     v3<double> psi = test_weights(pc.a->test_mode, l0, l1, l2);
     if (pc.kind == 0) {
@@ -528,7 +528,7 @@ __device__ __forceinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, dou
 }
 
 // evaluate one point in FP32 (triangle sources in VP_MIXED); false when it lies where FP32 cancels
-__device__ __forceinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float l0, float l1, float l2, float W) {
+__device__ __noinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float l0, float l1, float l2, float W) {
     if (pc.a->test_mode == 2) return false;  // the dual test's ties are decided in FP64
     const WarpSh& sh = *pc.sh;
     SrcKern<float> S;
@@ -648,7 +648,7 @@ __device__ __forceinline__ SrcKern<float> src32(const WarpSh& sh) {
 }
 
 // one point in FP64, adjoint: W nu(q) times s = w·m and its derivatives (source sheets), or the filament's
-__device__ __forceinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, double l0, double l1, double l2, double W) {
+__device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, double l0, double l1, double l2, double W) {
     const WarpSh& sh = *pc.sh;
     v3<double> psi = test_weights(pc.a->test_mode, l0, l1, l2);
     double Wn = W * (pc.nu[0] * psi.x + pc.nu[1] * psi.y + pc.nu[2] * psi.z);
@@ -682,7 +682,7 @@ __device__ __forceinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, dou
 }
 
 // one point in FP32 under the guard, adjoint; false when it must be evaluated in FP64
-__device__ __forceinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float l0, float l1, float l2, float W) {
+__device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float l0, float l1, float l2, float W) {
     if (pc.a->test_mode == 2) return false;
     const WarpSh& sh = *pc.sh;
     SrcKern<float> S = src32(sh);
@@ -739,7 +739,7 @@ __device__ __forceinline__ void tri_corners(const TriGeo& g, v3<double>* v) {
 // FP64 evaluation of the queued points, 32 at a time (all of them when `all`): rule point qi of the current piece
 // (corners b, fraction frac) or of buffered leaf ql
 template <class Acc>
-__device__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* b, double frac) {
+__device__ __noinline__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* b, double frac) {
     const RulePt* R = pc.a->rule[rid];
     const double areaT = pc.T->area;
     while (pc.nq64 >= 32 || (all && pc.nq64 > 0)) {
@@ -809,7 +809,7 @@ __device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, in
 
 // a piece carrying a whole tabulated rule: lanes stride over its points
 template <class Acc>
-__device__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, double frac) {
+__device__ __noinline__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, double frac) {
     const int n = pc.a->nrule[rid];
     float bf[10];
     for (int z = 0; z < 9; ++z) bf[z] = float(b[z]);
@@ -825,7 +825,7 @@ __device__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, doubl
 }
 
 template <class Acc>
-__device__ void flush_leaves(PairCtx& pc, Acc& acc) {
+__device__ __noinline__ void flush_leaves(PairCtx& pc, Acc& acc) {
     const int nl = pc.nleaf;
     if (nl == 0) return;
     __syncwarp();
@@ -946,7 +946,7 @@ __device__ __forceinline__ void bmix(double* o, const double* a, double sa, cons
 
 // near_pieces! (assemble.jl:131-142) as a depth-first walk of the quadtree of sub-triangles
 template <class Acc>
-__device__ void near_pieces(PairCtx& pc, Acc& acc, const SrcRef& src, const double* b0, double frac0, int depth) {
+__device__ __noinline__ void near_pieces(PairCtx& pc, Acc& acc, const SrcRef& src, const double* b0, double frac0, int depth) {
     int level = 0;
     unsigned path = 0;  // base-4 digits, most significant first
     const double ratio = pc.a->near_ratio;
@@ -991,7 +991,7 @@ __device__ void near_pieces(PairCtx& pc, Acc& acc, const SrcRef& src, const doub
 // vertex_pieces! (assemble.jl:102-116): the vertex rule toward corner k of the piece with corners p, b; tan: this
 // lane's tangent of b and frac (adjoint; null for a piece fixed in the test triangle)
 template <class Acc>
-__device__ void vertex_pieces(PairCtx& pc, Acc& acc, const v3<double>* p, int k, const double* b, double frac,
+__device__ __noinline__ void vertex_pieces(PairCtx& pc, Acc& acc, const v3<double>* p, int k, const double* b, double frac,
                               const double* tan) {
     int i = (k + 1) % 3, j = (k + 2) % 3;
     v3<double> u = p[i] - p[k], v = p[j] - p[k];
@@ -1070,7 +1070,7 @@ __device__ __forceinline__ bool on_edge_split(v3<double> q, v3<double> a, v3<dou
 
 // contact_rule / contact_pieces! (assemble.jl:199-238) for a triangle source S; returns false without contact
 template <class Acc>
-__device__ bool contact_rule(PairCtx& pc, Acc& acc, const TriGeo& S, const bool* shared) {
+__device__ __noinline__ bool contact_rule(PairCtx& pc, Acc& acc, const TriGeo& S, const bool* shared) {
     const TriGeo& T = *pc.T;
     const NearArgs& a = *pc.a;
     double tol = a.contact_rel * fmin(T.diam, S.diam);
