@@ -114,16 +114,17 @@ int vp_solve_system(vp_ctx* ctx, const vp_factor* F, const vp_system* sys, doubl
  * nrhs) out. VP_MIXED factors are refined with FP64 residuals of M'. */
 int vp_solve_transposed(vp_ctx* ctx, const vp_factor* F, int nrhs, const double* g, double* xi);
 
-/* Adjoint pair derivatives (no counterpart in the reference): for the inputs of vp_assemble, row values nu (nslot)
- * and column values mu (nslot + nwnode), the derivatives of F = nu' (A(x) mu - b(x)) with respect to the body nodes
- * (grad_x, nnode x 3), the wake nodes (grad_wx, nwnode x 3) and the angle of attack (dalpha), with sigma = -vinf·n
- * differentiated as such and dvinf = d vinf / d alpha. The quadrature of every pair is the assembly's. stats may be
- * NULL. For J(x, q) with M q = r: dJ/dx = dJ/dx|_q - dF/dx with nu = C xi, mu = [C q; W q], xi from
- * vp_solve_transposed with g = dJ/dq. */
+/* Adjoint pair derivatives (no counterpart in the reference): for the inputs of vp_assemble, nadj (1 or 2) vectors
+ * of row values nu (nslot x nadj, column-major) and column values mu (nslot + nwnode), the derivatives of
+ * F_k = nu_k' (A(x) mu - b(x)) with respect to the body nodes (grad_x, nnode x 3 per vector), the wake nodes
+ * (grad_wx, nwnode x 3 per vector) and the angle of attack (dalpha, nadj), with sigma = -vinf·n differentiated as such
+ * and dvinf = d vinf / d alpha. The quadrature of every pair is the assembly's; the vectors share one evaluation of
+ * every point. stats may be NULL. For J(x, q) with M q = r: dJ/dx = dJ/dx|_q - dF/dx with nu = C xi,
+ * mu = [C q; W q], xi from vp_solve_transposed with g = dJ/dq. */
 int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,
                const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil, const int* fil,
-               const double* nu, const double* mu, const double* dvinf, double* grad_x, double* grad_wx,
+               int nadj, const double* nu, const double* mu, const double* dvinf, double* grad_x, double* grad_wx,
                double* dalpha, vp_assembly_stats* stats);
 
 /* Instrumentation (no counterpart in the reference, which only times with @elapsed): device milliseconds per phase

@@ -75,6 +75,58 @@ __device__ __forceinline__ T adj_point_far(AdjSums<T>& acc, const SrcKern<T>& S,
     return sv;
 }
 
+// several adjoint vectors at once (their point weights Wn[k], k < nk): the kernel and its derivatives are evaluated
+// once, and each set of sums takes its own weight
+template <class T>
+__device__ __forceinline__ T adj_point_exact_multi(AdjSums<T>* acc, int nk, const T* Wn, const SrcKern<T>& S, T l0, T l1,
+                                                   T l2, v3<T> r0, v3<T> r1, v3<T> r2, v3<T> r, v3<T> m, int side,
+                                                   T plane_tol, v3<T>& gx) {
+    v3<T> g0, g1, g2;
+    ExactShape<T> sh;
+    T sv = sv_exact_vjp(S, r0, r1, r2, r, m, side, plane_tol, g0, g1, g2, sh);
+    const T i4pi = T(1) / (T(4) * vp_pi<T>());
+    const v3<T> w = (sh.L[0] * S.nu[0] + sh.L[1] * S.nu[1] + sh.L[2] * S.nu[2] + sh.Om * S.n) * i4pi;
+    gx = g0 + g1 + g2;
+    for (int k = 0; k < nk; ++k) {
+        AdjSums<T>& a = acc[k];
+        const T wn = Wn[k];
+        a.Q += wn * w;
+        a.Xg[0] += (wn * l0) * gx;
+        a.Xg[1] += (wn * l1) * gx;
+        a.Xg[2] += (wn * l2) * gx;
+        a.Gr[0] += wn * g0;
+        a.Gr[1] += wn * g1;
+        a.Gr[2] += wn * g2;
+        for (int e = 0; e < 3; ++e) {
+            a.L[e] += wn * sh.L[e];
+            a.N[e] += wn * sh.dLdlen[e];
+        }
+        a.O += wn * sh.Om;
+    }
+    return sv;
+}
+
+template <class T>
+__device__ __forceinline__ T adj_point_far_multi(AdjSums<T>* acc, int nk, const T* Wn, const SrcKern<T>& S, T l0, T l1,
+                                                 T l2, v3<T> r, v3<T> m, v3<T>& gx) {
+    v3<T> gd[3];
+    T ga;
+    T sv = sv_far_vjp(S, r, m, gx, gd, ga);
+    const v3<T> w = sv_far(S, r);
+    for (int k = 0; k < nk; ++k) {
+        AdjSums<T>& a = acc[k];
+        const T wn = Wn[k];
+        a.Q += wn * w;
+        a.Xg[0] += (wn * l0) * gx;
+        a.Xg[1] += (wn * l1) * gx;
+        a.Xg[2] += (wn * l2) * gx;
+        a.Grf += wn * gx;
+        for (int b = 0; b < 3; ++b) a.Gd[b] += wn * gd[b];
+        a.A += wn * ga;
+    }
+    return sv;
+}
+
 // The sums a source collects over all its (test triangle, point) evaluations, with m = n_T x Gamma_S + sigma_S n_T the
 // pair's direction (Gamma_S = sum_b mu_b gamma_b the source sheet's vortex density): exact form Gr (ds/dr_a at fixed
 // shape), Lm_e = sum L_e m, Nm_e = sum dL_e/dlen_e (nu_e·m), Om = sum Omega m; multipole form Grf, Gd, A (as AdjSums);

@@ -10,8 +10,8 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
 int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
                     const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                     const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
-                    const int* fil, const double* nu, const double* mu, const double* dvinf, double* grad_x,
-                    double* grad_wx, double* dalpha, vp_assembly_stats* stats);
+                    const int* fil, int nadj, const double* nu, const double* mu, const double* dvinf,
+                    double* grad_x, double* grad_wx, double* dalpha, vp_assembly_stats* stats);
 
 int vp_fail(vp_ctx* ctx, int code, const std::string& msg) {
     if (ctx) ctx->err = msg;
@@ -146,12 +146,12 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
 int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,
                const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil, const int* fil,
-               const double* nu, const double* mu, const double* dvinf, double* grad_x, double* grad_wx,
+               int nadj, const double* nu, const double* mu, const double* dvinf, double* grad_x, double* grad_wx,
                double* dalpha, vp_assembly_stats* stats) {
     if (!ctx) return VP_ERR_ARG;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
     return vp_adjoint_impl(ctx, opts, nnode, x, ntri, tris, corner_slot, nslot, ntouch, touch_pairs, sigma, vinf,
-                           nwnode, wx, nwtri, wtris, nfil, fil, nu, mu, dvinf, grad_x, grad_wx, dalpha, stats);
+                           nwnode, wx, nwtri, wtris, nfil, fil, nadj, nu, mu, dvinf, grad_x, grad_wx, dalpha, stats);
 }
 
 int vp_system_shape(const vp_system* sys, int* nrows, int* ncols) {

@@ -581,26 +581,39 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, 
 // non-far pairs, tip filaments and freestream: one warp per test triangle
 
 
+// the adjoint vectors of one pass of the warp-cooperative kernel, each with its outputs
+struct AdjMulti {
+    AdjExtra x[ADJ_MAX];
+    int nadj;
+};
+
 // this lane's rule-geometry derivative (direction lane < 18) to the test triangle's nodes and the source's
-__device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjExtra& x, const TriGeo& T, const TriGeo* S, bool wake) {
+__device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjMulti& mx, const TriGeo& T, const TriGeo* S,
+                                           bool wake) {
     const int d = pc.lane;
-    if (d < 18 && pc.gdir != 0.0) {
-        if (d < 9)
-            atomicAdd(x.gx + 3 * T.node[d / 3] + d % 3, pc.gdir);
-        else if (S)
-            atomicAdd((wake ? x.gwx + 3 * S->slot[(d - 9) / 3] : x.gx + 3 * S->node[(d - 9) / 3]) + (d - 9) % 3, pc.gdir);
+    for (int k = 0; k < mx.nadj; ++k) {
+        const AdjExtra& x = mx.x[k];
+        if (d < 18 && pc.gdir[k] != 0.0) {
+            if (d < 9)
+                atomicAdd(x.gx + 3 * T.node[d / 3] + d % 3, pc.gdir[k]);
+            else if (S)
+                atomicAdd((wake ? x.gwx + 3 * S->slot[(d - 9) / 3] : x.gx + 3 * S->node[(d - 9) / 3]) + (d - 9) % 3,
+                          pc.gdir[k]);
+        }
+        pc.gdir[k] = 0;
     }
-    pc.gdir = 0;
 }
 
-// the pairs the lanes kernel left (self, touching, contact), the tip filaments and the freestream
-__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, AdjExtra x) {
+// the pairs the lanes kernel left (self, touching, contact), the tip filaments and the freestream, for up to ADJ_MAX
+// adjoint vectors at once: every point's kernel and derivatives are evaluated once, and each vector keeps its sums
+__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, AdjMulti mx) {
     __shared__ WarpSh shm[NEAR_WARPS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int idx = blockIdx.x * NEAR_WARPS + w;
     if (idx >= a.ntests) return;
     const int t = a.tests[idx];
     const TriGeo& T = a.tri[t];
+    const int K = mx.nadj;
     PairCtx pc;
     pc.a = &a;
     pc.T = &T;
@@ -609,17 +622,23 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
     pc.nleaf = 0;
     pc.nq64 = 0;
     pc.fp32 = 0;
+    pc.nadj = K;
     for (int k = 0; k < 3; ++k) {
-        pc.nu[k] = x.nu[T.slot[k]];
+        for (int j = 0; j < ADJ_MAX; ++j) pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+        pc.nu[k] = pc.nuk[0][k];
         pc.Xc[k] = ld3(T.x + 3 * k) - ld3(T.c);
         pc.Xcf[k] = mk3(float(pc.Xc[k].x), float(pc.Xc[k].y), float(pc.Xc[k].z));
     }
     pc.dep = 0;
-    pc.gdir = 0;
+    for (int j = 0; j < ADJ_MAX; ++j) pc.gdir[j] = 0;
     const v3<double> nT = ld3(T.n);
-    v3<double> Xg[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
-    v3<double> U = mk3(0.0, 0.0, 0.0);
-    double fs = 0, dal = 0;
+    v3<double> Xg[ADJ_MAX][3], U[ADJ_MAX];
+    double fs[ADJ_MAX], dal[ADJ_MAX];
+    for (int j = 0; j < ADJ_MAX; ++j) {
+        for (int k = 0; k < 3; ++k) Xg[j][k] = mk3(0.0, 0.0, 0.0);
+        U[j] = mk3(0.0, 0.0, 0.0);
+        fs[j] = dal[j] = 0;
+    }
     unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
     for (int set = 0; set < 2; ++set) {
@@ -630,7 +649,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
         for (long long e = e0; e < e1; ++e) {
             const int s = list[e];
             const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
-            const double* gp = (wake ? x.gam_w : x.gam_b) + 3 * size_t(s);
+            const double* gp = (wake ? mx.x[0].gam_w : mx.x[0].gam_b) + 3 * size_t(s);
             const v3<double> G = mk3(gp[0], gp[1], gp[2]);
             const double sig = wake ? 0.0 : S.sigma;
             pc.m = cross(nT, G) + sig * nT;
@@ -642,29 +661,31 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
             pc.nleaf = 0;
             pc.nq64 = 0;
             int tier = tri_pair(pc, acc, t, s, wake);
-            flush_gdir(pc, x, T, &S, wake);
+            flush_gdir(pc, mx, T, &S, wake);
             fold32(acc);
-            adj_warp_sum(acc.d);
-            const AdjSums<double>& d = acc.d;
-            for (int k = 0; k < 3; ++k) Xg[k] += d.Xg[k];
-            U += cross(G, d.Q) + sig * d.Q;
-            fs += dot(d.Q, pc.m);
-            // the source side: lane k adds field k
             v3<double> xS[3];
             tri_corners(S, xS);
-            SrcAdj<double> sa = src_of_pair(xS, d, pc.m, nT);
-            double f[NSA];
-            sa_flat(sa, f);
-            double* dst = x.SA[set] + size_t(s) * NSA;
-            double mine = 0, mine2 = 0;
+            for (int j = 0; j < K; ++j) {
+                adj_warp_sum(acc.d[j]);
+                const AdjSums<double>& d = acc.d[j];
+                for (int k = 0; k < 3; ++k) Xg[j][k] += d.Xg[k];
+                U[j] += cross(G, d.Q) + sig * d.Q;
+                fs[j] += dot(d.Q, pc.m);
+                // the source side: lane k adds field k
+                SrcAdj<double> sa = src_of_pair(xS, d, pc.m, nT);
+                double f[NSA];
+                sa_flat(sa, f);
+                double* dst = mx.x[j].SA[set] + size_t(s) * NSA;
+                double mine = 0, mine2 = 0;
 #pragma unroll
-            for (int k = 0; k < 32; ++k)
-                if (k == lane) mine = f[k];
+                for (int k = 0; k < 32; ++k)
+                    if (k == lane) mine = f[k];
 #pragma unroll
-            for (int k = 32; k < NSA; ++k)
-                if (k - 32 == lane) mine2 = f[k];
-            if (mine != 0.0) atomicAdd(dst + lane, mine);
-            if (lane < NSA - 32 && mine2 != 0.0) atomicAdd(dst + 32 + lane, mine2);
+                for (int k = 32; k < NSA; ++k)
+                    if (k - 32 == lane) mine2 = f[k];
+                if (mine != 0.0) atomicAdd(dst + lane, mine);
+                if (lane < NSA - 32 && mine2 != 0.0) atomicAdd(dst + 32 + lane, mine2);
+            }
             __syncwarp();
             P[tier] += 1;
             Q[tier] += pc.npts;
@@ -692,8 +713,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
         pc.n64 = 0;
         pc.side = 0;
         pc.fp32 = 0;
-        pc.mua = x.mu[a.nslot + ia];
-        pc.mub = x.mu[a.nslot + ib];
+        pc.mua = mx.x[0].mu[a.nslot + ia];
+        pc.mub = mx.x[0].mu[a.nslot + ib];
         const double L = vnorm(fb - fa);
         int tier;
         if (vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, L)) {
@@ -713,39 +734,42 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
                 flush_leaves(pc, acc);
             }
         }
-        flush_gdir(pc, x, T, nullptr, false);
-        adj_warp_sum(acc.d);
-        const AdjSums<double>& d = acc.d;
-        for (int k = 0; k < 3; ++k) Xg[k] += d.Xg[k];
-        U += d.Q;
-        fs += dot(d.Q, nT);
-        if (lane < 3) {
-            const double ga[3] = {d.Gr[0].x, d.Gr[0].y, d.Gr[0].z}, gb[3] = {d.Gr[1].x, d.Gr[1].y, d.Gr[1].z};
-            atomicAdd(x.gwx + 3 * ia + lane, -ga[lane]);
-            atomicAdd(x.gwx + 3 * ib + lane, -gb[lane]);
+        flush_gdir(pc, mx, T, nullptr, false);
+        for (int j = 0; j < K; ++j) {
+            adj_warp_sum(acc.d[j]);
+            const AdjSums<double>& d = acc.d[j];
+            for (int k = 0; k < 3; ++k) Xg[j][k] += d.Xg[k];
+            U[j] += d.Q;
+            fs[j] += dot(d.Q, nT);
+            if (lane < 3) {
+                const double ga[3] = {d.Gr[0].x, d.Gr[0].y, d.Gr[0].z}, gb[3] = {d.Gr[1].x, d.Gr[1].y, d.Gr[1].z};
+                atomicAdd(mx.x[j].gwx + 3 * ia + lane, -ga[lane]);
+                atomicAdd(mx.x[j].gwx + 3 * ib + lane, -gb[lane]);
+            }
         }
         __syncwarp();
         P[tier] += 1;
         Q[tier] += pc.npts;
         Q64 += pc.n64;
     }
-    // freestream (assemble.jl:422): (V·n_T) A_T sum_a nu_a ti_a
-    {
-        const double c = (pc.nu[0] * a.tint[0] + pc.nu[1] * a.tint[1] + pc.nu[2] * a.tint[2]) * T.area;
-        const v3<double> V = mk3(x.V[0], x.V[1], x.V[2]), dV = mk3(x.dV[0], x.dV[1], x.dV[2]);
-        U += c * V;
-        fs += c * dot(V, nT);
-        dal += c * dot(dV, nT);
-    }
-    const double v[NTA] = {Xg[0].x, Xg[0].y, Xg[0].z, Xg[1].x, Xg[1].y, Xg[1].z, Xg[2].x, Xg[2].y, Xg[2].z,
-                           U.x,     U.y,     U.z,     fs};
-    double mine = 0;
+    // freestream (assemble.jl:422): (V·n_T) A_T sum_a nu_a ti_a, and the test side of every vector
+    const v3<double> V = mk3(mx.x[0].V[0], mx.x[0].V[1], mx.x[0].V[2]);
+    const v3<double> dV = mk3(mx.x[0].dV[0], mx.x[0].dV[1], mx.x[0].dV[2]);
+    for (int j = 0; j < K; ++j) {
+        const double c = (pc.nuk[j][0] * a.tint[0] + pc.nuk[j][1] * a.tint[1] + pc.nuk[j][2] * a.tint[2]) * T.area;
+        U[j] += c * V;
+        fs[j] += c * dot(V, nT);
+        dal[j] += c * dot(dV, nT);
+        const double v[NTA] = {Xg[j][0].x, Xg[j][0].y, Xg[j][0].z, Xg[j][1].x, Xg[j][1].y, Xg[j][1].z,
+                               Xg[j][2].x, Xg[j][2].y, Xg[j][2].z, U[j].x,     U[j].y,     U[j].z,     fs[j]};
+        double mine = 0;
 #pragma unroll
-    for (int k = 0; k < NTA; ++k)
-        if (k == lane) mine = v[k];
-    if (lane < NTA && mine != 0.0) atomicAdd(x.TA + size_t(t) * NTA + lane, mine);
+        for (int k = 0; k < NTA; ++k)
+            if (k == lane) mine = v[k];
+        if (lane < NTA && mine != 0.0) atomicAdd(mx.x[j].TA + size_t(t) * NTA + lane, mine);
+        if (lane == 0) atomicAdd(mx.x[j].dal, dal[j]);
+    }
     if (lane == 0) {
-        atomicAdd(x.dal, dal);
         for (int k = 0; k < 6; ++k) {
             if (P[k]) atomicAdd(a.stats + k, P[k]);
             if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
@@ -877,11 +901,12 @@ int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const dou
 int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
                     const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                     const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
-                    const int* fil, const double* nu, const double* mu, const double* dvinf, double* grad_x,
+                    const int* fil, int nadj, const double* nu, const double* mu, const double* dvinf, double* grad_x,
                     double* grad_wx, double* dalpha, vp_assembly_stats* stats) {
     auto t0 = std::chrono::steady_clock::now();
     if (!nu || !mu || !dvinf || !grad_x || !dalpha || (nwnode > 0 && !grad_wx))
         return vp_fail(ctx, VP_ERR_ARG, "null argument");
+    if (nadj < 1 || nadj > ADJ_MAX) return vp_fail(ctx, VP_ERR_ARG, "nadj must be 1 or 2");
     const PairInput in{o,     nnode, x,     ntri, tris,  corner_slot, nslot, ntouch, touch_pairs,
                        sigma, vinf,  nwnode, wx,  nwtri, wtris,       nfil,  fil};
     PairSetup ps;
@@ -890,9 +915,9 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     DevList& dl = ps.dl;
     const int ncols = ps.ncols;
     vp_phase_begin(ctx, PH_ADJOINT);
-    double *d_nu, *d_mu, *d_SA0, *d_SA1, *d_TA, *d_gx, *d_gwx, *d_dal, *d_gamb, *d_gamw;
-    unsigned long long* d_stats;
-    std::vector<double> hnu(nu, nu + nslot), hmu(mu, mu + ncols);
+    double *d_mu, *d_gamb, *d_gamw;
+    unsigned long long *d_stats, *d_stats_x;
+    std::vector<double> hmu(mu, mu + ncols);
     std::vector<double> gamb(size_t(3) * ntri), gamw(size_t(3) * std::max(nwtri, 1), 0.0);
     for (int s = 0; s < ntri; ++s)
         for (int k = 0; k < 3; ++k) {
@@ -906,25 +931,53 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
             for (int b = 0; b < 3; ++b) v += mu[nslot + ps.wg[s].slot[b]] * ps.wg[s].gam[3 * b + k];
             gamw[3 * size_t(s) + k] = v;
         }
-    if ((r = dl.up(ctx, &d_nu, hnu)) || (r = dl.up(ctx, &d_mu, hmu)) || (r = dl.up(ctx, &d_gamb, gamb)) ||
-        (r = dl.up(ctx, &d_gamw, gamw)) || (r = dl.alloc(ctx, &d_SA0, size_t(NSA) * ntri)) ||
-        (r = dl.alloc(ctx, &d_SA1, size_t(NSA) * std::max(nwtri, 1))) || (r = dl.alloc(ctx, &d_TA, size_t(NTA) * ntri)) ||
-        (r = dl.alloc(ctx, &d_gx, size_t(3) * nnode)) || (r = dl.alloc(ctx, &d_gwx, size_t(3) * std::max(nwnode, 1))) ||
-        (r = dl.alloc(ctx, &d_dal, 1)) || (r = dl.alloc(ctx, &d_stats, 13)))
+    if ((r = dl.up(ctx, &d_mu, hmu)) || (r = dl.up(ctx, &d_gamb, gamb)) || (r = dl.up(ctx, &d_gamw, gamw)) ||
+        (r = dl.alloc(ctx, &d_stats, 13)) || (r = dl.alloc(ctx, &d_stats_x, 13)))
         return r;
-    VP_CUDA(ctx, cudaMemsetAsync(d_SA0, 0, sizeof(double) * NSA * ntri, ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(d_SA1, 0, sizeof(double) * NSA * std::max(nwtri, 1), ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(d_TA, 0, sizeof(double) * NTA * ntri, ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(d_gx, 0, sizeof(double) * 3 * nnode, ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(d_gwx, 0, sizeof(double) * 3 * std::max(nwnode, 1), ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(d_dal, 0, sizeof(double), ctx->stream));
     VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(d_stats_x, 0, sizeof(unsigned long long) * 13, ctx->stream));
+    // per adjoint vector: its values and outputs
+    AdjMulti mx{};
+    mx.nadj = nadj;
+    for (int k = 0; k < nadj; ++k) {
+        AdjExtra& ex = mx.x[k];
+        double *d_nu, *d_SA0, *d_SA1, *d_TA, *d_gx, *d_gwx, *d_dal;
+        std::vector<double> hnu(nu + size_t(k) * nslot, nu + size_t(k + 1) * nslot);
+        if ((r = dl.up(ctx, &d_nu, hnu)) || (r = dl.alloc(ctx, &d_SA0, size_t(NSA) * ntri)) ||
+            (r = dl.alloc(ctx, &d_SA1, size_t(NSA) * std::max(nwtri, 1))) ||
+            (r = dl.alloc(ctx, &d_TA, size_t(NTA) * ntri)) || (r = dl.alloc(ctx, &d_gx, size_t(3) * nnode)) ||
+            (r = dl.alloc(ctx, &d_gwx, size_t(3) * std::max(nwnode, 1))) || (r = dl.alloc(ctx, &d_dal, 1)))
+            return r;
+        VP_CUDA(ctx, cudaMemsetAsync(d_SA0, 0, sizeof(double) * NSA * ntri, ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_SA1, 0, sizeof(double) * NSA * std::max(nwtri, 1), ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_TA, 0, sizeof(double) * NTA * ntri, ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_gx, 0, sizeof(double) * 3 * nnode, ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_gwx, 0, sizeof(double) * 3 * std::max(nwnode, 1), ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_dal, 0, sizeof(double), ctx->stream));
+        ex.nu = d_nu;
+        ex.mu = d_mu;
+        ex.gam_b = d_gamb;
+        ex.gam_w = d_gamw;
+        for (int z = 0; z < 3; ++z) {
+            ex.V[z] = vinf[z];
+            ex.dV[z] = dvinf[z];
+        }
+        ex.SA[0] = d_SA0;
+        ex.SA[1] = d_SA1;
+        ex.TA = d_TA;
+        ex.gx = d_gx;
+        ex.gwx = d_gwx;
+        ex.dal = d_dal;
+    }
     vp_phase_end(ctx);
-    // far tier
-    r = ps.mixed ? run_adj_far<float, 8>(ctx, ps, in, d_nu, mu, d_SA0, d_SA1, d_TA, dl)
-                 : run_adj_far<double, 4>(ctx, ps, in, d_nu, mu, d_SA0, d_SA1, d_TA, dl);
-    if (r) return r;
-    // non-far pairs, filaments, freestream
+    // far tier, one launch per adjoint vector
+    for (int k = 0; k < nadj; ++k) {
+        const AdjExtra& ex = mx.x[k];
+        r = ps.mixed ? run_adj_far<float, 8>(ctx, ps, in, ex.nu, mu, ex.SA[0], ex.SA[1], ex.TA, dl)
+                     : run_adj_far<double, 4>(ctx, ps, in, ex.nu, mu, ex.SA[0], ex.SA[1], ex.TA, dl);
+        if (r) return r;
+    }
+    // non-far pairs: the near tier one pair per lane (a launch per adjoint vector), then the rest with all vectors
     {
         std::vector<int> all(ntri);
         std::iota(all.begin(), all.end(), 0);
@@ -933,22 +986,6 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         NearArgs na = near_args(ps, in);
         na.tests = d_tests;
         na.ntests = ntri;
-        na.stats = d_stats;
-        AdjExtra ex{};
-        ex.nu = d_nu;
-        ex.mu = d_mu;
-        ex.gam_b = d_gamb;
-        ex.gam_w = d_gamw;
-        for (int k = 0; k < 3; ++k) {
-            ex.V[k] = vinf[k];
-            ex.dV[k] = dvinf[k];
-        }
-        ex.SA[0] = d_SA0;
-        ex.SA[1] = d_SA1;
-        ex.TA = d_TA;
-        ex.gx = d_gx;
-        ex.gwx = d_gwx;
-        ex.dal = d_dal;
         int *d_rest, *d_wrest, *d_rcnt;
         if ((r = dl.alloc(ctx, &d_rest, size_t(std::max(ps.nfptr[ntri], 1LL)))) ||
             (r = dl.alloc(ctx, &d_wrest, size_t(std::max(ps.wfptr[ntri], 1LL)))) ||
@@ -961,32 +998,37 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         VP_CUDA(ctx, cudaFuncSetAttribute(adj_lanes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         const int nb = (ntri + NEAR_WARPS - 1) / NEAR_WARPS;
         vp_phase_begin(ctx, PH_ADJ_NEAR);
-        adj_lanes_kernel<<<nb, 32 * NEAR_WARPS, smem, ctx->stream>>>(na, ex);
-        adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, ex);
+        for (int k = 0; k < nadj; ++k) {
+            na.stats = k == 0 ? d_stats : d_stats_x;  // the pair counts once
+            adj_lanes_kernel<<<nb, 32 * NEAR_WARPS, smem, ctx->stream>>>(na, mx.x[k]);
+        }
+        na.stats = d_stats;
+        adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
         vp_phase_end(ctx);
-        ctx->launches += 2;
+        ctx->launches += nadj + 1;
         VP_CUDA(ctx, cudaGetLastError());
     }
     vp_phase_begin(ctx, PH_ADJOINT);
-    // node derivatives
-    {
+    // node derivatives, per adjoint vector
+    for (int k = 0; k < nadj; ++k) {
+        const AdjExtra& ex = mx.x[k];
         AdjFinish f{};
         f.tri = ps.d_tg;
         f.wtri = ps.d_wg;
         f.ntri = ntri;
         f.nwtri = nwtri;
         f.nslot = nslot;
-        f.TA = d_TA;
-        f.SA[0] = d_SA0;
-        f.SA[1] = d_SA1;
+        f.TA = ex.TA;
+        f.SA[0] = ex.SA[0];
+        f.SA[1] = ex.SA[1];
         f.mu = d_mu;
-        for (int k = 0; k < 3; ++k) {
-            f.V[k] = vinf[k];
-            f.dV[k] = dvinf[k];
+        for (int z = 0; z < 3; ++z) {
+            f.V[z] = vinf[z];
+            f.dV[z] = dvinf[z];
         }
-        f.gx = d_gx;
-        f.gwx = d_gwx;
-        f.dal = d_dal;
+        f.gx = ex.gx;
+        f.gwx = ex.gwx;
+        f.dal = ex.dal;
         const int n = ntri + nwtri;
         adj_finish_kernel<<<(n + 127) / 128, 128, 0, ctx->stream>>>(f);
         ctx->launches++;
@@ -994,9 +1036,13 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     }
     vp_phase_end(ctx);
     unsigned long long hs[13];
-    VP_CUDA(ctx, vp_d2h(ctx, grad_x, d_gx, sizeof(double) * 3 * nnode));
-    if (nwnode > 0) VP_CUDA(ctx, vp_d2h(ctx, grad_wx, d_gwx, sizeof(double) * 3 * nwnode));
-    VP_CUDA(ctx, vp_d2h(ctx, dalpha, d_dal, sizeof(double)));
+    for (int k = 0; k < nadj; ++k) {
+        const AdjExtra& ex = mx.x[k];
+        VP_CUDA(ctx, vp_d2h(ctx, grad_x + size_t(k) * 3 * nnode, ex.gx, sizeof(double) * 3 * nnode));
+        if (nwnode > 0)
+            VP_CUDA(ctx, vp_d2h(ctx, grad_wx + size_t(k) * 3 * nwnode, ex.gwx, sizeof(double) * 3 * nwnode));
+        VP_CUDA(ctx, vp_d2h(ctx, dalpha + k, ex.dal, sizeof(double)));
+    }
     VP_CUDA(ctx, vp_d2h(ctx, hs, d_stats, sizeof(hs)));
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("adjoint kernels: ") + cudaGetErrorString(e));

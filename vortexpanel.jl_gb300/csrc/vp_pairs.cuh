@@ -460,8 +460,11 @@ struct PairCtx {
     int nq64;       // queued FP64 points (uniform)
     long long npts; // points of this pair (uniform)
     long long n64;  // points of this pair evaluated in FP64 (uniform)
-    // adjoint: the test function weights nu_a at T's corners, the pair's direction m, a filament's end values
+    // adjoint: the test function weights nu_a at T's corners (nadj adjoint vectors, nu = the first), the pair's
+    // direction m, a filament's end values
+    int nadj;
     double nu[3];
+    double nuk[2][3];
     v3<double> m;
     v3<float> mf;
     double mua, mub;
@@ -473,7 +476,7 @@ struct PairCtx {
     double pfrac;
     double binv[9];
     double tb[10];
-    double gdir;
+    double gdir[2];
     v3<double> Xc[3];
     v3<float> Xcf[3];
 };
@@ -563,13 +566,15 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float 
 }
 
 // ---- adjoint accumulation of a pair (warp-cooperative path) --------------------------------------------------------
+constexpr int ADJ_MAX = 2;  // adjoint vectors of one pass
+
 struct AdjAcc {
-    AdjSums<double> d;  // FP64 sums
-    AdjSums<float> f;   // FP32 partial sums, folded into d every few points
+    AdjSums<double> d[ADJ_MAX];  // FP64 sums, per adjoint vector
+    AdjSums<float> f[ADJ_MAX];   // FP32 partial sums, folded into d every few points
     int nf;
     // the current dependent piece: sum W beta_j dphi/dl_k (Bb, 3 x 3) and sum W phi (Fb), phi = nu(l) s
-    double Bb[9], Fb;
-    float Bbf[9], Fbf;
+    double Bb[ADJ_MAX][9], Fb[ADJ_MAX];
+    float Bbf[ADJ_MAX][9], Fbf[ADJ_MAX];
 };
 
 template <class A, class B>
@@ -589,22 +594,24 @@ __device__ __forceinline__ void adj_add(AdjSums<A>& d, const AdjSums<B>& f) {
 }
 
 __device__ __forceinline__ void fold32(AdjAcc& acc) {
-    adj_add(acc.d, acc.f);
-    adj_zero(acc.f);
-    for (int k = 0; k < 9; ++k) {
-        acc.Bb[k] += double(acc.Bbf[k]);
-        acc.Bbf[k] = 0.f;
+    for (int j = 0; j < ADJ_MAX; ++j) {
+        adj_add(acc.d[j], acc.f[j]);
+        adj_zero(acc.f[j]);
+        for (int k = 0; k < 9; ++k) {
+            acc.Bb[j][k] += double(acc.Bbf[j][k]);
+            acc.Bbf[j][k] = 0.f;
+        }
+        acc.Fb[j] += double(acc.Fbf[j]);
+        acc.Fbf[j] = 0.f;
     }
-    acc.Fb += double(acc.Fbf);
-    acc.Fbf = 0.f;
     acc.nf = 0;
 }
 
 // the rule-geometry sums of one point of a dependent piece: weight W, barycentrics l, value s = w·m, ds/dx
 template <class T>
-__device__ __forceinline__ void rule_point(const PairCtx& pc, T* Bb, T& Fb, T W, T l0, T l1, T l2, T sv, v3<T> gx,
-                                           const v3<T>* Xc) {
-    const T n0 = T(pc.nu[0]), n1 = T(pc.nu[1]), n2 = T(pc.nu[2]);
+__device__ __forceinline__ void rule_point(const PairCtx& pc, const double* nu, T* Bb, T& Fb, T W, T l0, T l1, T l2,
+                                           T sv, v3<T> gx, const v3<T>* Xc) {
+    const T n0 = T(nu[0]), n1 = T(nu[1]), n2 = T(nu[2]);
     const bool hat = pc.a->test_mode == 0;
     const T nul = hat ? n0 * l0 + n1 * l1 + n2 * l2 : (pc.a->test_mode == 1 ? n0 + n1 + n2 : T(0));
     T dphi[3];
@@ -651,34 +658,39 @@ __device__ __forceinline__ SrcKern<float> src32(const WarpSh& sh) {
 __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, double l0, double l1, double l2, double W) {
     const WarpSh& sh = *pc.sh;
     v3<double> psi = test_weights(pc.a->test_mode, l0, l1, l2);
-    double Wn = W * (pc.nu[0] * psi.x + pc.nu[1] * psi.y + pc.nu[2] * psi.z);
+    double Wn[ADJ_MAX];
+    for (int k = 0; k < ADJ_MAX; ++k) Wn[k] = W * (pc.nuk[k][0] * psi.x + pc.nuk[k][1] * psi.y + pc.nuk[k][2] * psi.z);
     v3<double> ra = l0 * ld3(sh.E + 0) + l1 * ld3(sh.E + 9) + l2 * ld3(sh.E + 18);
     v3<double> rb = l0 * ld3(sh.E + 3) + l1 * ld3(sh.E + 12) + l2 * ld3(sh.E + 21);
+    v3<double> gx;
+    double sv;
     if (pc.kind == 0) {
         v3<double> rc = l0 * ld3(sh.E + 6) + l1 * ld3(sh.E + 15) + l2 * ld3(sh.E + 24);
         v3<double> r = l0 * ld3(sh.D) + l1 * ld3(sh.D + 3) + l2 * ld3(sh.D + 6);
         SrcKern<double> S = src64(sh);
         double fd = pc.a->kernel_far * S.diam;
-        v3<double> gx;
-        double sv;
         if (dot(r, r) > fd * fd)
-            sv = adj_point_far(acc.d, S, Wn, l0, l1, l2, r, pc.m, &gx);
+            sv = adj_point_far_multi(acc.d, pc.nadj, Wn, S, l0, l1, l2, r, pc.m, gx);
         else
-            sv = adj_point_exact(acc.d, S, Wn, l0, l1, l2, ra, rb, rc, r, pc.m, pc.side, 1e-12, &gx);
-        if (pc.dep) rule_point(pc, acc.Bb, acc.Fb, W, l0, l1, l2, sv, gx, pc.Xc);
+            sv = adj_point_exact_multi(acc.d, pc.nadj, Wn, S, l0, l1, l2, ra, rb, rc, r, pc.m, pc.side, 1e-12, gx);
     } else {
         v3<double> n = ld3(pc.T->n), va, vb, ga, gb;
         segment_velocity(ra, rb, va, vb);
         seg_vjp(ra, rb, n, pc.mua, pc.mub, ga, gb);
-        acc.d.Q += Wn * (pc.mua * va + pc.mub * vb);
-        v3<double> gx = ga + gb;
-        acc.d.Xg[0] += (Wn * l0) * gx;
-        acc.d.Xg[1] += (Wn * l1) * gx;
-        acc.d.Xg[2] += (Wn * l2) * gx;
-        acc.d.Gr[0] += Wn * ga;
-        acc.d.Gr[1] += Wn * gb;
-        if (pc.dep) rule_point(pc, acc.Bb, acc.Fb, W, l0, l1, l2, pc.mua * dot(va, n) + pc.mub * dot(vb, n), gx, pc.Xc);
+        gx = ga + gb;
+        sv = pc.mua * dot(va, n) + pc.mub * dot(vb, n);
+        for (int k = 0; k < pc.nadj; ++k) {
+            AdjSums<double>& d = acc.d[k];
+            d.Q += Wn[k] * (pc.mua * va + pc.mub * vb);
+            d.Xg[0] += (Wn[k] * l0) * gx;
+            d.Xg[1] += (Wn[k] * l1) * gx;
+            d.Xg[2] += (Wn[k] * l2) * gx;
+            d.Gr[0] += Wn[k] * ga;
+            d.Gr[1] += Wn[k] * gb;
+        }
     }
+    if (pc.dep)
+        for (int k = 0; k < pc.nadj; ++k) rule_point(pc, pc.nuk[k], acc.Bb[k], acc.Fb[k], W, l0, l1, l2, sv, gx, pc.Xc);
 }
 
 // one point in FP32 under the guard, adjoint; false when it must be evaluated in FP64
@@ -689,12 +701,14 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
     v3<float> r = l0 * mk3(sh.D32[0], sh.D32[1], sh.D32[2]) + l1 * mk3(sh.D32[3], sh.D32[4], sh.D32[5]) +
                   l2 * mk3(sh.D32[6], sh.D32[7], sh.D32[8]);
     v3<float> psi = pc.a->test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);
-    float Wn = W * (float(pc.nu[0]) * psi.x + float(pc.nu[1]) * psi.y + float(pc.nu[2]) * psi.z);
+    float Wn[ADJ_MAX];
+    for (int k = 0; k < ADJ_MAX; ++k)
+        Wn[k] = W * (float(pc.nuk[k][0]) * psi.x + float(pc.nuk[k][1]) * psi.y + float(pc.nuk[k][2]) * psi.z);
     float fd = float(pc.a->kernel_far) * S.diam;
     v3<float> gx;
     float sv;
     if (dot(r, r) > fd * fd) {
-        sv = adj_point_far(acc.f, S, Wn, l0, l1, l2, r, pc.mf, &gx);
+        sv = adj_point_far_multi(acc.f, pc.nadj, Wn, S, l0, l1, l2, r, pc.mf, gx);
     } else {
         const float* E = sh.E32;
         v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
@@ -703,9 +717,12 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
         if (!fp32_guard_ok(S, ra, rb, rc, pc.side, Fp32Guard{ADJ_GUARD})) return false;
         // the self pair's points lie in the source's plane up to FP32 rounding: its in-plane branch (solid angle
         // side 2 pi, as the forward's FP32 kernel takes it) must not depend on the sign of that rounding
-        sv = adj_point_exact(acc.f, S, Wn, l0, l1, l2, ra, rb, rc, r, pc.mf, pc.side, pc.side ? 1e-4f : 1e-12f, &gx);
+        sv = adj_point_exact_multi(acc.f, pc.nadj, Wn, S, l0, l1, l2, ra, rb, rc, r, pc.mf, pc.side,
+                                   pc.side ? 1e-4f : 1e-12f, gx);
     }
-    if (pc.dep) rule_point(pc, acc.Bbf, acc.Fbf, W, l0, l1, l2, sv, gx, pc.Xcf);
+    if (pc.dep)
+        for (int k = 0; k < pc.nadj; ++k)
+            rule_point(pc, pc.nuk[k], acc.Bbf[k], acc.Fbf[k], W, l0, l1, l2, sv, gx, pc.Xcf);
     if (++acc.nf == 16) fold32(acc);
     return true;
 }
@@ -898,14 +915,16 @@ __device__ void piece_end(PairCtx& pc, AdjAcc& acc) {
     if (!pc.dep) return;
     if (pc.nleaf) flush_leaves(pc, acc);
     fold32(acc);
-    double v = 0;
-    for (int k = 0; k < 9; ++k) {
-        v += wsum_d(acc.Bb[k]) * pc.tb[k];
-        acc.Bb[k] = 0;
+    for (int j = 0; j < pc.nadj; ++j) {
+        double v = 0;
+        for (int k = 0; k < 9; ++k) {
+            v += wsum_d(acc.Bb[j][k]) * pc.tb[k];
+            acc.Bb[j][k] = 0;
+        }
+        v += wsum_d(acc.Fb[j]) * pc.tb[9] / pc.pfrac;
+        acc.Fb[j] = 0;
+        if (pc.lane < 18) pc.gdir[j] += v;
     }
-    v += wsum_d(acc.Fb) * pc.tb[9] / pc.pfrac;
-    acc.Fb = 0;
-    if (pc.lane < 18) pc.gdir += v;
     pc.dep = 0;
 }
 

@@ -57,7 +57,7 @@ SIGNATURES = [
     ("vp_solve_transposed", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, D, D]),
     ("vp_adjoint", ctypes.c_int,
      [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
-      ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I, D, D, D, D, D, D,
+      ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I, ctypes.c_int, D, D, D, D, D, D,
       ctypes.POINTER(vp_assembly_stats)]),
     ("vp_blob_velocities", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, ctypes.c_int, D, D]),
     ("vp_body_velocity", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, D, D, ctypes.c_double,

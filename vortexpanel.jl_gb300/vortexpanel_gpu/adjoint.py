@@ -42,7 +42,8 @@ def solve_transposed(F, g):
 
 
 def pair_derivatives(g, dm, sigma, V, dV, nu, mu, opts: AssemblyOptions = None, wake=None, ctx=None):
-    """d/dx, d/dwx and d/dalpha of nu' (A(x) mu - b(x)) (vp_adjoint); returns (grad_x, grad_wx, dalpha, stats)"""
+    """d/dx, d/dwx and d/dalpha of nu' (A(x) mu - b(x)) (vp_adjoint) for one adjoint vector nu (nslot) or two
+    (nslot x 2, one pass); returns (grad_x, grad_wx, dalpha, stats), with a leading axis of 2 for two vectors"""
     opts = opts or AssemblyOptions()
     ctx = ctx or default_context()
     o = opts.c_struct()
@@ -63,18 +64,27 @@ def pair_derivatives(g, dm, sigma, V, dV, nu, mu, opts: AssemblyOptions = None, 
         wx = wt = wf = None
         pwx, pwt, pwf = None, None, None
         nw = nwt = nf = 0
-    nuu, pnu = _dp(nu)
+    nu = np.asarray(nu, float)
+    single = nu.ndim == 1
+    nv = nu.reshape(dm.nslot, -1)
+    k = nv.shape[1]
+    if k not in (1, 2):
+        raise ValueError("one or two adjoint vectors")
+    nuu, pnu = _dp(nv.T.copy().ravel())
     muu, pmu = _dp(mu)
-    if nuu.shape != (dm.nslot,) or muu.shape != (dm.nslot + nw,):
-        raise ValueError("nu must have one value per slot and mu one per column")
-    gx = np.zeros((g.nnode, 3))
-    gw = np.zeros((max(nw, 1), 3))
-    dal = ctypes.c_double()
+    if muu.shape != (dm.nslot + nw,):
+        raise ValueError("mu must have one value per column")
+    gx = np.zeros((k, g.nnode, 3))
+    gw = np.zeros((k, max(nw, 1), 3))
+    dal = np.zeros(k)
     st = _lib.vp_assembly_stats()
     check(ctx.h, load().vp_adjoint(ctx.h, ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(tp), ptp, ps, pV,
-                                   nw, pwx, nwt, pwt, nf, pwf, pnu, pmu, pdV, gx.ctypes.data_as(D),
-                                   gw.ctypes.data_as(D), ctypes.byref(dal), ctypes.byref(st)))
-    return gx, gw[:nw], dal.value, st
+                                   nw, pwx, nwt, pwt, nf, pwf, k, pnu, pmu, pdV, gx.ctypes.data_as(D),
+                                   gw.ctypes.data_as(D), dal.ctypes.data_as(D), ctypes.byref(st)))
+    gw = gw[:, :nw]
+    if single:
+        return gx[0], gw[0], float(dal[0]), st
+    return gx, gw, dal, st
 
 
 # ---- objectives with their explicit derivatives ------------------------------------------------------------------------
@@ -233,16 +243,16 @@ def wing_gradients(w, wake, W, alpha, precision="mixed", opts=None, ctx=None, ti
     xi = solve_transposed(F, np.stack([dm.C.T @ dCL_dmu, dm.K.T @ dCDi_dmuw], axis=1))
     del F
     out = dict(CL=CL, CDi=CDi, q=q, stats=stats, cond=s["cond"])
+    nu = np.stack([dm.C @ xi[:, 0], dm.C @ xi[:, 1]], axis=1)
+    fx, fw, fa, st = pair_derivatives(g, dm, sig, V, dV, nu, mu_cols, opts=opts, wake=wake, ctx=ctx)
+    out["adjoint_points"] = dict(zip(("self", "edge", "vertex", "contact", "near", "far"), list(st.points)))
+    out["adjoint_points_fp64"] = st.points_fp64
     for name, gx, al, k in (("CL", gCL, aCL, 0), ("CDi", gCDi, aCDi, 1)):
-        nu = dm.C @ xi[:, k]
-        fx, fw, fa, st = pair_derivatives(g, dm, sig, V, dV, nu, mu_cols, opts=opts, wake=wake, ctx=ctx)
-        out["adjoint_points"] = dict(zip(("self", "edge", "vertex", "contact", "near", "far"), list(st.points)))
-        out["adjoint_points_fp64"] = st.points_fp64
-        grad = gx - fx
-        if wake is not None and len(fw):
-            np.add.at(grad, dm.wake_te.node[wake.te], -fw)
+        grad = gx - fx[k]
+        if wake is not None and fw.shape[1]:
+            np.add.at(grad, dm.wake_te.node[wake.te], -fw[k])
         out["d" + name + "_dx"] = grad
-        out["d" + name + "_dalpha"] = al - fa
+        out["d" + name + "_dalpha"] = al - fa[k]
     if timings is not None:
         timings["forward"] = t1 - t0
         timings["adjoint"] = time.perf_counter() - t1
