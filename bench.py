@@ -29,9 +29,11 @@ sys.path.insert(0, os.path.join(ROOT, "vortexpanel.jl_gb300"))
 
 METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|<1e-6"
 # algorithmic flops per quadrature point: forward (kernel evaluation ~230 + contraction into the hat block 18) and
-# adjoint (value and reverse-mode derivatives of the kernel ~620 + the sums of the test and source sides ~110)
+# adjoint (value and reverse-mode derivatives of the kernel ~620, once per point, + the sums of the test and source
+# sides ~110 per adjoint vector; the CL and CDi vectors share a pass of the non-far kernels, the far tier runs each)
 FLOP_FWD_POINT = 248
-FLOP_ADJ_POINT = 730
+FLOP_ADJ_EVAL = 620
+FLOP_ADJ_SUMS = 110
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
 SIZES = {"wing25k": (112, 56), "medium": (56, 28), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
@@ -287,9 +289,14 @@ def main():
     elif dom == "near":
         roof = {"kernel": "near_kernel_lanes + near_kernel_rest", "bound": "fp32", "flops": nonfar(pts) * FLOP_FWD_POINT}
     elif dom == "adj_far":
-        roof = {"kernel": "adj_far_kernel<float,8>", "bound": "fp32", "flops": 2 * apts["far"] * FLOP_ADJ_POINT}
+        roof = {"kernel": "adj_far_kernel<float,8> (x2)", "bound": "fp32",
+                "flops": 2 * apts["far"] * (FLOP_ADJ_EVAL + FLOP_ADJ_SUMS)}
     elif dom == "adj_near":
-        roof = {"kernel": "adj_near_kernel", "bound": "fp32", "flops": 2 * nonfar(apts) * FLOP_ADJ_POINT}
+        # the near tier runs once per vector (adj_lanes_kernel x2), the touching and contact tiers once for both
+        near_pts = apts["near"]
+        roof = {"kernel": "adj_lanes_kernel x2 + adj_near_kernel", "bound": "fp32",
+                "flops": 2 * near_pts * (FLOP_ADJ_EVAL + FLOP_ADJ_SUMS) +
+                (nonfar(apts) - near_pts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS)}
     else:
         n = w.dm.nq + 1
         roof = {"kernel": "lu (cluster panels + sgemm)", "bound": "tensor", "flops": 2 / 3 * n ** 3}

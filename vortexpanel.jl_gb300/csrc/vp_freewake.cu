@@ -27,7 +27,9 @@ __device__ __forceinline__ v3<T> blob_vel(v3<T> r, v3<T> al, T d2core) {
     return s * cross(al, r);
 }
 
-// blobs: x (3), alpha (3), delta (1) per blob. FP32: every tile summed in FP32, the tiles in FP64.
+// blobs: x (3), alpha (3), delta (1) per blob. FP64: the plain sum. FP32 (float specialisation below): two points
+// per thread, the tile's blobs as float4 pairs (x, delta^2) and (alpha / 4 pi), 1/d^3 by a reciprocal square root,
+// every tile summed in FP32 and the tiles in FP64.
 template <class T>
 __global__ void __launch_bounds__(NB_THREADS) blob_kernel(int nblob, const double* __restrict__ blobs, int npts,
                                                         const double* __restrict__ X, double* __restrict__ U) {
@@ -47,7 +49,6 @@ __global__ void __launch_bounds__(NB_THREADS) blob_kernel(int nblob, const doubl
         }
         __syncthreads();
         v3<T> part = mk3(T(0), T(0), T(0));
-#pragma unroll 4
         for (int k = 0; k < nb; ++k) {
             v3<T> r = xt - mk3(sb[k][0], sb[k][1], sb[k][2]);
             part += blob_vel(r, mk3(sb[k][3], sb[k][4], sb[k][5]), sb[k][6]);
@@ -58,6 +59,74 @@ __global__ void __launch_bounds__(NB_THREADS) blob_kernel(int nblob, const doubl
         U[3 * i] = acc.x;
         U[3 * i + 1] = acc.y;
         U[3 * i + 2] = acc.z;
+    }
+}
+
+constexpr int NB_PTS = 2;  // points per thread of the FP32 kernel
+
+template <>
+__global__ void __launch_bounds__(NB_THREADS) blob_kernel<float>(int nblob, const double* __restrict__ blobs, int npts,
+                                                               const double* __restrict__ X, double* __restrict__ U) {
+    __shared__ float4 sx[NB_TILE], sa[NB_TILE];
+    const float i4pi = 1.f / (4.f * vp_pi<float>());
+    const int i0 = blockIdx.x * NB_THREADS * NB_PTS + threadIdx.x;
+    float px[NB_PTS], py[NB_PTS], pz[NB_PTS];
+    double ax[NB_PTS], ay[NB_PTS], az[NB_PTS];
+#pragma unroll
+    for (int j = 0; j < NB_PTS; ++j) {
+        const int i = i0 + j * NB_THREADS;
+        const bool v = i < npts;
+        px[j] = v ? float(X[3 * i]) : 0.f;
+        py[j] = v ? float(X[3 * i + 1]) : 0.f;
+        pz[j] = v ? float(X[3 * i + 2]) : 0.f;
+        ax[j] = ay[j] = az[j] = 0.0;
+    }
+    for (int b0 = 0; b0 < nblob; b0 += NB_TILE) {
+        const int nb = min(NB_TILE, nblob - b0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < NB_TILE; k += NB_THREADS) {
+            if (k < nb) {
+                const double* p = blobs + 7 * size_t(b0 + k);
+                sx[k] = make_float4(float(p[0]), float(p[1]), float(p[2]), float(p[6] * p[6]));
+                sa[k] = make_float4(float(p[3]) * i4pi, float(p[4]) * i4pi, float(p[5]) * i4pi, 0.f);
+            } else {  // padding: a blob of zero strength far away
+                sx[k] = make_float4(0.f, 0.f, 0.f, 1.f);
+                sa[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+        }
+        __syncthreads();
+        float ux[NB_PTS], uy[NB_PTS], uz[NB_PTS];
+#pragma unroll
+        for (int j = 0; j < NB_PTS; ++j) ux[j] = uy[j] = uz[j] = 0.f;
+#pragma unroll 8
+        for (int k = 0; k < NB_TILE; ++k) {
+            const float4 b = sx[k], al = sa[k];
+#pragma unroll
+            for (int j = 0; j < NB_PTS; ++j) {
+                const float rx = px[j] - b.x, ry = py[j] - b.y, rz = pz[j] - b.z;
+                const float d2 = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, b.w)));
+                const float inv = rsqrtf(d2);
+                const float s = inv * inv * inv;
+                ux[j] = fmaf(s, al.y * rz - al.z * ry, ux[j]);
+                uy[j] = fmaf(s, al.z * rx - al.x * rz, uy[j]);
+                uz[j] = fmaf(s, al.x * ry - al.y * rx, uz[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NB_PTS; ++j) {
+            ax[j] += double(ux[j]);
+            ay[j] += double(uy[j]);
+            az[j] += double(uz[j]);
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < NB_PTS; ++j) {
+        const int i = i0 + j * NB_THREADS;
+        if (i < npts) {
+            U[3 * i] = ax[j];
+            U[3 * i + 1] = ay[j];
+            U[3 * i + 2] = az[j];
+        }
     }
 }
 
@@ -252,7 +321,8 @@ extern "C" int vp_blob_velocities(vp_ctx* ctx, int precision, int nblob, const d
     if (precision == VP_FP64)
         blob_kernel<double><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(nblob, db, npts, dx, du);
     else
-        blob_kernel<float><<<points_grid(npts), NB_THREADS, 0, ctx->stream>>>(nblob, db, npts, dx, du);
+        blob_kernel<float><<<(npts + NB_THREADS * NB_PTS - 1) / (NB_THREADS * NB_PTS), NB_THREADS, 0, ctx->stream>>>(
+            nblob, db, npts, dx, du);
     vp_phase_end(ctx);
     ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
