@@ -212,7 +212,8 @@ def main():
     config = {"workload": f"wing AR{ASPECT:g} NACA0012 {NCHORD}x{NSPAN}/side ({w.g.ntri} tris, {w.dm.nq} unknowns), "
                           f"rigid wake {len(wake.tris)} tris + {len(wake.filaments)} filaments, alpha {ALPHA:g} deg",
               "ntri": w.g.ntri, "nq": w.dm.nq, "nwake_nodes": wake.nwake, "precision": "mixed",
-              "l2": "inputs larger than L2 (A is 1.6 GB FP64)", "parallelism": f"replicas x{world}"}
+              "l2": f"inputs larger than L2 (A is {8 * w.dm.nslot * (w.dm.nslot + wake.nwake) / 1e9:.2f} GB FP64)",
+              "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -287,14 +288,15 @@ def main():
     if dom == "far":
         roof = {"kernel": "far_kernel<float,8>", "bound": "fp32", "flops": pts["far"] * FLOP_FWD_POINT}
     elif dom == "near":
-        roof = {"kernel": "near_kernel_lanes + near_kernel_rest", "bound": "fp32", "flops": nonfar(pts) * FLOP_FWD_POINT}
+        roof = {"kernel": "near_kernel_lanes + near_kernel_pairs + near_kernel_rest", "bound": "fp32",
+                "flops": nonfar(pts) * FLOP_FWD_POINT}
     elif dom == "adj_far":
         roof = {"kernel": "adj_far_kernel<float,8> (x2)", "bound": "fp32",
                 "flops": 2 * apts["far"] * (FLOP_ADJ_EVAL + FLOP_ADJ_SUMS)}
     elif dom == "adj_near":
         # the near tier runs once per vector (adj_lanes_kernel x2), the touching and contact tiers once for both
         near_pts = apts["near"]
-        roof = {"kernel": "adj_lanes_kernel x2 + adj_near_kernel", "bound": "fp32",
+        roof = {"kernel": "adj_lanes_kernel x2 + adj_pairs_kernel + adj_near_kernel", "bound": "fp32",
                 "flops": 2 * near_pts * (FLOP_ADJ_EVAL + FLOP_ADJ_SUMS) +
                 (nonfar(apts) - near_pts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS)}
     else:

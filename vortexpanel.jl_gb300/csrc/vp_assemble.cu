@@ -478,7 +478,74 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a)
     }
 }
 
-// the self, touching and contact pairs (one warp per test triangle), the tip filaments and the freestream
+// the block of one pair: the per-lane sums reduced and contracted with n_T x gamma_b (9 values, row-major), and the
+// source part of the right hand side sigma_S (P_a . n_T) (3 values, subtracted when the pair is added)
+__device__ void pair_block_out(PairCtx& pc, FwdAcc& acc, const TriGeo& S, double* out, bool with_rhs) {
+    fold32(acc);
+    double P[9];
+    for (int a = 0; a < 3; ++a) {
+        P[3 * a + 0] = warp_sum(acc.P[a].x);
+        P[3 * a + 1] = warp_sum(acc.P[a].y);
+        P[3 * a + 2] = warp_sum(acc.P[a].z);
+    }
+    const TriGeo& T = *pc.T;
+    v3<double> nT = ld3(T.n);
+    if (pc.lane < 9) {
+        int ai = pc.lane / 3, bb = pc.lane % 3;
+        v3<double> m = cross(nT, ld3(S.gam + 3 * bb));
+        out[pc.lane] = P[3 * ai] * m.x + P[3 * ai + 1] * m.y + P[3 * ai + 2] * m.z;
+    } else if (pc.lane < 12) {
+        int ai = pc.lane - 9;
+        out[pc.lane] = with_rhs ? S.sigma * (P[3 * ai] * nT.x + P[3 * ai + 1] * nT.y + P[3 * ai + 2] * nT.z) : 0.0;
+    }
+    __syncwarp();
+}
+
+// the self, touching and contact pairs, one warp per pair: a persistent grid whose warps take the next pair of the
+// list from a counter, so that test triangles with many contact pairs (thin panels at a sharp trailing edge) do not
+// hold a launch; the blocks go to pair_out and near_kernel_rest adds them in the list's order
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_pairs(NearArgs a) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = 2 * a.ntri;
+    const long long total = a.rest_off[n];
+    PairCtx pc;
+    pc.a = &a;
+    pc.sh = &shm[w];
+    pc.lane = lane;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+    for (;;) {
+        const long long idx = next_rest_pair(a.next, lane);
+        if (idx >= total) break;
+        const int g = rest_entry(a.rest_off, n, idx);
+        const int t = g >> 1;
+        const bool wake = (g & 1) != 0;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
+        const int s = (wake ? a.wrest_src : a.rest_src)[e0 + (idx - a.rest_off[g])];
+        pc.T = &a.tri[t];
+        FwdAcc acc = {};
+        pc.kind = 0;
+        pc.npts = 0;
+        pc.n64 = 0;
+        pc.nleaf = 0;
+        pc.nq64 = 0;
+        const int tier = tri_pair(pc, acc, t, s, wake);
+        pair_block_out(pc, acc, wake ? a.wtri[s] : a.tri[s], a.pair_out + 12 * idx, !wake);
+        P[tier] += 1;
+        Q[tier] += pc.npts;
+        Q64 += pc.n64;
+    }
+    if (lane == 0) {
+        for (int k = 0; k < 6; ++k) {
+            if (P[k]) atomicAdd(a.stats + k, P[k]);
+            if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
+        }
+        if (Q64) atomicAdd(a.stats + 12, Q64);
+    }
+}
+
+// the blocks of the self, touching and contact pairs (from near_kernel_pairs, added in the order of the test
+// triangle's list), the tip filaments and the freestream: one warp per test triangle, a launch per colour
 __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) {
     __shared__ WarpSh shm[NEAR_WARPS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -503,19 +570,17 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) 
         const int n = a.rest_cnt[2 * t + set];
         const int* rest = wake ? a.wrest_src : a.rest_src;
         const int col0 = wake ? a.nslot : 0;
+        const double* blk = a.pair_out + 12 * a.rest_off[2 * t + set];
         for (int e = 0; e < n; ++e) {
-            const int s = rest[e0 + e];
-            FwdAcc acc = {};
-            pc.kind = 0;
-            pc.npts = 0;
-            pc.n64 = 0;
-            pc.nleaf = 0;
-            pc.nq64 = 0;
-            int tier = tri_pair(pc, acc, t, s, wake);
-            add_block(pc, acc, wake ? a.wtri[s] : a.tri[s], col0, rbt, !wake);
-            P[tier] += 1;
-            Q[tier] += pc.npts;
-            Q64 += pc.n64;
+            const TriGeo& S = wake ? a.wtri[rest[e0 + e]] : a.tri[rest[e0 + e]];
+            const double* pb = blk + 12 * e;
+            if (lane < 9) {
+                double* dst = a.A + size_t(T.slot[lane / 3]) * size_t(a.lda) + col0 + S.slot[lane % 3];
+                *dst += pb[lane];
+            }
+            if (!wake)
+                for (int ai = 0; ai < 3; ++ai) rbt[ai] -= pb[9 + ai];
+            __syncwarp();
         }
     }
     // tip filaments (assemble.jl:344-354): segment_rule (:299-306) and segment_block (:312-321), FP64
@@ -769,7 +834,23 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
         vp_phase_begin(ctx, PH_NEAR);
         const size_t near_smem = sizeof(NearChunkSh) * NEAR_WARPS;
         VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, int(near_smem)));
-        for (int pass = 0; pass < 2; ++pass)
+        for (int pass = 0; pass < 2; ++pass) {
+            if (pass == 1) {
+                // the rest pairs as one list, evaluated pair-parallel into per-pair blocks
+                long long nrest = 0;
+                double* d_pairs;
+                if ((r = rest_list(ctx, dl, na, &nrest)) ||
+                    (r = dl.alloc(ctx, &d_pairs, size_t(12) * size_t(std::max(nrest, 1LL))))) {
+                    vp_system_free(sys);
+                    return r;
+                }
+                na.pair_out = d_pairs;
+                if (nrest > 0) {
+                    const int nb = persistent_blocks(ctx, near_kernel_pairs, 32 * NEAR_WARPS, 0);
+                    near_kernel_pairs<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+                    ctx->launches++;
+                }
+            }
             for (size_t c = 0; c < colours.size(); ++c) {
                 na.tests = d_tests + off[c];
                 na.ntests = off[c + 1] - off[c];
@@ -781,6 +862,7 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
                     near_kernel_rest<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
                 ctx->launches++;
             }
+        }
         vp_phase_end(ctx);
         VP_CUDA(ctx, cudaGetLastError());
     }

@@ -604,8 +604,105 @@ __device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjMulti& mx, cons
     }
 }
 
-// the pairs the lanes kernel left (self, touching, contact), the tip filaments and the freestream, for up to ADJ_MAX
-// adjoint vectors at once: every point's kernel and derivatives are evaluated once, and each vector keeps its sums
+// the pairs the lanes kernel left (self, touching, contact), one warp per pair, for up to ADJ_MAX adjoint vectors at
+// once: every point's kernel and derivatives are evaluated once, and each vector keeps its sums. A persistent grid
+// whose warps take the next pair of the list from a counter, so that test triangles with many contact pairs do not
+// leave the end of the launch to a few warps. The test side of a pair goes to TA, the source side to SA (atomics).
+__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, AdjMulti mx) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = 2 * a.ntri;
+    const long long total = a.rest_off[n];
+    const int K = mx.nadj;
+    PairCtx pc;
+    pc.a = &a;
+    pc.sh = &shm[w];
+    pc.lane = lane;
+    pc.nleaf = 0;
+    pc.nq64 = 0;
+    pc.fp32 = 0;
+    pc.nadj = K;
+    pc.dep = 0;
+    for (int j = 0; j < ADJ_MAX; ++j) pc.gdir[j] = 0;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+    for (;;) {
+        const long long idx = next_rest_pair(a.next, lane);
+        if (idx >= total) break;
+        const int g = rest_entry(a.rest_off, n, idx);
+        const int t = g >> 1;
+        const int set = g & 1;
+        const bool wake = set == 1;
+        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
+        const int s = (wake ? a.wrest_src : a.rest_src)[e0 + (idx - a.rest_off[g])];
+        const TriGeo& T = a.tri[t];
+        pc.T = &T;
+        for (int k = 0; k < 3; ++k) {
+            for (int j = 0; j < ADJ_MAX; ++j) pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+            pc.nu[k] = pc.nuk[0][k];
+            pc.Xc[k] = ld3(T.x + 3 * k) - ld3(T.c);
+            pc.Xcf[k] = mk3(float(pc.Xc[k].x), float(pc.Xc[k].y), float(pc.Xc[k].z));
+        }
+        pc.dep = 0;
+        const v3<double> nT = ld3(T.n);
+        const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
+        const double* gp = (wake ? mx.x[0].gam_w : mx.x[0].gam_b) + 3 * size_t(s);
+        const v3<double> G = mk3(gp[0], gp[1], gp[2]);
+        const double sig = wake ? 0.0 : S.sigma;
+        pc.m = cross(nT, G) + sig * nT;
+        pc.mf = mk3(float(pc.m.x), float(pc.m.y), float(pc.m.z));
+        AdjAcc acc = {};
+        pc.kind = 0;
+        pc.npts = 0;
+        pc.n64 = 0;
+        pc.nleaf = 0;
+        pc.nq64 = 0;
+        const int tier = tri_pair(pc, acc, t, s, wake);
+        flush_gdir(pc, mx, T, &S, wake);
+        fold32(acc);
+        v3<double> xS[3];
+        tri_corners(S, xS);
+        for (int j = 0; j < K; ++j) {
+            adj_warp_sum(acc.d[j]);
+            const AdjSums<double>& d = acc.d[j];
+            // the test side: lane k adds field k of the pair's (Xg, U, fs)
+            const v3<double> U = cross(G, d.Q) + sig * d.Q;
+            const double v[NTA] = {d.Xg[0].x, d.Xg[0].y, d.Xg[0].z, d.Xg[1].x, d.Xg[1].y, d.Xg[1].z,
+                                   d.Xg[2].x, d.Xg[2].y, d.Xg[2].z, U.x,       U.y,       U.z,       dot(d.Q, pc.m)};
+            double tmine = 0;
+#pragma unroll
+            for (int k = 0; k < NTA; ++k)
+                if (k == lane) tmine = v[k];
+            if (lane < NTA && tmine != 0.0) atomicAdd(mx.x[j].TA + size_t(t) * NTA + lane, tmine);
+            // the source side: lane k adds field k
+            SrcAdj<double> sa = src_of_pair(xS, d, pc.m, nT);
+            double f[NSA];
+            sa_flat(sa, f);
+            double* dst = mx.x[j].SA[set] + size_t(s) * NSA;
+            double mine = 0, mine2 = 0;
+#pragma unroll
+            for (int k = 0; k < 32; ++k)
+                if (k == lane) mine = f[k];
+#pragma unroll
+            for (int k = 32; k < NSA; ++k)
+                if (k - 32 == lane) mine2 = f[k];
+            if (mine != 0.0) atomicAdd(dst + lane, mine);
+            if (lane < NSA - 32 && mine2 != 0.0) atomicAdd(dst + 32 + lane, mine2);
+        }
+        __syncwarp();
+        P[tier] += 1;
+        Q[tier] += pc.npts;
+        Q64 += pc.n64;
+    }
+    if (lane == 0) {
+        for (int k = 0; k < 6; ++k) {
+            if (P[k]) atomicAdd(a.stats + k, P[k]);
+            if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
+        }
+        if (Q64) atomicAdd(a.stats + 12, Q64);
+    }
+}
+
+// the tip filaments and the freestream of one test triangle (one warp each), for up to ADJ_MAX adjoint vectors
 __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, AdjMulti mx) {
     __shared__ WarpSh shm[NEAR_WARPS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -641,57 +738,6 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
     }
     unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    for (int set = 0; set < 2; ++set) {
-        const bool wake = set == 1;
-        const long long e0 = wake ? a.wf_ptr[t] : a.nf_ptr[t];
-        const long long e1 = e0 + a.rest_cnt[2 * t + set];
-        const int* list = wake ? a.wrest_src : a.rest_src;
-        for (long long e = e0; e < e1; ++e) {
-            const int s = list[e];
-            const TriGeo& S = wake ? a.wtri[s] : a.tri[s];
-            const double* gp = (wake ? mx.x[0].gam_w : mx.x[0].gam_b) + 3 * size_t(s);
-            const v3<double> G = mk3(gp[0], gp[1], gp[2]);
-            const double sig = wake ? 0.0 : S.sigma;
-            pc.m = cross(nT, G) + sig * nT;
-            pc.mf = mk3(float(pc.m.x), float(pc.m.y), float(pc.m.z));
-            AdjAcc acc = {};
-            pc.kind = 0;
-            pc.npts = 0;
-            pc.n64 = 0;
-            pc.nleaf = 0;
-            pc.nq64 = 0;
-            int tier = tri_pair(pc, acc, t, s, wake);
-            flush_gdir(pc, mx, T, &S, wake);
-            fold32(acc);
-            v3<double> xS[3];
-            tri_corners(S, xS);
-            for (int j = 0; j < K; ++j) {
-                adj_warp_sum(acc.d[j]);
-                const AdjSums<double>& d = acc.d[j];
-                for (int k = 0; k < 3; ++k) Xg[j][k] += d.Xg[k];
-                U[j] += cross(G, d.Q) + sig * d.Q;
-                fs[j] += dot(d.Q, pc.m);
-                // the source side: lane k adds field k
-                SrcAdj<double> sa = src_of_pair(xS, d, pc.m, nT);
-                double f[NSA];
-                sa_flat(sa, f);
-                double* dst = mx.x[j].SA[set] + size_t(s) * NSA;
-                double mine = 0, mine2 = 0;
-#pragma unroll
-                for (int k = 0; k < 32; ++k)
-                    if (k == lane) mine = f[k];
-#pragma unroll
-                for (int k = 32; k < NSA; ++k)
-                    if (k - 32 == lane) mine2 = f[k];
-                if (mine != 0.0) atomicAdd(dst + lane, mine);
-                if (lane < NSA - 32 && mine2 != 0.0) atomicAdd(dst + 32 + lane, mine2);
-            }
-            __syncwarp();
-            P[tier] += 1;
-            Q[tier] += pc.npts;
-            Q64 += pc.n64;
-        }
-    }
     // tip filaments (assemble.jl:344-354), FP64: f = sum W nu (mu_a va + mu_b vb)·n_T
     for (int fi = 0; fi < a.nfil; ++fi) {
         const int ia = a.fil[2 * fi], ib = a.fil[2 * fi + 1];
@@ -1003,9 +1049,12 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
             adj_lanes_kernel<<<nb, 32 * NEAR_WARPS, smem, ctx->stream>>>(na, mx.x[k]);
         }
         na.stats = d_stats;
+        if ((r = rest_list(ctx, dl, na, nullptr))) return r;
+        adj_pairs_kernel<<<persistent_blocks(ctx, adj_pairs_kernel, 32 * NEAR_WARPS, 0), 32 * NEAR_WARPS, 0,
+                           ctx->stream>>>(na, mx);
         adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
         vp_phase_end(ctx);
-        ctx->launches += nadj + 1;
+        ctx->launches += nadj + 2;
         VP_CUDA(ctx, cudaGetLastError());
     }
     vp_phase_begin(ctx, PH_ADJOINT);

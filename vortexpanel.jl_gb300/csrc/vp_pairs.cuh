@@ -333,6 +333,9 @@ struct NearArgs {
     int* rest_src;   // per test, at the offsets of nf_src: the body sources left to the warp-cooperative path
     int* wrest_src;  // the same for the wake sources
     int* rest_cnt;   // per test: counts of both (2 x ntri)
+    const long long* rest_off;  // exclusive prefix sums of rest_cnt (2 x ntri + 1): a rest pair's place in the list
+    double* pair_out;           // forward: per rest pair, its 3 x 3 block (row-major) and its 3 right hand side terms
+    unsigned long long* next;   // work counter of the pair-parallel kernels
     const long long* touch;  // sorted keys t * ntri + s
     int ntouch;
     const RulePt* rule[5];
@@ -1944,6 +1947,88 @@ int setup_pairs(vp_ctx* ctx, const PairInput& in, int ph_setup, int ph_classify,
 
 // the arguments of the near, touching and contact kernels that come from the set-up (A, b, tests, stats and the
 // rest lists are the caller's)
+// ---- the rest pairs (self, touching, contact) as one list, for the pair-parallel kernels ---------------------------
+// The lanes kernels leave, per test triangle t and source set (0 body, 1 wake), rest_cnt[2t + set] pairs at the
+// start of its segment of rest_src / wrest_src. Their exclusive prefix sums number the pairs 0 .. total - 1 in the
+// order (t, set, position); a warp of a pair-parallel kernel takes the next number from a counter.
+
+constexpr int SCAN_NT = 1024;
+
+// rest_off[i] = sum of cnt[0 .. i - 1] for i = 0 .. n (one block of SCAN_NT threads)
+__global__ void __launch_bounds__(SCAN_NT) rest_scan_kernel(const int* __restrict__ cnt, int n, long long* off) {
+    __shared__ long long s[SCAN_NT];
+    __shared__ long long carry;
+    const int i0 = threadIdx.x;
+    if (i0 == 0) carry = 0;
+    __syncthreads();
+    for (int base = 0; base < n; base += SCAN_NT) {
+        const int i = base + i0;
+        const long long v = i < n ? (long long)cnt[i] : 0;
+        s[i0] = v;
+        __syncthreads();
+        for (int o = 1; o < SCAN_NT; o <<= 1) {
+            const long long u = i0 >= o ? s[i0 - o] : 0;
+            __syncthreads();
+            s[i0] += u;
+            __syncthreads();
+        }
+        if (i < n) off[i] = carry + s[i0] - v;
+        __syncthreads();
+        if (i0 == SCAN_NT - 1) carry += s[SCAN_NT - 1];
+        __syncthreads();
+    }
+    if (i0 == 0) off[n] = carry;
+}
+
+// the (t, set) entry g = 2 t + set of rest pair idx: the largest g with off[g] <= idx (0 <= idx < off[n], so g < n
+// and off[g + 1] > idx: empty entries are skipped)
+__device__ __forceinline__ int rest_entry(const long long* __restrict__ off, int n, long long idx) {
+    int lo = 0, hi = n;
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (off[mid] <= idx) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// the next rest pair of this warp (all lanes call it together)
+__device__ __forceinline__ long long next_rest_pair(unsigned long long* next, int lane) {
+    unsigned long long v = 0;
+    if (lane == 0) v = atomicAdd(next, 1ull);
+    return (long long)__shfl_sync(0xffffffffu, v, 0);
+}
+
+// the offsets of the rest pairs (after the lanes kernel) and a zeroed work counter; with `total`, the number of rest
+// pairs is copied to the host (the stream is synchronised)
+int rest_list(vp_ctx* ctx, DevList& dl, NearArgs& na, long long* total) {
+    long long* d_off;
+    unsigned long long* d_next;
+    int r;
+    const int n = 2 * na.ntri;
+    if ((r = dl.alloc(ctx, &d_off, size_t(n) + 1)) || (r = dl.alloc(ctx, &d_next, 1))) return r;
+    rest_scan_kernel<<<1, SCAN_NT, 0, ctx->stream>>>(na.rest_cnt, n, d_off);
+    ctx->launches++;
+    VP_CUDA(ctx, cudaGetLastError());
+    VP_CUDA(ctx, cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), ctx->stream));
+    na.rest_off = d_off;
+    na.next = d_next;
+    if (total) {
+        VP_CUDA(ctx, vp_d2h(ctx, total, d_off + n, sizeof(long long)));
+        VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return VP_OK;
+}
+
+// CTAs of a persistent pair-parallel kernel: as many as stay resident on every SM
+template <class K>
+int persistent_blocks(vp_ctx* ctx, K kernel, int threads, size_t smem) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return per_sm * std::max(ctx->nsm, 1);
+}
+
 NearArgs near_args(const PairSetup& ps, const PairInput& in) {
     const vp_assembly_options* o = in.o;
     NearArgs na{};
