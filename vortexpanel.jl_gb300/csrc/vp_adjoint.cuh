@@ -19,12 +19,12 @@ struct ExactShape {
 };
 
 // s = w·m of the exact kernel at fixed shape (nu, len, n from the source) and ds/dr_a.
-template <class T>
+template <class T, class M = KMath<T>>
 __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r1, v3<T> r2, v3<T> r, v3<T> m,
                                           int side, T plane_tol, v3<T>& g0, v3<T>& g1, v3<T>& g2, ExactShape<T>& sh) {
     const T i4pi = T(1) / (T(4) * vp_pi<T>());
     const v3<T> R[3] = {r0, r1, r2};
-    T l[3] = {vnorm(r0), vnorm(r1), vnorm(r2)};
+    T l[3] = {M::sqrt(dot(r0, r0)), M::sqrt(dot(r1, r1)), M::sqrt(dot(r2, r2))};
     v3<T> gr[3] = {mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0))};
     T lbar[3] = {T(0), T(0), T(0)};
     T s = T(0);
@@ -39,23 +39,26 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
         T c2 = norm2(c);
         if (p < T(0)) {
             T den = l[i] * l[j] - p;
-            T q = den / (T(2) * c2);
-            L = vlog(num * num * q);
+            T q = M::div(den, T(2) * c2);
+            L = M::log(num * num * q);
             // d log q: li -> lj/den, lj -> li/den, p -> -1/den, c2 -> -1/c2
-            dLdli = T(2) / num + l[j] / den;
-            dLdlj = T(2) / num + l[i] / den;
-            dLdp = -T(1) / den;
-            T dLdc2 = -T(1) / c2;
+            dLdli = M::div(T(2), num) + M::div(l[j], den);
+            dLdlj = M::div(T(2), num) + M::div(l[i], den);
+            dLdp = M::div(-T(1), den);
+            T dLdc2 = M::div(-T(1), c2);
             T coef = dot(S.nu[e], m) * i4pi;
             // c2 = |ri x rj|^2: d/dri = 2 rj x c, d/drj = 2 c x ri
             gr[i] += (coef * dLdc2 * T(2)) * cross(rj, c);
             gr[j] += (coef * dLdc2 * T(2)) * cross(c, ri);
         } else {
             T den = l[i] * l[j] + p;
-            L = sizeof(T) == 4 ? T(log1pf(float(S.len[e] * num / den))) : vlog(num * num / (T(2) * den));
-            dLdli = T(2) / num - l[j] / den;
-            dLdlj = T(2) / num - l[i] / den;
-            dLdp = -T(1) / den;
+            if constexpr (M::hybrid)
+                L = M::log1p(M::div(S.len[e] * num, den));
+            else
+                L = sizeof(T) == 4 ? T(log1pf(float(S.len[e] * num / den))) : vlog(num * num / (T(2) * den));
+            dLdli = M::div(T(2), num) - M::div(l[j], den);
+            dLdlj = M::div(T(2), num) - M::div(l[i], den);
+            dLdp = M::div(-T(1), den);
         }
         T coef = dot(S.nu[e], m) * i4pi;
         s += L * coef;
@@ -64,7 +67,7 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
         gr[i] += (coef * dLdp) * rj;
         gr[j] += (coef * dLdp) * ri;
         sh.L[e] = L;
-        sh.dLdlen[e] = T(2) / num;
+        sh.dLdlen[e] = M::div(T(2), num);
     }
     T z = dot(r, S.n);
     T nm = dot(S.n, m) * i4pi;
@@ -74,12 +77,12 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
         v3<T> q[3] = {-r0, -r1, -r2};
         sh.Om = side == 0 ? T(0) : T(side) * T(2) * vp_pi<T>() * inplane_fraction_rel(q, S.n, S.area, plane_tol);
     } else {
-        sh.Om = T(2) * vatan2(N, D);
+        sh.Om = T(2) * M::atan2(N, D);
     }
     // 2 atan2(N, D) is smooth across the plane away from the triangle's edges (N = 0, D != 0): in the plane its
     // derivative along the normal is the one-sided limit of the general formula, which the in-plane branch keeps
     if (N * N + D * D > T(0)) {
-        T h = T(2) / (N * N + D * D);
+        T h = M::div(T(2), N * N + D * D);
         T Nb = nm * D * h, Db = -nm * N * h;
         gr[0] += Nb * cross(r1, r2);
         gr[1] += Nb * cross(r2, r0);
@@ -93,7 +96,7 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
     }
     s += sh.Om * nm;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) gr[a] += (lbar[a] / l[a]) * R[a];
+    for (int a = 0; a < 3; ++a) gr[a] += M::div(lbar[a], l[a]) * R[a];
     g0 = gr[0];
     g1 = gr[1];
     g2 = gr[2];

@@ -77,13 +77,13 @@ __device__ __forceinline__ T adj_point_far(AdjSums<T>& acc, const SrcKern<T>& S,
 
 // several adjoint vectors at once (their point weights Wn[k], k < nk): the kernel and its derivatives are evaluated
 // once, and each set of sums takes its own weight
-template <class T>
+template <class T, class M = KMath<T>>
 __device__ __forceinline__ T adj_point_exact_multi(AdjSums<T>* acc, int nk, const T* Wn, const SrcKern<T>& S, T l0, T l1,
                                                    T l2, v3<T> r0, v3<T> r1, v3<T> r2, v3<T> r, v3<T> m, int side,
                                                    T plane_tol, v3<T>& gx) {
     v3<T> g0, g1, g2;
     ExactShape<T> sh;
-    T sv = sv_exact_vjp(S, r0, r1, r2, r, m, side, plane_tol, g0, g1, g2, sh);
+    T sv = sv_exact_vjp<T, M>(S, r0, r1, r2, r, m, side, plane_tol, g0, g1, g2, sh);
     const T i4pi = T(1) / (T(4) * vp_pi<T>());
     const v3<T> w = (sh.L[0] * S.nu[0] + sh.L[1] * S.nu[1] + sh.L[2] * S.nu[2] + sh.Om * S.n) * i4pi;
     gx = g0 + g1 + g2;

@@ -504,7 +504,7 @@ __device__ void pair_block_out(PairCtx& pc, FwdAcc& acc, const TriGeo& S, double
 // the self, touching and contact pairs, one warp per pair: a persistent grid whose warps take the next pair of the
 // list from a counter, so that test triangles with many contact pairs (thin panels at a sharp trailing edge) do not
 // hold a launch; the blocks go to pair_out and near_kernel_rest adds them in the list's order
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_pairs(NearArgs a) {
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_pairs(NearArgs a) {
     __shared__ WarpSh shm[NEAR_WARPS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int n = 2 * a.ntri;
@@ -544,9 +544,38 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_pairs(NearArgs a)
     }
 }
 
+// one far tip filament of test triangle T, summed by one lane: segment_block (assemble.jl:312-321) with the far rule
+// (the columns of the filament's two end nodes, ca and cb, per test function)
+__device__ void far_filament_fwd(const NearArgs& a, const TriGeo& T, v3<double> fa, v3<double> fb, double* ca,
+                                 double* cb) {
+    const RulePt* R = a.rule[R_FAR];
+    const v3<double> n = ld3(T.n);
+    v3<double> Ea[3], Eb[3];
+    for (int k = 0; k < 3; ++k) {
+        Ea[k] = ld3(T.x + 3 * k) - fa;
+        Eb[k] = ld3(T.x + 3 * k) - fb;
+    }
+    for (int i = 0; i < a.nrule[R_FAR]; ++i) {
+        const RulePt m = R[i];
+        const double W = m.w * T.area;
+        const v3<double> ra = m.l0 * Ea[0] + m.l1 * Ea[1] + m.l2 * Ea[2];
+        const v3<double> rb = m.l0 * Eb[0] + m.l1 * Eb[1] + m.l2 * Eb[2];
+        v3<double> va, vb;
+        segment_velocity(ra, rb, va, vb);
+        const v3<double> psi = test_weights(a.test_mode, m.l0, m.l1, m.l2);
+        const double da = dot(va, n) * W, db = dot(vb, n) * W;
+        ca[0] += da * psi.x;
+        ca[1] += da * psi.y;
+        ca[2] += da * psi.z;
+        cb[0] += db * psi.x;
+        cb[1] += db * psi.y;
+        cb[2] += db * psi.z;
+    }
+}
+
 // the blocks of the self, touching and contact pairs (from near_kernel_pairs, added in the order of the test
 // triangle's list), the tip filaments and the freestream: one warp per test triangle, a launch per colour
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) {
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_rest(NearArgs a) {
     __shared__ WarpSh shm[NEAR_WARPS];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int idx = blockIdx.x * NEAR_WARPS + w;
@@ -583,34 +612,61 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) 
             __syncwarp();
         }
     }
-    // tip filaments (assemble.jl:344-354): segment_rule (:299-306) and segment_block (:312-321), FP64
-    for (int f = 0; f < a.nfil; ++f) {
-        int ia = a.fil[2 * f], ib = a.fil[2 * f + 1];
-        v3<double> fa = ld3(a.wx + 3 * ia), fb = ld3(a.wx + 3 * ib);
-        if (lane == 0) {
-            for (int k = 0; k < 3; ++k) {
-                pc.sh->E[9 * k + 0] = T.x[3 * k + 0] - fa.x;
-                pc.sh->E[9 * k + 1] = T.x[3 * k + 1] - fa.y;
-                pc.sh->E[9 * k + 2] = T.x[3 * k + 2] - fa.z;
-                pc.sh->E[9 * k + 3] = T.x[3 * k + 0] - fb.x;
-                pc.sh->E[9 * k + 4] = T.x[3 * k + 1] - fb.y;
-                pc.sh->E[9 * k + 5] = T.x[3 * k + 2] - fb.z;
-            }
+    // tip filaments (assemble.jl:344-354): segment_rule (:299-306) and segment_block (:312-321), FP64. A warp takes 32
+    // filaments at once: a far one (the far rule's few points) is summed by its own lane, the others by the whole
+    // warp; the columns are added in the filaments' order.
+    for (int f0 = 0; f0 < a.nfil; f0 += 32) {
+        const int cnt = a.nfil - f0 < 32 ? a.nfil - f0 : 32;
+        int mia = 0, mib = 0;
+        double mca[3] = {0, 0, 0}, mcb[3] = {0, 0, 0};
+        bool mfar = false;
+        if (lane < cnt) {
+            mia = a.fil[2 * (f0 + lane)];
+            mib = a.fil[2 * (f0 + lane) + 1];
+            const v3<double> fa = ld3(a.wx + 3 * mia), fb = ld3(a.wx + 3 * mib);
+            mfar = vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, vnorm(fb - fa));
+            if (mfar) far_filament_fwd(a, T, fa, fb, mca, mcb);
         }
-        __syncwarp();
-        FwdAcc acc = {};
-        pc.kind = 1;
-        pc.npts = 0;
-        pc.n64 = 0;
-        pc.side = 0;
-        pc.fp32 = 0;
-        double L = vnorm(fb - fa);
-        int tier;
-        if (vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, L)) {
-            tier = TIER_FAR;
-            emit_rule(pc, acc, R_FAR, corners, 1.0);
-        } else {
-            int kv = -1;
+        const unsigned farmask = __ballot_sync(0xffffffffu, mfar);
+        for (int q = 0; q < cnt; ++q) {
+            const int ia = __shfl_sync(0xffffffffu, mia, q), ib = __shfl_sync(0xffffffffu, mib, q);
+            if ((farmask >> q) & 1u) {
+                double ca[3], cb[3];
+                for (int k = 0; k < 3; ++k) {
+                    ca[k] = __shfl_sync(0xffffffffu, mca[k], q);
+                    cb[k] = __shfl_sync(0xffffffffu, mcb[k], q);
+                }
+                if (lane < 3) {
+                    double* row = a.A + size_t(T.slot[lane]) * size_t(a.lda) + a.nslot;
+                    row[ia] += lane == 0 ? ca[0] : (lane == 1 ? ca[1] : ca[2]);
+                    __syncwarp(0x7u);
+                    row[ib] += lane == 0 ? cb[0] : (lane == 1 ? cb[1] : cb[2]);
+                }
+                __syncwarp();
+                P[TIER_FAR] += 1;
+                Q[TIER_FAR] += a.nrule[R_FAR];
+                continue;
+            }
+            // near and vertex filaments (segment_rule, assemble.jl:299-306), the whole warp
+            const v3<double> fa = ld3(a.wx + 3 * ia), fb = ld3(a.wx + 3 * ib);
+            if (lane == 0) {
+                for (int k = 0; k < 3; ++k) {
+                    pc.sh->E[9 * k + 0] = T.x[3 * k + 0] - fa.x;
+                    pc.sh->E[9 * k + 1] = T.x[3 * k + 1] - fa.y;
+                    pc.sh->E[9 * k + 2] = T.x[3 * k + 2] - fa.z;
+                    pc.sh->E[9 * k + 3] = T.x[3 * k + 0] - fb.x;
+                    pc.sh->E[9 * k + 4] = T.x[3 * k + 1] - fb.y;
+                    pc.sh->E[9 * k + 5] = T.x[3 * k + 2] - fb.z;
+                }
+            }
+            __syncwarp();
+            FwdAcc acc = {};
+            pc.kind = 1;
+            pc.npts = 0;
+            pc.n64 = 0;
+            pc.side = 0;
+            pc.fp32 = 0;
+            int tier, kv = -1;
             for (int k = 0; k < 3 && kv < 0; ++k)
                 if (fmin(vnorm(ld3(T.x + 3 * k) - fa), vnorm(ld3(T.x + 3 * k) - fb)) <= 1e-12 * T.diam) kv = k;
             if (kv >= 0) {
@@ -622,22 +678,22 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_rest(NearArgs a) 
                 near_pieces(pc, acc, src, corners, 1.0, a.near_depth);
                 flush_leaves(pc, acc);
             }
+            double ca[3], cb[3];
+            for (int k = 0; k < 3; ++k) {
+                ca[k] = warp_sum(acc.ca[k]);
+                cb[k] = warp_sum(acc.cb[k]);
+            }
+            if (lane < 3) {
+                double* row = a.A + size_t(T.slot[lane]) * size_t(a.lda) + a.nslot;
+                row[ia] += ca[lane];
+                __syncwarp(0x7u);
+                row[ib] += cb[lane];
+            }
+            __syncwarp();
+            P[tier] += 1;
+            Q[tier] += pc.npts;
+            Q64 += pc.n64;
         }
-        double ca[3], cb[3];
-        for (int k = 0; k < 3; ++k) {
-            ca[k] = warp_sum(acc.ca[k]);
-            cb[k] = warp_sum(acc.cb[k]);
-        }
-        if (lane < 3) {
-            double* row = a.A + size_t(T.slot[lane]) * size_t(a.lda) + a.nslot;
-            row[ia] += ca[lane];
-            __syncwarp(0x7u);
-            row[ib] += cb[lane];
-        }
-        __syncwarp();
-        P[tier] += 1;
-        Q[tier] += pc.npts;
-        Q64 += pc.n64;
     }
     // freestream, exact (assemble.jl:422), and the rows of b
     if (lane == 0) {

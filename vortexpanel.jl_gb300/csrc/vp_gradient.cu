@@ -702,6 +702,56 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, 
     }
 }
 
+// one far tip filament (ends ia, ib) of test triangle T, summed by one lane for every adjoint vector: the far rule's
+// points of the filament's part of f = sum W nu (mu_a va + mu_b vb)·n_T (eval_point64's filament branch), added to
+// the lane's test-side sums Xg, U, fs; the derivatives to the filament's end nodes go to gwx
+__device__ void far_filament_adj(const NearArgs& a, const AdjMulti& mx, const PairCtx& pc, const TriGeo& T, int ia,
+                                 int ib, v3<double> fa, v3<double> fb, v3<double> (*Xg)[3], v3<double>* U,
+                                 double* fs) {
+    const RulePt* R = a.rule[R_FAR];
+    const v3<double> n = ld3(T.n);
+    const double mua = mx.x[0].mu[a.nslot + ia], mub = mx.x[0].mu[a.nslot + ib];
+    v3<double> Ea[3], Eb[3];
+    for (int k = 0; k < 3; ++k) {
+        Ea[k] = ld3(T.x + 3 * k) - fa;
+        Eb[k] = ld3(T.x + 3 * k) - fb;
+    }
+    v3<double> Ga[ADJ_MAX], Gb[ADJ_MAX], Qs[ADJ_MAX];
+    for (int j = 0; j < ADJ_MAX; ++j) Ga[j] = Gb[j] = Qs[j] = mk3(0.0, 0.0, 0.0);
+    for (int i = 0; i < a.nrule[R_FAR]; ++i) {
+        const RulePt m = R[i];
+        const double W = m.w * T.area;
+        const v3<double> psi = test_weights(a.test_mode, m.l0, m.l1, m.l2);
+        const v3<double> ra = m.l0 * Ea[0] + m.l1 * Ea[1] + m.l2 * Ea[2];
+        const v3<double> rb = m.l0 * Eb[0] + m.l1 * Eb[1] + m.l2 * Eb[2];
+        v3<double> va, vb, ga, gb;
+        segment_velocity(ra, rb, va, vb);
+        seg_vjp(ra, rb, n, mua, mub, ga, gb);
+        const v3<double> gx = ga + gb;
+        const v3<double> q = mua * va + mub * vb;
+        for (int j = 0; j < mx.nadj; ++j) {
+            const double Wn = W * (pc.nuk[j][0] * psi.x + pc.nuk[j][1] * psi.y + pc.nuk[j][2] * psi.z);
+            Qs[j] += Wn * q;
+            Xg[j][0] += (Wn * m.l0) * gx;
+            Xg[j][1] += (Wn * m.l1) * gx;
+            Xg[j][2] += (Wn * m.l2) * gx;
+            Ga[j] += Wn * ga;
+            Gb[j] += Wn * gb;
+        }
+    }
+    for (int j = 0; j < mx.nadj; ++j) {
+        U[j] += Qs[j];
+        fs[j] += dot(Qs[j], n);
+        double* g = mx.x[j].gwx;
+        atomicAdd(g + 3 * ia + 0, -Ga[j].x);
+        atomicAdd(g + 3 * ia + 1, -Ga[j].y);
+        atomicAdd(g + 3 * ia + 2, -Ga[j].z);
+        atomicAdd(g + 3 * ib + 0, -Gb[j].x);
+        atomicAdd(g + 3 * ib + 1, -Gb[j].y);
+        atomicAdd(g + 3 * ib + 2, -Gb[j].z);
+    }
+}
+
 // the tip filaments and the freestream of one test triangle (one warp each), for up to ADJ_MAX adjoint vectors
 __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, AdjMulti mx) {
     __shared__ WarpSh shm[NEAR_WARPS];
@@ -738,65 +788,92 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
     }
     unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
     const double corners[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-    // tip filaments (assemble.jl:344-354), FP64: f = sum W nu (mu_a va + mu_b vb)·n_T
-    for (int fi = 0; fi < a.nfil; ++fi) {
-        const int ia = a.fil[2 * fi], ib = a.fil[2 * fi + 1];
-        v3<double> fa = ld3(a.wx + 3 * ia), fb = ld3(a.wx + 3 * ib);
-        if (lane == 0) {
-            for (int k = 0; k < 3; ++k) {
-                pc.sh->E[9 * k + 0] = T.x[3 * k + 0] - fa.x;
-                pc.sh->E[9 * k + 1] = T.x[3 * k + 1] - fa.y;
-                pc.sh->E[9 * k + 2] = T.x[3 * k + 2] - fa.z;
-                pc.sh->E[9 * k + 3] = T.x[3 * k + 0] - fb.x;
-                pc.sh->E[9 * k + 4] = T.x[3 * k + 1] - fb.y;
-                pc.sh->E[9 * k + 5] = T.x[3 * k + 2] - fb.z;
+    // tip filaments (assemble.jl:344-354), FP64: f = sum W nu (mu_a va + mu_b vb)·n_T. A warp takes 32 filaments at
+    // once: a far one (the far rule's few points) is summed by its own lane, the others by the whole warp.
+    {
+        v3<double> lXg[ADJ_MAX][3], lU[ADJ_MAX];
+        double lfs[ADJ_MAX];
+        for (int j = 0; j < ADJ_MAX; ++j) {
+            for (int k = 0; k < 3; ++k) lXg[j][k] = mk3(0.0, 0.0, 0.0);
+            lU[j] = mk3(0.0, 0.0, 0.0);
+            lfs[j] = 0;
+        }
+        for (int f0 = 0; f0 < a.nfil; f0 += 32) {
+            const int cnt = a.nfil - f0 < 32 ? a.nfil - f0 : 32;
+            bool mfar = false;
+            if (lane < cnt) {
+                const int ia = a.fil[2 * (f0 + lane)], ib = a.fil[2 * (f0 + lane) + 1];
+                const v3<double> fa = ld3(a.wx + 3 * ia), fb = ld3(a.wx + 3 * ib);
+                mfar = vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, vnorm(fb - fa));
+                if (mfar)
+                    far_filament_adj(a, mx, pc, T, ia, ib, fa, fb, lXg, lU, lfs);
+            }
+            const unsigned farmask = __ballot_sync(0xffffffffu, mfar);
+            P[TIER_FAR] += __popc(farmask);
+            Q[TIER_FAR] += (unsigned long long)__popc(farmask) * a.nrule[R_FAR];
+            for (int q = 0; q < cnt; ++q) {
+                if ((farmask >> q) & 1u) continue;
+                // near and vertex filaments (segment_rule, assemble.jl:299-306), the whole warp
+                const int fi = f0 + q;
+                const int ia = a.fil[2 * fi], ib = a.fil[2 * fi + 1];
+                v3<double> fa = ld3(a.wx + 3 * ia), fb = ld3(a.wx + 3 * ib);
+                if (lane == 0) {
+                    for (int k = 0; k < 3; ++k) {
+                        pc.sh->E[9 * k + 0] = T.x[3 * k + 0] - fa.x;
+                        pc.sh->E[9 * k + 1] = T.x[3 * k + 1] - fa.y;
+                        pc.sh->E[9 * k + 2] = T.x[3 * k + 2] - fa.z;
+                        pc.sh->E[9 * k + 3] = T.x[3 * k + 0] - fb.x;
+                        pc.sh->E[9 * k + 4] = T.x[3 * k + 1] - fb.y;
+                        pc.sh->E[9 * k + 5] = T.x[3 * k + 2] - fb.z;
+                    }
+                }
+                __syncwarp();
+                AdjAcc acc = {};
+                pc.kind = 1;
+                pc.npts = 0;
+                pc.n64 = 0;
+                pc.side = 0;
+                pc.fp32 = 0;
+                pc.mua = mx.x[0].mu[a.nslot + ia];
+                pc.mub = mx.x[0].mu[a.nslot + ib];
+                int tier, kv = -1;
+                for (int k = 0; k < 3 && kv < 0; ++k)
+                    if (fmin(vnorm(ld3(T.x + 3 * k) - fa), vnorm(ld3(T.x + 3 * k) - fb)) <= 1e-12 * T.diam) kv = k;
+                if (kv >= 0) {
+                    tier = TIER_VERTEX;
+                    vertex_rule(pc, acc, kv);
+                } else {
+                    tier = TIER_NEAR;
+                    SrcRef src{1, nullptr, fa, fb};
+                    near_pieces(pc, acc, src, corners, 1.0, a.near_depth);
+                    flush_leaves(pc, acc);
+                }
+                flush_gdir(pc, mx, T, nullptr, false);
+                for (int j = 0; j < K; ++j) {
+                    adj_warp_sum(acc.d[j]);
+                    const AdjSums<double>& d = acc.d[j];
+                    for (int k = 0; k < 3; ++k) Xg[j][k] += d.Xg[k];
+                    U[j] += d.Q;
+                    fs[j] += dot(d.Q, nT);
+                    if (lane < 3) {
+                        const double ga[3] = {d.Gr[0].x, d.Gr[0].y, d.Gr[0].z},
+                                     gb[3] = {d.Gr[1].x, d.Gr[1].y, d.Gr[1].z};
+                        atomicAdd(mx.x[j].gwx + 3 * ia + lane, -ga[lane]);
+                        atomicAdd(mx.x[j].gwx + 3 * ib + lane, -gb[lane]);
+                    }
+                }
+                __syncwarp();
+                P[tier] += 1;
+                Q[tier] += pc.npts;
+                Q64 += pc.n64;
             }
         }
-        __syncwarp();
-        AdjAcc acc = {};
-        pc.kind = 1;
-        pc.npts = 0;
-        pc.n64 = 0;
-        pc.side = 0;
-        pc.fp32 = 0;
-        pc.mua = mx.x[0].mu[a.nslot + ia];
-        pc.mub = mx.x[0].mu[a.nslot + ib];
-        const double L = vnorm(fb - fa);
-        int tier;
-        if (vnorm((fa + fb) / 2.0 - ld3(T.c)) > a.far_ratio * fmax(T.diam, L)) {
-            tier = TIER_FAR;
-            emit_rule(pc, acc, R_FAR, corners, 1.0);
-        } else {
-            int kv = -1;
-            for (int k = 0; k < 3 && kv < 0; ++k)
-                if (fmin(vnorm(ld3(T.x + 3 * k) - fa), vnorm(ld3(T.x + 3 * k) - fb)) <= 1e-12 * T.diam) kv = k;
-            if (kv >= 0) {
-                tier = TIER_VERTEX;
-                vertex_rule(pc, acc, kv);
-            } else {
-                tier = TIER_NEAR;
-                SrcRef src{1, nullptr, fa, fb};
-                near_pieces(pc, acc, src, corners, 1.0, a.near_depth);
-                flush_leaves(pc, acc);
-            }
-        }
-        flush_gdir(pc, mx, T, nullptr, false);
+        // the lanes' far filaments into the warp's test-side sums
         for (int j = 0; j < K; ++j) {
-            adj_warp_sum(acc.d[j]);
-            const AdjSums<double>& d = acc.d[j];
-            for (int k = 0; k < 3; ++k) Xg[j][k] += d.Xg[k];
-            U[j] += d.Q;
-            fs[j] += dot(d.Q, nT);
-            if (lane < 3) {
-                const double ga[3] = {d.Gr[0].x, d.Gr[0].y, d.Gr[0].z}, gb[3] = {d.Gr[1].x, d.Gr[1].y, d.Gr[1].z};
-                atomicAdd(mx.x[j].gwx + 3 * ia + lane, -ga[lane]);
-                atomicAdd(mx.x[j].gwx + 3 * ib + lane, -gb[lane]);
-            }
+            for (int k = 0; k < 3; ++k) Xg[j][k] += wsum3(lXg[j][k]);
+            U[j] += wsum3(lU[j]);
+            fs[j] += wsum_d(lfs[j]);
         }
-        __syncwarp();
-        P[tier] += 1;
-        Q[tier] += pc.npts;
-        Q64 += pc.n64;
     }
     // freestream (assemble.jl:422): (V·n_T) A_T sum_a nu_a ti_a, and the test side of every vector
     const v3<double> V = mk3(mx.x[0].V[0], mx.x[0].V[1], mx.x[0].V[2]);

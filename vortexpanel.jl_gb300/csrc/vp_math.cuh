@@ -37,6 +37,60 @@ __device__ __forceinline__ float vacos(float a) { return acosf(a); }
 __device__ __forceinline__ double vacos(double a) { return acos(a); }
 template <class T> __device__ __forceinline__ T vnorm(v3<T> a) { return vsqrt(dot(a, a)); }
 
+// The scalar functions of the exact kernel and its derivatives, as a policy of the evaluation.
+// KMath<T>: the plain FP32 or FP64 functions.
+// KMathHyb: the FP64 evaluation of the mixed-precision path, for the points that FP32 cannot take (near a source's
+// corners and edges, where the offsets, cross products and the solid angle's numerator and denominator cancel).
+// Those quantities stay FP64; the functions applied to them are FP32-based:
+// - the square root and the reciprocal are refined by one Newton step in FP64 (relative error ~1e-14);
+// - log, log1p and atan2 are the FP32 functions of the FP64-formed arguments (relative error ~1e-7, the accuracy of
+//   the points evaluated in FP32).
+// Arguments outside FP32's comfortable range go to the FP64 functions.
+template <class T>
+struct KMath {
+    static constexpr bool hybrid = false;
+    static __device__ __forceinline__ T sqrt(T x) { return vsqrt(x); }
+    static __device__ __forceinline__ T div(T a, T b) { return a / b; }
+    static __device__ __forceinline__ T log(T x) { return vlog(x); }
+    static __device__ __forceinline__ T atan2(T y, T x) { return vatan2(y, x); }
+};
+
+// the FP64 functions out of line, for KMathHyb's rare out-of-range arguments (kept off the hot path's registers)
+static __device__ __noinline__ double f64_sqrt(double x) { return sqrt(x); }
+static __device__ __noinline__ double f64_rcp(double x) { return 1.0 / x; }
+static __device__ __noinline__ double f64_log(double x) { return log(x); }
+static __device__ __noinline__ double f64_log1p(double x) { return log1p(x); }
+static __device__ __noinline__ double f64_atan2(double y, double x) { return atan2(y, x); }
+
+struct KMathHyb {
+    static constexpr bool hybrid = true;
+    static __device__ __forceinline__ bool in_range(double m) { return m > 1e-30 && m < 1e30; }
+    static __device__ __forceinline__ double sqrt(double x) {
+        if (!in_range(x)) return f64_sqrt(x);
+        const double y = double(rsqrtf(float(x)));
+        const double r = x * y;
+        return fma(0.5 * y, fma(-r, r, x), r);  // Newton: r + (x - r^2) / (2 r), with 1/r ~ y
+    }
+    static __device__ __forceinline__ double rcp(double x) {
+        if (!in_range(fabs(x))) return f64_rcp(x);
+        const double r = double(1.0f / float(x));
+        return fma(r, fma(-x, r, 1.0), r);  // Newton: r (2 - x r)
+    }
+    static __device__ __forceinline__ double div(double a, double b) { return a * rcp(b); }
+    static __device__ __forceinline__ double log(double x) {
+        if (!in_range(x)) return f64_log(x);
+        return double(logf(float(x)));
+    }
+    static __device__ __forceinline__ double log1p(double x) {
+        if (!(x > -0.5 && x < 1e30)) return f64_log1p(x);
+        return double(log1pf(float(x)));
+    }
+    static __device__ __forceinline__ double atan2(double y, double x) {
+        if (!in_range(fmax(fabs(x), fabs(y)))) return f64_atan2(y, x);
+        return double(atan2f(float(y), float(x)));
+    }
+};
+
 template <class T> __host__ __device__ __forceinline__ T vp_pi() { return T(3.141592653589793238462643383279502884); }
 
 // The source data the kernel needs, relative to the source centroid c (vertices v_a = c + d_a).
@@ -73,23 +127,27 @@ __device__ T inplane_fraction_rel(const v3<T> q[3], v3<T> n, T area, T tol) {
 // formed without cancellation as |ri x rj|^2 / (r_i r_j - ri.rj) when ri.rj < 0 (source_triangle.jl:39-44)
 // (FP32: where ri.rj >= 0 the same value as log1p(d (r_i + r_j + d) / (r_i r_j + ri.rj)), using
 // (r_i + r_j)^2 - d^2 = 2 (r_i r_j + ri.rj), which keeps its accuracy at a distance where the log's argument nears 1)
-template <class T>
+template <class T, class M = KMath<T>>
 __device__ __forceinline__ T edge_log_n(v3<T> ri, v3<T> rj, T li, T lj, T d) {
     T p = dot(ri, rj);
     T num = li + lj + d;
-    if (sizeof(T) == 4 && p >= T(0)) return T(log1pf(float(d * num / (li * lj + p))));
-    T q = p < T(0) ? (li * lj - p) / (T(2) * norm2(cross(ri, rj))) : T(1) / (T(2) * (li * lj + p));
-    return vlog(num * num * q);
+    if constexpr (M::hybrid) {
+        if (p >= T(0)) return M::log1p(M::div(d * num, li * lj + p));
+    } else {
+        if (sizeof(T) == 4 && p >= T(0)) return T(log1pf(float(d * num / (li * lj + p))));
+    }
+    T q = p < T(0) ? M::div(li * lj - p, T(2) * norm2(cross(ri, rj))) : M::div(T(1), T(2) * (li * lj + p));
+    return M::log(num * num * q);
 }
 
 // source_velocity_exact (source_triangle.jl:75-89) from the point's offsets to the three vertices ra, rb, rc
 // (r_a = x - v_a) and to the centroid r = x - c.
-template <class T>
+template <class T, class M = KMath<T>>
 __device__ __forceinline__ v3<T> sv_exact3(const SrcKern<T>& S, v3<T> ra, v3<T> rb, v3<T> rc, v3<T> r, int side,
                                            T plane_tol) {
-    T la = vnorm(ra), lb = vnorm(rb), lc = vnorm(rc);
-    v3<T> wt = edge_log_n(ra, rb, la, lb, S.len[0]) * S.nu[0] + edge_log_n(rb, rc, lb, lc, S.len[1]) * S.nu[1] +
-               edge_log_n(rc, ra, lc, la, S.len[2]) * S.nu[2];
+    T la = M::sqrt(dot(ra, ra)), lb = M::sqrt(dot(rb, rb)), lc = M::sqrt(dot(rc, rc));
+    v3<T> wt = edge_log_n<T, M>(ra, rb, la, lb, S.len[0]) * S.nu[0] + edge_log_n<T, M>(rb, rc, lb, lc, S.len[1]) * S.nu[1] +
+               edge_log_n<T, M>(rc, ra, lc, la, S.len[2]) * S.nu[2];
     T z = dot(r, S.n);
     T Om;
     if (fabs(z) <= plane_tol * S.diam) {
@@ -98,7 +156,7 @@ __device__ __forceinline__ v3<T> sv_exact3(const SrcKern<T>& S, v3<T> ra, v3<T> 
     } else {
         T N = dot(ra, cross(rb, rc));
         T D = la * lb * lc + dot(ra, rb) * lc + dot(ra, rc) * lb + dot(rb, rc) * la;
-        Om = T(2) * vatan2(N, D);
+        Om = T(2) * M::atan2(N, D);
     }
     return (wt + Om * S.n) * (T(1) / (T(4) * vp_pi<T>()));
 }

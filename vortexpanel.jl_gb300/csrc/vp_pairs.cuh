@@ -513,7 +513,10 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double
         S.area = sh.Sarea;
         S.diam = sh.Sdiam;
         double fd = pc.a->kernel_far * S.diam;
-        v3<double> w = dot(r, r) > fd * fd ? sv_far(S, r) : sv_exact3(S, ra, rb, rc, r, pc.side, 1e-12);
+        // the mixed path's FP64 points (where FP32 cancels): FP64 geometry, FP32-based functions (KMathHyb)
+        v3<double> w = dot(r, r) > fd * fd ? sv_far(S, r)
+                       : pc.fp32            ? sv_exact3<double, KMathHyb>(S, ra, rb, rc, r, pc.side, 1e-12)
+                                            : sv_exact3(S, ra, rb, rc, r, pc.side, 1e-12);
         acc.P[0] += (W * psi.x) * w;
         acc.P[1] += (W * psi.y) * w;
         acc.P[2] += (W * psi.z) * w;
@@ -674,6 +677,9 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, double
         double fd = pc.a->kernel_far * S.diam;
         if (dot(r, r) > fd * fd)
             sv = adj_point_far_multi(acc.d, pc.nadj, Wn, S, l0, l1, l2, r, pc.m, gx);
+        else if (pc.fp32)  // the mixed path's FP64 points: FP64 geometry and derivatives, FP32-based functions
+            sv = adj_point_exact_multi<double, KMathHyb>(acc.d, pc.nadj, Wn, S, l0, l1, l2, ra, rb, rc, r, pc.m,
+                                                         pc.side, 1e-12, gx);
         else
             sv = adj_point_exact_multi(acc.d, pc.nadj, Wn, S, l0, l1, l2, ra, rb, rc, r, pc.m, pc.side, 1e-12, gx);
     } else {
