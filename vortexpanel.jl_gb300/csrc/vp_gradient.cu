@@ -67,7 +67,7 @@ struct AdjFarArgs {
     const TriGeo* tgeo;
     const CentF* tcent;
     const double* lam;   // far rule barycentrics (nq x 3)
-    const double* nu;    // row slot values
+    const double* nu[ADJ_MAX];  // row slot values, per adjoint vector of the pass
     int nset;
     int nsrc[2], ntile[2];
     const void* soa[2];  // NFIELD x pad (T), as the assembly's far kernel
@@ -75,8 +75,8 @@ struct AdjFarArgs {
     int pad[2];
     const CentF* scent[2];
     const TriGeo* sgeo[2];
-    double* SA[2];
-    double* TA;
+    double* SA[ADJ_MAX][2];
+    double* TA[ADJ_MAX];
     float ratio32;
     double ratio, kernel_far;
 };
@@ -84,7 +84,7 @@ struct AdjFarArgs {
 template <class T>
 struct AdjFarTest {
     T xh[NQMAX][3], xl[NQMAX][3];
-    T Wn[NQMAX];  // w_q A_T nu(q)
+    T Wn[ADJ_MAX][NQMAX];  // w_q A_T nu(q), per adjoint vector
     T n[3];
     CentF cf;
     double c64[3];
@@ -92,11 +92,12 @@ struct AdjFarTest {
     int t;  // -1: past the end
 };
 
-template <class T, int TT>
+// K adjoint vectors in one pass (their weights differ, the kernel values and derivatives are shared)
+template <class T, int TT, int K>
 __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
     __shared__ AdjFarTest<T> ts[TT];
     __shared__ T lam[NQMAX][3];
-    __shared__ T red[TT][FAR_NT / 32][NTA];
+    __shared__ T red[TT][FAR_NT / 32][K * NTA];
     const T i4pi = T(1) / (T(4) * vp_pi<T>());
     int bx = blockIdx.x, set = 0;
     if (bx >= a.ntile[0]) {
@@ -130,8 +131,9 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
         G = mk3(g[s], g[size_t(pad) + s], g[2 * size_t(pad) + s]);
         scf = a.scent[set][s];
     }
-    SrcAdj<T> acc;
-    src_zero(acc);
+    SrcAdj<T> acc[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) src_zero(acc[j]);
     if (tid < 3 * a.nq) lam[tid / 3][tid % 3] = T(a.lam[tid]);
     const T fd = T(a.kernel_far) * (sv ? S.diam : T(0));
     const int tile0 = blockIdx.y * a.tiles_per_chunk;
@@ -144,7 +146,6 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
             q.t = t < a.ntest ? t : -1;
             if (q.t >= 0) {
                 const TriGeo& g = a.tgeo[t];
-                const double nv[3] = {a.nu[g.slot[0]], a.nu[g.slot[1]], a.nu[g.slot[2]]};
                 for (int p = 0; p < a.nq; ++p) {
                     const double* tq = a.tq + (size_t(t) * NQMAX + p) * 3;
                     const double* tw = a.tw + (size_t(t) * NQMAX + p) * 3;
@@ -153,7 +154,10 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
                         q.xh[p][k] = h;
                         q.xl[p][k] = T(tq[k] - double(h));
                     }
-                    q.Wn[p] = T(nv[0] * tw[0] + nv[1] * tw[1] + nv[2] * tw[2]);
+                    for (int j = 0; j < K; ++j) {
+                        const double* nu = a.nu[j];
+                        q.Wn[j][p] = T(nu[g.slot[0]] * tw[0] + nu[g.slot[1]] * tw[1] + nu[g.slot[2]] * tw[2]);
+                    }
                 }
                 for (int k = 0; k < 3; ++k) {
                     q.n[k] = T(g.n[k]);
@@ -177,16 +181,19 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
                     far = f == 1;
                 }
             }
-            v3<T> Xg[3] = {mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0)), mk3(T(0), T(0), T(0))};
-            v3<T> U = mk3(T(0), T(0), T(0));
-            T fs = T(0);
+            v3<T> Xg[K][3], U[K];
+            T fs[K];
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                Xg[j][0] = Xg[j][1] = Xg[j][2] = U[j] = mk3(T(0), T(0), T(0));
+                fs[j] = T(0);
+            }
             if (far) {
                 const v3<T> nT = mk3(q.n[0], q.n[1], q.n[2]);
                 const v3<T> m = cross(nT, G) + sig * nT;
                 for (int p = 0; p < a.nq; ++p) {
                     v3<T> r = mk3((q.xh[p][0] - ch.x) + (q.xl[p][0] - cl.x), (q.xh[p][1] - ch.y) + (q.xl[p][1] - cl.y),
                                   (q.xh[p][2] - ch.z) + (q.xl[p][2] - cl.z));
-                    const T Wn = q.Wn[p];
                     v3<T> w, gx;
                     T sval;
                     if (dot(r, r) > fd * fd) {
@@ -194,60 +201,82 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
                         T ga;
                         sval = sv_far_vjp(S, r, m, gr, gd, ga);
                         w = sv_far(S, r);
-                        acc.Grf += Wn * gr;
-                        for (int k = 0; k < 3; ++k) acc.Gd[k] += Wn * gd[k];
-                        acc.A += Wn * ga;
+#pragma unroll
+                        for (int j = 0; j < K; ++j) {
+                            const T Wn = q.Wn[j][p];
+                            acc[j].Grf += Wn * gr;
+                            for (int k = 0; k < 3; ++k) acc[j].Gd[k] += Wn * gd[k];
+                            acc[j].A += Wn * ga;
+                        }
                         gx = gr;
                     } else {
                         v3<T> g0, g1, g2;
                         ExactShape<T> sh;
                         sval = sv_exact_vjp(S, r - S.d[0], r - S.d[1], r - S.d[2], r, m, 0, T(1e-12), g0, g1, g2, sh);
                         w = (sh.L[0] * S.nu[0] + sh.L[1] * S.nu[1] + sh.L[2] * S.nu[2] + sh.Om * S.n) * i4pi;
-                        acc.Gr[0] += Wn * g0;
-                        acc.Gr[1] += Wn * g1;
-                        acc.Gr[2] += Wn * g2;
-                        for (int e = 0; e < 3; ++e) {
-                            acc.Lm[e] += (Wn * sh.L[e]) * m;
-                            acc.Nm[e] += Wn * sh.dLdlen[e] * dot(S.nu[e], m);
+#pragma unroll
+                        for (int j = 0; j < K; ++j) {
+                            const T Wn = q.Wn[j][p];
+                            acc[j].Gr[0] += Wn * g0;
+                            acc[j].Gr[1] += Wn * g1;
+                            acc[j].Gr[2] += Wn * g2;
+                            for (int e = 0; e < 3; ++e) {
+                                acc[j].Lm[e] += (Wn * sh.L[e]) * m;
+                                acc[j].Nm[e] += Wn * sh.dLdlen[e] * dot(S.nu[e], m);
+                            }
+                            acc[j].Om += (Wn * sh.Om) * m;
                         }
-                        acc.Om += (Wn * sh.Om) * m;
                         gx = g0 + g1 + g2;
                     }
-                    acc.Gb += Wn * cross(w, nT);
-                    acc.Sb += Wn * dot(w, nT);
-                    for (int k = 0; k < 3; ++k) Xg[k] += (Wn * lam[p][k]) * gx;
-                    U += Wn * (cross(G, w) + sig * w);
-                    fs += Wn * sval;
+                    const v3<T> wxn = cross(w, nT), uw = cross(G, w) + sig * w;
+                    const T wn = dot(w, nT);
+#pragma unroll
+                    for (int j = 0; j < K; ++j) {
+                        const T Wn = q.Wn[j][p];
+                        acc[j].Gb += Wn * wxn;
+                        acc[j].Sb += Wn * wn;
+                        for (int k = 0; k < 3; ++k) Xg[j][k] += (Wn * lam[p][k]) * gx;
+                        U[j] += Wn * uw;
+                        fs[j] += Wn * sval;
+                    }
                 }
             }
             // the test side of this test: sum over the warp, then over the CTA's warps below
-            T v[NTA] = {Xg[0].x, Xg[0].y, Xg[0].z, Xg[1].x, Xg[1].y, Xg[1].z, Xg[2].x, Xg[2].y, Xg[2].z, U.x, U.y, U.z, fs};
-            if (__any_sync(0xffffffffu, far)) {
+            const bool anyfar = __any_sync(0xffffffffu, far);
 #pragma unroll
-                for (int k = 0; k < NTA; ++k)
+            for (int j = 0; j < K; ++j) {
+                T v[NTA] = {Xg[j][0].x, Xg[j][0].y, Xg[j][0].z, Xg[j][1].x, Xg[j][1].y, Xg[j][1].z,
+                            Xg[j][2].x, Xg[j][2].y, Xg[j][2].z, U[j].x,     U[j].y,     U[j].z,     fs[j]};
+                if (anyfar) {
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+                    for (int k = 0; k < NTA; ++k)
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+                }
+                if (lane == 0)
+#pragma unroll
+                    for (int k = 0; k < NTA; ++k) red[i][wid][j * NTA + k] = v[k];
             }
-            if (lane == 0)
-#pragma unroll
-                for (int k = 0; k < NTA; ++k) red[i][wid][k] = v[k];
         }
         __syncthreads();
-        for (int k = tid; k < TT * NTA; k += FAR_NT) {
-            const int i = k / NTA, f = k - i * NTA;
+        for (int k = tid; k < TT * K * NTA; k += FAR_NT) {
+            const int i = k / (K * NTA), jf = k - i * (K * NTA), j = jf / NTA, f = jf - j * NTA;
             if (ts[i].t < 0) continue;
             T v = T(0);
-            for (int w = 0; w < FAR_NT / 32; ++w) v += red[i][w][f];
-            if (v != T(0)) atomicAdd(a.TA + size_t(ts[i].t) * NTA + f, double(v));
+            for (int w = 0; w < FAR_NT / 32; ++w) v += red[i][w][jf];
+            if (v != T(0)) atomicAdd(a.TA[j] + size_t(ts[i].t) * NTA + f, double(v));
         }
     }
     if (sv) {
-        T f[NSA];
-        sa_flat(acc, f);
-        double* dst = a.SA[set] + size_t(s) * NSA;
 #pragma unroll
-        for (int k = 0; k < NSA; ++k)
-            if (f[k] != T(0)) atomicAdd(dst + k, double(f[k]));
+        for (int j = 0; j < K; ++j) {
+            T f[NSA];
+            sa_flat(acc[j], f);
+            double* dst = a.SA[j][set] + size_t(s) * NSA;
+#pragma unroll
+            for (int k = 0; k < NSA; ++k)
+                if (f[k] != T(0)) atomicAdd(dst + k, double(f[k]));
+        }
     }
 }
 
@@ -958,9 +987,10 @@ void fill_gam(const std::vector<TriGeo>& g, int n, const double* mu, int col0, i
         }
 }
 
-template <class T, int TT>
-int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const double* d_nu, const double* mu,
-                double* d_SA0, double* d_SA1, double* d_TA, DevList& dl) {
+// the far tier for the adjoint vectors x[0 .. K-1] in one launch
+template <class T, int TT, int K>
+int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const AdjExtra* x, const double* mu,
+                DevList& dl) {
     AdjFarArgs fa{};
     fa.ntest = in.ntri;
     fa.nq = ps.nq;
@@ -969,11 +999,13 @@ int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const dou
     fa.tw = ps.d_tw;
     fa.tgeo = ps.d_tg;
     fa.tcent = ps.d_tc;
-    fa.nu = d_nu;
+    for (int j = 0; j < K; ++j) {
+        fa.nu[j] = x[j].nu;
+        fa.SA[j][0] = x[j].SA[0];
+        fa.SA[j][1] = x[j].SA[1];
+        fa.TA[j] = x[j].TA;
+    }
     fa.nset = in.nwtri > 0 ? 2 : 1;
-    fa.SA[0] = d_SA0;
-    fa.SA[1] = d_SA1;
-    fa.TA = d_TA;
     fa.ratio32 = ps.ratio32;
     fa.ratio = in.o->far_ratio;
     fa.kernel_far = in.o->kernel_far;
@@ -1012,7 +1044,7 @@ int run_adj_far(vp_ctx* ctx, const PairSetup& ps, const PairInput& in, const dou
     fa.tiles_per_chunk = (fa.ntiles_test + chunks - 1) / chunks;
     chunks = (fa.ntiles_test + fa.tiles_per_chunk - 1) / fa.tiles_per_chunk;
     vp_phase_begin(ctx, PH_ADJ_FAR);
-    adj_far_kernel<T, TT><<<dim3(tiles, chunks), FAR_NT, 0, ctx->stream>>>(fa);
+    adj_far_kernel<T, TT, K><<<dim3(tiles, chunks), FAR_NT, 0, ctx->stream>>>(fa);
     vp_phase_end(ctx);
     ctx->launches++;
     VP_CUDA(ctx, cudaGetLastError());
@@ -1094,11 +1126,15 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     }
     vp_phase_end(ctx);
     // far tier, one launch per adjoint vector
-    for (int k = 0; k < nadj; ++k) {
-        const AdjExtra& ex = mx.x[k];
-        r = ps.mixed ? run_adj_far<float, 8>(ctx, ps, in, ex.nu, mu, ex.SA[0], ex.SA[1], ex.TA, dl)
-                     : run_adj_far<double, 4>(ctx, ps, in, ex.nu, mu, ex.SA[0], ex.SA[1], ex.TA, dl);
-        if (r) return r;
+    // (mixed: both vectors in one pass; FP64: a launch per vector, whose FP64 sums would not fit twice in registers)
+    if (ps.mixed && nadj == 2) {
+        if ((r = run_adj_far<float, 8, 2>(ctx, ps, in, mx.x, mu, dl))) return r;
+    } else {
+        for (int k = 0; k < nadj; ++k) {
+            r = ps.mixed ? run_adj_far<float, 8, 1>(ctx, ps, in, mx.x + k, mu, dl)
+                         : run_adj_far<double, 4, 1>(ctx, ps, in, mx.x + k, mu, dl);
+            if (r) return r;
+        }
     }
     // non-far pairs: the near tier one pair per lane (a launch per adjoint vector), then the rest with all vectors
     {
