@@ -34,6 +34,10 @@ METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|
 FLOP_FWD_POINT = 248
 FLOP_ADJ_EVAL = 620
 FLOP_ADJ_SUMS = 110
+# DRAM bytes per touching/contact point of the pair-parallel kernels, from ncu captures on the 28 x 14 per side wing
+# (115.3M such points): adj_pairs_kernel 0.38 GB read + 4.50 GB written, near_kernel_pairs 0.012 + 0.180 GB. It is
+# the per-lane accumulators' stack traffic, which grows with the points; the algorithmic bytes are a few MB.
+DRAM_PER_TOUCH_POINT = {"adj_pairs": 42.3, "near_pairs": 1.66}
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
 SIZES = {"wing25k": (112, 56), "medium": (56, 28), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
@@ -196,6 +200,17 @@ def dist_setup(n_gpus):
     return rank, world, local, None
 
 
+def max_over_ranks(vals, dist):
+    """each value's largest over the ranks (the slowest replica sets the step time); the values themselves on one rank"""
+    if not dist:
+        return [float(v) for v in vals]
+    import torch
+
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -242,16 +257,13 @@ def main():
             t0 = time.perf_counter()
             out = step(vp, w, wake, W, "mixed", ctx)
             walls.append(time.perf_counter() - t0)
+    if dist:
+        dist.barrier()
     phases, launches = ctx.phase_times(reset=True)
     h2d, d2h = ctx.transfer_bytes(reset=True)
     dev_s = sum(phases.values()) / 1e3 / args.steps
     e2e_s = sum(walls) / args.steps
-    if dist:
-        import torch
-
-        t = torch.tensor([dev_s, e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_s, e2e_s = float(t[0]), float(t[1])
+    dev_s, e2e_s = max_over_ranks([dev_s, e2e_s], dist)
     CL, CDi, stats, cond = out["CL"], out["CDi"], out["stats"], out["cond"]
     # the plain FP64 GPU path on the same workload
     fp = {}
@@ -277,37 +289,40 @@ def main():
     if rank != 0:
         return
     per = {k: v / args.steps for k, v in phases.items()}
-    # roofline of the dominant kernel: the pair integrals are FP32 CUDA-core bound; algorithmic flops per evaluated
-    # point (kernel evaluation + contraction) from the device's per-tier point counts
+    # roofline of every pair kernel and of the LU (algorithmic flops per evaluated point from the device's per-tier
+    # point counts, over the kernel's CUDA-event time on the library's stream); the dominant one is the headline
     pk, src = peaks()
-    dom = max(("far", "near", "lu", "adj_far", "adj_near"), key=lambda k: per[k])
     sm_max = pk.get("sm_max_mhz", 2070.0)
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal FP32 FMA rate at the max SM clock
     pts, apts = stats["points"], out["adjoint_points"]
-    nonfar = lambda p: sum(v for k, v in p.items() if k != "far")  # noqa: E731
-    if dom == "far":
-        roof = {"kernel": "far_kernel<float,8>", "bound": "fp32", "flops": pts["far"] * FLOP_FWD_POINT}
-    elif dom == "near":
-        roof = {"kernel": "near_kernel_lanes + near_kernel_pairs + near_kernel_rest", "bound": "fp32",
-                "flops": nonfar(pts) * FLOP_FWD_POINT}
-    elif dom == "adj_far":
-        roof = {"kernel": "adj_far_kernel<float,8> (x2)", "bound": "fp32",
-                "flops": 2 * apts["far"] * (FLOP_ADJ_EVAL + FLOP_ADJ_SUMS)}
-    elif dom == "adj_near":
-        # the near tier runs once per vector (adj_lanes_kernel x2), the touching and contact tiers once for both
-        near_pts = apts["near"]
-        roof = {"kernel": "adj_lanes_kernel x2 + adj_pairs_kernel + adj_near_kernel", "bound": "fp32",
-                "flops": 2 * near_pts * (FLOP_ADJ_EVAL + FLOP_ADJ_SUMS) +
-                (nonfar(apts) - near_pts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS)}
-    else:
-        n = w.dm.nq + 1
-        roof = {"kernel": "lu (cluster panels + sgemm)", "bound": "tensor", "flops": 2 / 3 * n ** 3}
-    roof["achieved"] = roof.pop("flops") / (per[dom] / 1e3) / 1e12
-    roof["peak"] = fp32_peak if roof["bound"] == "fp32" else pk.get("bf16_tflops", 1900.0)
-    roof["unit"] = "TFLOP/s"
+    touch = lambda p: sum(v for k, v in p.items() if k not in ("far", "near"))  # noqa: E731  self/edge/vertex/contact
+    n = w.dm.nq + 1
+    adj_pt = FLOP_ADJ_EVAL + FLOP_ADJ_SUMS
+    kern = {  # phase: (kernels, bound, flops, points)
+        "far": ("far_kernel<float,8>", "fp32", pts["far"] * FLOP_FWD_POINT, pts["far"]),
+        "near": ("near_kernel_lanes (+ near_kernel_rest)", "fp32", pts["near"] * FLOP_FWD_POINT, pts["near"]),
+        "near_pairs": ("near_kernel_pairs", "fp32", touch(pts) * FLOP_FWD_POINT, touch(pts)),
+        "adj_far": ("adj_far_kernel<float,8,2>", "fp32", apts["far"] * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), apts["far"]),
+        "adj_near": ("adj_lanes_kernel x2 (+ adj_near_kernel)", "fp32", 2 * apts["near"] * adj_pt, apts["near"]),
+        "adj_pairs": ("adj_pairs_kernel", "fp32", touch(apts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), touch(apts)),
+        "lu": ("lu (cluster panels + cuBLAS SGEMM, FP32 CUDA cores)", "fp32", 2 / 3 * n ** 3, None),
+    }
+    kernels = {}
+    for ph, (name, bound, flops, npts) in kern.items():
+        if per.get(ph, 0.0) <= 0:
+            continue
+        peak = fp32_peak if bound == "fp32" else pk.get("bf16_tflops", 1900.0)
+        ach = flops / (per[ph] / 1e3) / 1e12
+        kernels[ph] = {"kernel": name, "ms": per[ph], "achieved": ach, "frac": ach / peak}
+    dom = max(kernels, key=lambda k: per[k])
+    name, bound, flops, npts = kern[dom]
+    roof = {"kernel": name, "bound": bound, "achieved": kernels[dom]["achieved"],
+            "peak": fp32_peak if bound == "fp32" else pk.get("bf16_tflops", 1900.0), "unit": "TFLOP/s"}
     roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["peak_source"] = "nominal (152 SMs x 128 FP32 lanes x 2 x max SM clock)" if roof["bound"] == "fp32" else src
-    roof["traffic"] = None
+    roof["peak_source"] = "nominal (152 SMs x 128 FP32 lanes x 2 x max SM clock)" if bound == "fp32" else src
+    traffic = DRAM_PER_TOUCH_POINT.get(dom)
+    roof["traffic"] = traffic * npts if traffic is not None and npts else None
+    roof["traffic_unit"] = "B per launch (ncu, small wing, scaled by points)" if roof["traffic"] else None
     line = {"metric": METRIC, "value": dev_s, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": config,
@@ -317,7 +332,8 @@ def main():
             "CL": CL, "CDi": CDi, "cond": cond, "tiers": stats, "roofline": roof, "clocks": clk.summary(),
             "fp64_point_share": stats["points_fp64"] / max(1, sum(stats["points"].values())),
             "adjoint_points": out["adjoint_points"],
-            "adjoint_fp64_point_share": out["adjoint_points_fp64"] / max(1, sum(out["adjoint_points"].values()))}
+            "adjoint_fp64_point_share": out["adjoint_points_fp64"] / max(1, sum(out["adjoint_points"].values())),
+            "kernels": kernels}
     line.update(fp)
     line["nbody"] = nbody(vp, ctx)
     if not args.no_cpu_baseline:

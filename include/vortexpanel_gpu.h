@@ -128,8 +128,11 @@ int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const do
                double* dalpha, vp_assembly_stats* stats);
 
 /* Instrumentation (no counterpart in the reference, which only times with @elapsed): device milliseconds per phase
- * since the last reset, measured with CUDA events on the context's stream, in the order setup, classify, far, near,
- * reduce, lu, cond, solve, adjoint (n entries at most), and the number of this library's kernel launches. */
+ * since the last reset, measured with CUDA events on the context's stream, in the order setup, classify, far, near
+ * (near tier and the adding of the pair blocks), reduce, lu, cond, solve, adjoint setup, adjoint far, adjoint near
+ * (near tier, filaments, freestream), adjoint solve, free wake, near pairs (the touching and contact pairs of the
+ * assembly), adjoint pairs (those of the adjoint) (n entries at most), and the number of this library's kernel
+ * launches. */
 int vp_phase_times(vp_ctx* ctx, double* ms, int n, long long* launches, int reset);
 /* Instrumentation (no counterpart in the reference): bytes copied host->device and device->host by the library. */
 int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset);

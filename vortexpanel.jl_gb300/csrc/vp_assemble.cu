@@ -903,7 +903,11 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
                 na.pair_out = d_pairs;
                 if (nrest > 0) {
                     const int nb = persistent_blocks(ctx, near_kernel_pairs, 32 * NEAR_WARPS, 0);
+                    vp_phase_end(ctx);
+                    vp_phase_begin(ctx, PH_NEAR_PAIRS);
                     near_kernel_pairs<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+                    vp_phase_end(ctx);
+                    vp_phase_begin(ctx, PH_NEAR);
                     ctx->launches++;
                 }
             }

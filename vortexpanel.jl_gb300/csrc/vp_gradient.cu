@@ -1163,8 +1163,12 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         }
         na.stats = d_stats;
         if ((r = rest_list(ctx, dl, na, nullptr))) return r;
-        adj_pairs_kernel<<<persistent_blocks(ctx, adj_pairs_kernel, 32 * NEAR_WARPS, 0), 32 * NEAR_WARPS, 0,
-                           ctx->stream>>>(na, mx);
+        const int npb = persistent_blocks(ctx, adj_pairs_kernel, 32 * NEAR_WARPS, 0);
+        vp_phase_end(ctx);
+        vp_phase_begin(ctx, PH_ADJ_PAIRS);
+        adj_pairs_kernel<<<npb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
+        vp_phase_end(ctx);
+        vp_phase_begin(ctx, PH_ADJ_NEAR);
         adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
         vp_phase_end(ctx);
         ctx->launches += nadj + 2;

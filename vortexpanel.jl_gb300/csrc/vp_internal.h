@@ -23,6 +23,8 @@ enum {
     PH_ADJ_NEAR,    // adjoint non-far pairs, filaments, freestream
     PH_ADJ_SOLVE,   // transposed solve
     PH_WAKE,        // free wake: blob sums, body velocity, explicit right hand side of particles
+    PH_NEAR_PAIRS,  // near_kernel_pairs alone (the touching and contact pairs of the assembly)
+    PH_ADJ_PAIRS,   // adj_pairs_kernel alone (the touching and contact pairs of the adjoint)
     PH_COUNT
 };
 
