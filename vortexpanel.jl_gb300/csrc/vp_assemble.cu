@@ -436,7 +436,7 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
     return __ballot_sync(FULL, valid && !near);
 }
 
-// near tier, one pair per lane; the other pairs are listed for near_kernel_rest
+// near tier, one pair per lane; the other pairs are listed for near_kernel_pairs
 __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a) {
     extern __shared__ __align__(16) unsigned char near_smem[];
     NearChunkSh* shm = reinterpret_cast<NearChunkSh*>(near_smem);

@@ -297,7 +297,7 @@ struct AdjExtra {
 // near-tier pairs, one per lane: the plan of the assembly's lanes kernel (tiers and quadtree leaves), every leaf point
 // of a chunk of 32 pairs evaluated across the lanes (FP32 under the adjoint's guard, or queued for FP64), per-pair
 // segmented sums, and each lane finishing its own pair: the source side added to SA, the test side summed over the
-// warp once per test triangle. The pairs of the other tiers are listed for the warp-cooperative kernel.
+// warp once per test triangle. The pairs of the other tiers are listed for adj_pairs_kernel.
 
 constexpr int NSUM = 41;  // AdjSums: Q (3), Xg (9), Gr (9), Grf (3), Gd (9), L (3), N (3), O, A
 

@@ -1356,30 +1356,6 @@ __device__ int tri_pair(PairCtx& pc, Acc& acc, int t, int s, bool wake) {
     return TIER_NEAR;
 }
 
-__device__ void add_block(PairCtx& pc, FwdAcc& acc, const TriGeo& S, int col0, double* rbt, bool with_rhs) {
-    // reduce the per-lane sums, contract with n_T x gamma_b and add the block to this warp's rows
-    fold32(acc);
-    double P[9];
-    for (int a = 0; a < 3; ++a) {
-        P[3 * a + 0] = warp_sum(acc.P[a].x);
-        P[3 * a + 1] = warp_sum(acc.P[a].y);
-        P[3 * a + 2] = warp_sum(acc.P[a].z);
-    }
-    const TriGeo& T = *pc.T;
-    v3<double> nT = ld3(T.n);
-    if (pc.lane < 9) {
-        int ai = pc.lane / 3, bb = pc.lane % 3;
-        v3<double> m = cross(nT, ld3(S.gam + 3 * bb));
-        double v = P[3 * ai] * m.x + P[3 * ai + 1] * m.y + P[3 * ai + 2] * m.z;
-        double* dst = pc.a->A + size_t(T.slot[ai]) * size_t(pc.a->lda) + col0 + S.slot[bb];
-        *dst += v;
-    }
-    if (with_rhs)
-        for (int ai = 0; ai < 3; ++ai)
-            rbt[ai] -= S.sigma * (P[3 * ai] * nT.x + P[3 * ai + 1] * nT.y + P[3 * ai + 2] * nT.z);
-    __syncwarp();
-}
-
 // vertex_rule (assemble.jl:119-125) toward corner k of the whole test triangle
 template <class Acc>
 __device__ void vertex_rule(PairCtx& pc, Acc& acc, int k) {
