@@ -666,7 +666,10 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, 
         const TriGeo& T = a.tri[t];
         pc.T = &T;
         for (int k = 0; k < 3; ++k) {
-            for (int j = 0; j < ADJ_MAX; ++j) pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+            for (int j = 0; j < ADJ_MAX; ++j) {
+                pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+                pc.nukf[j][k] = float(pc.nuk[j][k]);
+            }
             pc.nu[k] = pc.nuk[0][k];
             pc.Xc[k] = ld3(T.x + 3 * k) - ld3(T.c);
             pc.Xcf[k] = mk3(float(pc.Xc[k].x), float(pc.Xc[k].y), float(pc.Xc[k].z));
@@ -800,7 +803,10 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
     pc.fp32 = 0;
     pc.nadj = K;
     for (int k = 0; k < 3; ++k) {
-        for (int j = 0; j < ADJ_MAX; ++j) pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+        for (int j = 0; j < ADJ_MAX; ++j) {
+            pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+            pc.nukf[j][k] = float(pc.nuk[j][k]);
+        }
         pc.nu[k] = pc.nuk[0][k];
         pc.Xc[k] = ld3(T.x + 3 * k) - ld3(T.c);
         pc.Xcf[k] = mk3(float(pc.Xc[k].x), float(pc.Xc[k].y), float(pc.Xc[k].z));

@@ -21,6 +21,7 @@ constexpr int NQMAX = 7;     // points of the far rule, at most
 constexpr int NFIELD = 42;   // scalar fields per source in the far kernel's SoA
 constexpr int NEAR_WARPS = 4;
 constexpr int LEAFBUF = 32;
+constexpr int ADJ_MAX = 2;  // adjoint vectors of one pass
 // FP32 guard of the adjoint's derivative evaluations (corner, edge sin^2, plane): the forward's (the derivatives keep
 // the accuracy of the values there: adjoint gradients within 3e-6 of the FP64 path's on the wings measured)
 #define ADJ_GUARD 1e-2f, 4e-2f, 1e-4f
@@ -348,6 +349,7 @@ struct NearArgs {
     int ntests;
     int test_mode, near_depth, mixed;
     double far_ratio, near_ratio, corner_angle, contact_rel, kernel_far;
+    float kernel_far32;  // kernel_far in FP32 (the FP32 point evaluators)
     double vinf[3];
     double tint[3];
     unsigned long long* stats;  // pairs[6], points[6], points evaluated in FP64
@@ -365,6 +367,7 @@ struct WarpSh {
     float D32[9];          // D in FP32
     float Sdf[9], Snf[3], Snuf[9], Slenf[3], Sareaf, Sdiamf;
     double leaf[LEAFBUF][10];
+    float leaff[LEAFBUF][10];  // the leaves in FP32: corners, and frac x the test triangle's area
     int qi[64], ql[64];    // points waiting for FP64: rule point, and leaf (-1: the current piece)
 };
 
@@ -479,6 +482,9 @@ struct PairCtx {
     double pfrac;
     double binv[9];
     double tb[10];
+    // FP32 copies, converted once (a conversion from FP64 runs on the FP64 pipe): nuk, and binv per piece
+    float nukf[ADJ_MAX][3];
+    float binvf[9];
     double gdir[2];
     v3<double> Xc[3];
     v3<float> Xcf[3];
@@ -552,7 +558,7 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float 
     v3<float> r = l0 * mk3(sh.D32[0], sh.D32[1], sh.D32[2]) + l1 * mk3(sh.D32[3], sh.D32[4], sh.D32[5]) +
                   l2 * mk3(sh.D32[6], sh.D32[7], sh.D32[8]);
     v3<float> w;
-    float fd = float(pc.a->kernel_far) * S.diam;
+    float fd = pc.a->kernel_far32 * S.diam;
     if (dot(r, r) > fd * fd) {
         w = sv_far(S, r);
     } else {
@@ -572,7 +578,6 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float 
 }
 
 // ---- adjoint accumulation of a pair (warp-cooperative path) --------------------------------------------------------
-constexpr int ADJ_MAX = 2;  // adjoint vectors of one pass
 
 struct AdjAcc {
     AdjSums<double> d[ADJ_MAX];  // FP64 sums, per adjoint vector
@@ -615,9 +620,9 @@ __device__ __forceinline__ void fold32(AdjAcc& acc) {
 
 // the rule-geometry sums of one point of a dependent piece: weight W, barycentrics l, value s = w·m, ds/dx
 template <class T>
-__device__ __forceinline__ void rule_point(const PairCtx& pc, const double* nu, T* Bb, T& Fb, T W, T l0, T l1, T l2,
-                                           T sv, v3<T> gx, const v3<T>* Xc) {
-    const T n0 = T(nu[0]), n1 = T(nu[1]), n2 = T(nu[2]);
+__device__ __forceinline__ void rule_point(const PairCtx& pc, const T* nu, const T* binv, T* Bb, T& Fb, T W, T l0, T l1,
+                                           T l2, T sv, v3<T> gx, const v3<T>* Xc) {
+    const T n0 = nu[0], n1 = nu[1], n2 = nu[2];
     const bool hat = pc.a->test_mode == 0;
     const T nul = hat ? n0 * l0 + n1 * l1 + n2 * l2 : (pc.a->test_mode == 1 ? n0 + n1 + n2 : T(0));
     T dphi[3];
@@ -626,7 +631,7 @@ __device__ __forceinline__ void rule_point(const PairCtx& pc, const double* nu, 
     dphi[2] = (hat ? n2 * sv : T(0)) + nul * dot(gx, Xc[2]);
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
-        const T bj = W * (T(pc.binv[3 * j]) * l0 + T(pc.binv[3 * j + 1]) * l1 + T(pc.binv[3 * j + 2]) * l2);
+        const T bj = W * (binv[3 * j] * l0 + binv[3 * j + 1] * l1 + binv[3 * j + 2] * l2);
         Bb[3 * j] += bj * dphi[0];
         Bb[3 * j + 1] += bj * dphi[1];
         Bb[3 * j + 2] += bj * dphi[2];
@@ -699,7 +704,8 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAcc& acc, double
         }
     }
     if (pc.dep)
-        for (int k = 0; k < pc.nadj; ++k) rule_point(pc, pc.nuk[k], acc.Bb[k], acc.Fb[k], W, l0, l1, l2, sv, gx, pc.Xc);
+        for (int k = 0; k < pc.nadj; ++k)
+            rule_point(pc, pc.nuk[k], pc.binv, acc.Bb[k], acc.Fb[k], W, l0, l1, l2, sv, gx, pc.Xc);
 }
 
 // one point in FP32 under the guard, adjoint; false when it must be evaluated in FP64
@@ -712,8 +718,8 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
     v3<float> psi = pc.a->test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);
     float Wn[ADJ_MAX];
     for (int k = 0; k < ADJ_MAX; ++k)
-        Wn[k] = W * (float(pc.nuk[k][0]) * psi.x + float(pc.nuk[k][1]) * psi.y + float(pc.nuk[k][2]) * psi.z);
-    float fd = float(pc.a->kernel_far) * S.diam;
+        Wn[k] = W * (pc.nukf[k][0] * psi.x + pc.nukf[k][1] * psi.y + pc.nukf[k][2] * psi.z);
+    float fd = pc.a->kernel_far32 * S.diam;
     v3<float> gx;
     float sv;
     if (dot(r, r) > fd * fd) {
@@ -731,7 +737,7 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
     }
     if (pc.dep)
         for (int k = 0; k < pc.nadj; ++k)
-            rule_point(pc, pc.nuk[k], acc.Bbf[k], acc.Fbf[k], W, l0, l1, l2, sv, gx, pc.Xcf);
+            rule_point(pc, pc.nukf[k], pc.binvf, acc.Bbf[k], acc.Fbf[k], W, l0, l1, l2, sv, gx, pc.Xcf);
     if (++acc.nf == 16) fold32(acc);
     return true;
 }
@@ -861,10 +867,7 @@ __device__ __noinline__ void flush_leaves(PairCtx& pc, Acc& acc) {
         bool valid = i < nl * n;
         int lf = valid ? i / n : 0, q = valid ? i - lf * n : 0;
         const double* b = pc.sh->leaf[lf];
-        float bf[10];
-        for (int z = 0; z < 9; ++z) bf[z] = float(b[z]);
-        bf[9] = float(b[9] * pc.T->area);
-        point_step(pc, acc, valid, R_NEAR, q, lf, b, bf, b[9]);
+        point_step(pc, acc, valid, R_NEAR, q, lf, b, pc.sh->leaff[lf], b[9]);
         if (pc.nq64 >= 32) drain64(pc, acc, false, R_NEAR, nullptr, 0.0);
     }
     drain64(pc, acc, true, R_NEAR, nullptr, 0.0);
@@ -877,8 +880,12 @@ __device__ __noinline__ void flush_leaves(PairCtx& pc, Acc& acc) {
 template <class Acc>
 __device__ void emit_leaf(PairCtx& pc, Acc& acc, const double* b, double frac) {
     if (pc.lane == 0) {
-        for (int k = 0; k < 9; ++k) pc.sh->leaf[pc.nleaf][k] = b[k];
+        for (int k = 0; k < 9; ++k) {
+            pc.sh->leaf[pc.nleaf][k] = b[k];
+            pc.sh->leaff[pc.nleaf][k] = float(b[k]);
+        }
         pc.sh->leaf[pc.nleaf][9] = frac;
+        pc.sh->leaff[pc.nleaf][9] = float(frac * pc.T->area);
     }
     pc.nleaf++;
     if (pc.nleaf == LEAFBUF) flush_leaves(pc, acc);
@@ -918,6 +925,7 @@ __device__ void piece_begin(PairCtx& pc, AdjAcc& acc, const double* c, double fr
     pc.binv[6] = C * id;
     pc.binv[7] = -(a * h - b * g) * id;
     pc.binv[8] = (a * e - b * d) * id;
+    for (int k = 0; k < 9; ++k) pc.binvf[k] = float(pc.binv[k]);
 }
 
 __device__ void piece_end(PairCtx& pc, AdjAcc& acc) {
@@ -2044,6 +2052,7 @@ NearArgs near_args(const PairSetup& ps, const PairInput& in) {
     na.corner_angle = o->corner_angle;
     na.contact_rel = o->contact_rel;
     na.kernel_far = o->kernel_far;
+    na.kernel_far32 = float(o->kernel_far);
     for (int k = 0; k < 3; ++k) {
         na.vinf[k] = in.vinf[k];
         na.tint[k] = o->test == 1 ? 1.0 : 1.0 / 3;
