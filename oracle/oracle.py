@@ -345,6 +345,41 @@ def elements(g):
     return dict(n=n, area=A2 / 2, centroid=(a + b + c) / 3, gradl=gradl, gam=gam)
 
 
+def surface_velocity(g, dm, sigma, mu, V, wake=None, mu_wake=None, kernel_far=10.0):
+    """Velocity on the fluid side at every centroid from the singularities (Post.jl:32-64): V∞ + Σ σ_s w_s + γ_s × w_s
+    with the own sheet at side 1, plus the wake's sheets (Post.jl:49-51) and tip filaments (Post.jl:52-55).
+    Scalar loops over (point, source): small meshes only."""
+    els = elements(g)
+    V = np.asarray(V, float)
+    m = np.asarray(mu)[dm.corner_slot]
+    gam = sum(m[:, k:k + 1] * els["gam"][k] for k in range(3))
+    X = g.x[g.tris]
+    wsheets, wfil = [], []
+    if wake is not None:
+        mw = np.asarray(mu_wake, float)
+        for t in wake.tris:
+            a, b, c = wake.x[t[0]], wake.x[t[1]], wake.x[t[2]]
+            A2 = np.linalg.norm(np.cross(b - a, c - a))
+            e = [c - b, a - c, b - a]
+            wsheets.append((a, b, c, sum(mw[t[k]] * (-e[k] / A2) for k in range(3))))
+        for fa, fb in wake.filaments:
+            wfil.append((wake.x[fa], wake.x[fb], mw[fa], mw[fb]))
+    u = np.zeros((g.ntri, 3))
+    for t in range(g.ntri):
+        x = els["centroid"][t]
+        acc = V.copy()
+        for s in range(g.ntri):
+            w = source_velocity(X[s, 0], X[s, 1], X[s, 2], x, side=1 if s == t else 0, far=kernel_far)
+            acc += sigma[s] * w + np.cross(gam[s], w)
+        for a, b, c, gw in wsheets:
+            acc += np.cross(gw, source_velocity(a, b, c, x, far=kernel_far))
+        for a, b, ma, mb in wfil:
+            va, vb = segment_velocity(a, b, x)
+            acc += ma * va + mb * vb
+        u[t] = acc
+    return u
+
+
 def gradient_velocity(g, dm, mu, V, els=None):
     """V - (V.n)n + grad mu per triangle (Post.jl:72-73)"""
     els = els or elements(g)

@@ -1,5 +1,5 @@
 """The oracle pinned to the reference's known answers (CPU, no GPU): the quadrature rules
-(test/elements/test_elements.jl:8-47), the sphere's exact doublet and the system diagnostics
+(test/elements/test_elements.jl:8-47), the sphere's exact doublet, its surface velocity and the system diagnostics
 (test/assembly/test_sphere.jl:34-55), the Carlson integrals of the ellipsoid (test/assembly/test_ellipsoid.jl:30-33),
 and the Kutta-Joukowski and Trefftz loads of an elliptic loading (test/post/test_forces.jl:25-49). The reference
 stores no golden arrays; these are the values and bounds its own tests assert."""
@@ -82,6 +82,23 @@ def test_sphere_exact_doublet(oracle, sphere2):
     c = els["centroid"] / np.linalg.norm(els["centroid"], axis=1)[:, None]
     cpex = 1 - 9 / 4 * (1 - (c @ V) ** 2)
     assert math.sqrt(np.sum(els["area"] * (cp - cpex) ** 2) / np.sum(els["area"])) < 0.025
+
+
+def test_sphere_surface_velocity(oracle, sphere2):
+    # the two velocity routes agree and the leak is O(h) (test_sphere.jl:19-32,40): singularity sums at the centroids
+    # (Post.jl:32-64) against the doublet gradient
+    g, dm, V, A, b, stats, sol = sphere2
+    els = oracle.elements(g)
+    u = oracle.surface_velocity(g, dm, oracle.source_strengths(g, V), sol["mu"], V)
+    ug = oracle.gradient_velocity(g, dm, sol["mu"], V, els=els)
+    n = els["n"]
+    rms = lambda v: math.sqrt(np.sum(els["area"] * v ** 2) / np.sum(els["area"]))  # noqa: E731
+    c = els["centroid"] / np.linalg.norm(els["centroid"], axis=1)[:, None]
+    cpex = 1 - 9 / 4 * (1 - (c @ V) ** 2)
+    assert rms(oracle.pressure_coefficient(u, V) - cpex) < 0.08
+    tang = u - np.einsum("ij,ij->i", u, n)[:, None] * n
+    assert np.linalg.norm(tang - ug, axis=1).max() < 0.05
+    assert rms(np.einsum("ij,ij->i", u, n)) < 0.045
 
 
 def test_sphere_system_diagnostics(oracle, sphere2):

@@ -80,13 +80,15 @@ def _ip(a):
 
 @dataclass
 class Elements:
-    """The FlatTriangle fields of every triangle, as arrays: n, area, centroid, diam, gradλ (3 x ntri x 3), γ"""
+    """The FlatTriangle fields of every triangle, as arrays: n, area, centroid, diam, gradλ (3 x ntri x 3), γ, and the
+    corners (ntri x 9)"""
     n: np.ndarray
     area: np.ndarray
     centroid: np.ndarray
     diam: np.ndarray
     gradl: list
     gam: list
+    corners: np.ndarray = None
 
 
 def build_elements(g) -> Elements:
@@ -100,7 +102,7 @@ def build_elements(g) -> Elements:
     e = [c - b, a - c, b - a]
     diam = np.maximum.reduce([np.linalg.norm(b - a, axis=1), np.linalg.norm(c - b, axis=1), np.linalg.norm(a - c, axis=1)])
     return Elements(n, A2 / 2, (a + b + c) / 3, diam, [np.cross(n, ek) / A2[:, None] for ek in e],
-                    [-ek / A2[:, None] for ek in e])
+                    [-ek / A2[:, None] for ek in e], np.ascontiguousarray(np.concatenate([a, b, c], axis=1)))
 
 
 def source_strengths(els: Elements, V, V_body=None) -> np.ndarray:
@@ -270,6 +272,68 @@ def solve_galerkin(*args, W=None, precision=None, ctx=None):
 
 def element_values(dm, mu):
     return np.asarray(mu)[dm.corner_slot]
+
+
+def sheet_strengths(els: Elements, dm, mu):
+    """γ = Σ_b μ_b γ_b of every triangle (Post.jl:19-23)"""
+    m = element_values(dm, mu)
+    return sum(m[:, k:k + 1] * els.gam[k] for k in range(3))
+
+
+def _sheet_velocity(ctx, precision, corners, sigma, gamma, X, kernel_far):
+    """Σ σ_s w_s + γ_s × w_s of the triangles (corners n x 9) at the points X, on the GPU (vp_body_velocity)"""
+    c = np.ascontiguousarray(corners, dtype=np.float64)
+    sg = np.ascontiguousarray(sigma, dtype=np.float64)
+    gm = np.ascontiguousarray(gamma, dtype=np.float64)
+    x = np.ascontiguousarray(X, dtype=np.float64)
+    U = np.zeros_like(x)
+    prec = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}[precision]
+    check(ctx.h, load().vp_body_velocity(ctx.h, prec, len(c), c.ctypes.data_as(D), sg.ctypes.data_as(D),
+                                        gm.ctypes.data_as(D), kernel_far, len(x), x.ctypes.data_as(D),
+                                        U.ctypes.data_as(D)))
+    return U
+
+
+def surface_velocity(els: Elements, dm, sigma, mu, V, wake=None, mu_wake=None, kernel_far=10.0, precision="fp64",
+                     ctx=None):
+    """Velocity on the fluid side at every triangle's centroid from the singularities (Post.jl:32-64):
+    V∞ + Σ σ_s w_s + Σ γ_s × w_s, the triangle's own sheet taken on the side its normal points to, plus, with a
+    `wake` and the doublets of its nodes `mu_wake` (W q), the wake's sheets and tip filaments. The sums run on the
+    GPU: the sheets through vp_body_velocity, which takes every sheet at side 0 (at its own centroid, in its plane);
+    the side-1 limit of the own sheet adds ½σn + ½γ × n. The filaments go through vp_eval_points (mode 2, one
+    evaluation per centroid and filament)."""
+    ctx = ctx or default_context()
+    V = np.asarray(V, float)
+    sigma = np.asarray(sigma, float)
+    gam = sheet_strengths(els, dm, mu)
+    X = els.centroid
+    u = V + _sheet_velocity(ctx, precision, els.corners, sigma, gam, X, kernel_far)
+    u += 0.5 * (sigma[:, None] * els.n + np.cross(gam, els.n))
+    if wake is not None:
+        if mu_wake is None:
+            raise ValueError("surface_velocity with a wake needs mu_wake, the doublets of its nodes")
+        mw = np.asarray(mu_wake, float)
+        if len(wake.tris):
+            wc = wake.x[wake.tris]  # (nwtri, 3, 3)
+            wa, wb, wcc = wc[:, 0], wc[:, 1], wc[:, 2]
+            A2 = np.linalg.norm(np.cross(wb - wa, wcc - wa), axis=1)[:, None]
+            e = [wcc - wb, wa - wcc, wb - wa]
+            gw = sum(mw[wake.tris[:, k]][:, None] * (-e[k] / A2) for k in range(3))
+            u += _sheet_velocity(ctx, precision, wc.reshape(-1, 9), np.zeros(len(wc)), gw, X, kernel_far)
+        if len(wake.filaments):
+            nt, nf = len(X), len(wake.filaments)
+            fa, fb = wake.x[wake.filaments[:, 0]], wake.x[wake.filaments[:, 1]]
+            rows = np.zeros((nf, 9))
+            rows[:, 0:3], rows[:, 3:6] = fa, fb
+            rows[:, 6], rows[:, 7] = mw[wake.filaments[:, 0]], mw[wake.filaments[:, 1]]
+            rows = np.tile(rows, (nt, 1))
+            xs = np.repeat(X, nf, axis=0)
+            for k in range(3):
+                m = np.zeros((nt * nf, 3))
+                m[:, k] = 1.0
+                s = eval_points(2, rows, xs, m, precision=precision, ctx=ctx)[:, 0]
+                u[:, k] += s.reshape(nt, nf).sum(axis=1)
+    return u
 
 
 def gradient_velocity(els: Elements, dm, mu, V):
