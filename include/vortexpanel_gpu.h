@@ -147,8 +147,12 @@ int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset);
 int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const double* tri, const double* x, const double* m,
                    int side, double kernel_far, double* out);
 
-/* No counterpart in the reference. vp_eval_points with no device allocation: inputs and outputs are staged through
- * a fixed device array of VP_STATIC_POINTS_MAX points (about 0.45 MB); n above that returns VP_ERR_ARG. The array's
+/* No counterpart in the reference. vp_eval_points with no device allocation, for callers that cannot allocate device
+ * memory while they run: a host that keeps the device's memory in a pool of its own (Julia's CUDA.jl, a framework's
+ * caching allocator) and leaves little outside it, or a stepping loop that cannot afford cudaMalloc/cudaFree, which
+ * synchronise the device. Inputs and outputs are staged through a fixed device array of VP_STATIC_POINTS_MAX points
+ * (about 0.45 MB, held by every device that loads the library until the process exits); n above that returns
+ * VP_ERR_ARG. The array's
  * address is looked up on the first call for each device, which must come before any stream capture on that device.
  * Calls that overlap in time on one device share the array and race: serialise them. */
 #define VP_STATIC_POINTS_MAX 2048

@@ -1,6 +1,7 @@
-"""vp_eval_points_static (the allocation-free variant of vp_eval_points, staging through a fixed device array)
-against vp_eval_points on the same inputs: two calls in a row with different inputs and modes, so that nothing left
-in the array from one call reaches the next, and the size limit."""
+"""vp_eval_points_static, the variant of vp_eval_points for callers that cannot allocate device memory while they run
+(a host whose memory sits in its own pool, a loop that cannot afford cudaMalloc's synchronisation). It stages through a
+fixed device array. It is checked against vp_eval_points on the same inputs: two calls in a row with different inputs
+and modes, so that nothing left in the array from one call reaches the next, and the size limit."""
 import numpy as np
 import pytest
 

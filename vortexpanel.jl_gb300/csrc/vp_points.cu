@@ -127,12 +127,14 @@ extern "C" int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const
 }
 
 // ---------------------------------------------------------------------------------------------------------------------
-// vp_eval_points_static: the same evaluation as vp_eval_points with no device allocation. Inputs and outputs are
-// staged through one file-scope device array sized for VP_STATIC_POINTS_MAX points; its address is looked up once per
-// device with cudaGetSymbolAddress on the first call for that device, so that first call has to be made before any
-// stream capture on the device. Calls that overlap in time on one device (from two streams or two host threads) share
-// the array and race: the caller serialises them. No part of the array has to start at zero: points_kernel writes
-// every output slot of the n points it is given, and the inputs are copied in before the launch.
+// vp_eval_points_static: the same evaluation as vp_eval_points with no device allocation, for callers that cannot
+// allocate while they run (a host whose device memory sits in its own pool, a loop that cannot afford the device
+// synchronisation of cudaMalloc/cudaFree). Inputs and outputs are staged through one file-scope device array sized
+// for VP_STATIC_POINTS_MAX points; its address is looked up once per device with cudaGetSymbolAddress on the first
+// call for that device, so that first call has to be made before any stream capture on the device. Calls that
+// overlap in time on one device (from two streams or two host threads) share the array and race: the caller
+// serialises them. No part of the array has to start at zero: points_kernel writes every output slot of the n points
+// it is given, and the inputs are copied in before the launch.
 namespace {
 
 constexpr size_t kStaticTri = size_t(9) * VP_STATIC_POINTS_MAX;   // triangle (or filament) rows
