@@ -200,6 +200,45 @@ def dist_setup(n_gpus):
     return rank, world, local, None
 
 
+def rooflines(per, points, adjoint_points, n, pk_src):
+    """The achieved FLOP/s of every pair kernel and of the LU (n: the bordered system's order), each over its own
+    CUDA-event phase (per: ms per step), and the roofline object of the dominant one"""
+    # roofline of every pair kernel and of the LU (algorithmic flops per evaluated point from the device's per-tier
+    # point counts, over the kernel's CUDA-event time on the library's stream); the dominant one is the headline
+    pk, src = pk_src
+    sm_max = pk.get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal FP32 FMA rate at the max SM clock
+    pts, apts = points, adjoint_points
+    touch = lambda p: sum(v for k, v in p.items() if k not in ("far", "near"))  # noqa: E731  self/edge/vertex/contact
+    adj_pt = FLOP_ADJ_EVAL + FLOP_ADJ_SUMS
+    kern = {  # phase: (kernels, bound, flops, points)
+        "far": ("far_kernel<float,8>", "fp32", pts["far"] * FLOP_FWD_POINT, pts["far"]),
+        "near": ("near_kernel_lanes (+ near_kernel_rest)", "fp32", pts["near"] * FLOP_FWD_POINT, pts["near"]),
+        "near_pairs": ("near_kernel_pairs", "fp32", touch(pts) * FLOP_FWD_POINT, touch(pts)),
+        "adj_far": ("adj_far_kernel<float,8,2>", "fp32", apts["far"] * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), apts["far"]),
+        "adj_near": ("adj_lanes_kernel x2 (+ adj_near_kernel)", "fp32", 2 * apts["near"] * adj_pt, apts["near"]),
+        "adj_pairs": ("adj_pairs_kernel", "fp32", touch(apts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), touch(apts)),
+        "lu": ("lu (cluster panels + cuBLAS SGEMM, FP32 CUDA cores)", "fp32", 2 / 3 * n ** 3, None),
+    }
+    kernels = {}
+    for ph, (name, bound, flops, npts) in kern.items():
+        if per.get(ph, 0.0) <= 0:
+            continue
+        peak = fp32_peak if bound == "fp32" else pk.get("bf16_tflops", 1900.0)
+        ach = flops / (per[ph] / 1e3) / 1e12
+        kernels[ph] = {"kernel": name, "ms": per[ph], "achieved": ach, "frac": ach / peak}
+    dom = max(kernels, key=lambda k: per[k])
+    name, bound, flops, npts = kern[dom]
+    roof = {"kernel": name, "bound": bound, "achieved": kernels[dom]["achieved"],
+            "peak": fp32_peak if bound == "fp32" else pk.get("bf16_tflops", 1900.0), "unit": "TFLOP/s"}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["peak_source"] = "nominal (152 SMs x 128 FP32 lanes x 2 x max SM clock)" if bound == "fp32" else src
+    traffic = DRAM_PER_TOUCH_POINT.get(dom)
+    roof["traffic"] = traffic * npts if traffic is not None and npts else None
+    roof["traffic_unit"] = "B per launch (ncu, small wing, scaled by points)" if roof["traffic"] else None
+    return kernels, roof
+
+
 def max_over_ranks(vals, dist):
     """each value's largest over the ranks (the slowest replica sets the step time); the values themselves on one rank"""
     if not dist:
@@ -289,40 +328,7 @@ def main():
     if rank != 0:
         return
     per = {k: v / args.steps for k, v in phases.items()}
-    # roofline of every pair kernel and of the LU (algorithmic flops per evaluated point from the device's per-tier
-    # point counts, over the kernel's CUDA-event time on the library's stream); the dominant one is the headline
-    pk, src = peaks()
-    sm_max = pk.get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal FP32 FMA rate at the max SM clock
-    pts, apts = stats["points"], out["adjoint_points"]
-    touch = lambda p: sum(v for k, v in p.items() if k not in ("far", "near"))  # noqa: E731  self/edge/vertex/contact
-    n = w.dm.nq + 1
-    adj_pt = FLOP_ADJ_EVAL + FLOP_ADJ_SUMS
-    kern = {  # phase: (kernels, bound, flops, points)
-        "far": ("far_kernel<float,8>", "fp32", pts["far"] * FLOP_FWD_POINT, pts["far"]),
-        "near": ("near_kernel_lanes (+ near_kernel_rest)", "fp32", pts["near"] * FLOP_FWD_POINT, pts["near"]),
-        "near_pairs": ("near_kernel_pairs", "fp32", touch(pts) * FLOP_FWD_POINT, touch(pts)),
-        "adj_far": ("adj_far_kernel<float,8,2>", "fp32", apts["far"] * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), apts["far"]),
-        "adj_near": ("adj_lanes_kernel x2 (+ adj_near_kernel)", "fp32", 2 * apts["near"] * adj_pt, apts["near"]),
-        "adj_pairs": ("adj_pairs_kernel", "fp32", touch(apts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), touch(apts)),
-        "lu": ("lu (cluster panels + cuBLAS SGEMM, FP32 CUDA cores)", "fp32", 2 / 3 * n ** 3, None),
-    }
-    kernels = {}
-    for ph, (name, bound, flops, npts) in kern.items():
-        if per.get(ph, 0.0) <= 0:
-            continue
-        peak = fp32_peak if bound == "fp32" else pk.get("bf16_tflops", 1900.0)
-        ach = flops / (per[ph] / 1e3) / 1e12
-        kernels[ph] = {"kernel": name, "ms": per[ph], "achieved": ach, "frac": ach / peak}
-    dom = max(kernels, key=lambda k: per[k])
-    name, bound, flops, npts = kern[dom]
-    roof = {"kernel": name, "bound": bound, "achieved": kernels[dom]["achieved"],
-            "peak": fp32_peak if bound == "fp32" else pk.get("bf16_tflops", 1900.0), "unit": "TFLOP/s"}
-    roof["frac"] = roof["achieved"] / roof["peak"]
-    roof["peak_source"] = "nominal (152 SMs x 128 FP32 lanes x 2 x max SM clock)" if bound == "fp32" else src
-    traffic = DRAM_PER_TOUCH_POINT.get(dom)
-    roof["traffic"] = traffic * npts if traffic is not None and npts else None
-    roof["traffic_unit"] = "B per launch (ncu, small wing, scaled by points)" if roof["traffic"] else None
+    kernels, roof = rooflines(per, stats["points"], out["adjoint_points"], w.dm.nq + 1, peaks())
     line = {"metric": METRIC, "value": dev_s, "unit": "s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_s * 1e3, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic", "config": config,
