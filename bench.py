@@ -266,7 +266,8 @@ def main():
     config = {"workload": f"wing AR{ASPECT:g} NACA0012 {NCHORD}x{NSPAN}/side ({w.g.ntri} tris, {w.dm.nq} unknowns), "
                           f"rigid wake {len(wake.tris)} tris + {len(wake.filaments)} filaments, alpha {ALPHA:g} deg",
               "ntri": w.g.ntri, "nq": w.dm.nq, "nwake_nodes": wake.nwake, "precision": "mixed",
-              "l2": f"inputs larger than L2 (A is {8 * w.dm.nslot * (w.dm.nslot + wake.nwake) / 1e9:.2f} GB FP64)",
+              "l2": ("inputs larger than L2" if 8 * w.dm.nslot * (w.dm.nslot + wake.nwake) > 129e6 else "inputs within L2") +
+                    f" (A is {8 * w.dm.nslot * (w.dm.nslot + wake.nwake) / 1e9:.2f} GB FP64)",
               "parallelism": f"replicas x{world}"}
 
     if args.impl == "reference":
