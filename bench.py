@@ -149,10 +149,11 @@ def nbody(vp, ctx, n=400_000, reps=3):
                          "unit": "TFLOP/s", "frac": ach / peak, "peak_source": "nominal"}}
 
 
-def cpu_baseline(w, wake, W, V, budget_s=20.0):
+def cpu_baseline(w, wake, W, V, budget_s=20.0, rows=None):
     """The oracle (C++ restatement of the reference's assembly, OpenMP over test triangles as assemble.jl:395, and the
     reference's LAPACK dgetrf/dgetrs through scipy) on a bounded sample: the rows of a slice of test triangles, and
-    the LU of a leading principal block; scaled to the full step (rows linearly, the LU by n^3)."""
+    the LU of a leading principal block; scaled to the full step (rows linearly, the LU by n^3). The slice grows
+    until it takes about budget_s / 4, unless `rows` fixes it (the returned "rows" of an earlier sample)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     import scipy.linalg as sla
@@ -165,12 +166,13 @@ def cpu_baseline(w, wake, W, V, budget_s=20.0):
     nt = w.g.ntri
     cores = os.cpu_count() or 1
     # assembly: grow the slice until it takes a measurable time
-    rows = max(8, nt // 2000)
+    fixed = rows is not None
+    rows = rows if fixed else max(8, nt // 2000)
     while True:
         t0 = time.perf_counter()
         oracle.assemble(w.g, w.dm, sig, V, wake=wake, rows=(nt // 2, nt // 2 + rows), nthreads=cores)
         ta = time.perf_counter() - t0
-        if ta > budget_s / 4 or rows >= nt // 4:
+        if fixed or ta > budget_s / 4 or rows >= nt // 4:
             break
         rows = min(nt // 4, int(rows * max(2.0, (budget_s / 4) / max(ta, 1e-3))))
     t_asm = ta * nt / rows
@@ -185,7 +187,7 @@ def cpu_baseline(w, wake, W, V, budget_s=20.0):
     return {"value": t_asm + t_lu, "unit": "s", "cores": cores, "kind": "port",
             "sample": f"oracle assembly of {rows} of {nt} test-triangle rows ({ta:.1f} s, scaled x{nt / rows:.0f}) + "
                       f"scipy/LAPACK dgetrf of a {m}x{m} block ({tl:.2f} s, scaled by (n/m)^3 to n={n})",
-            "assembly_s": t_asm, "lu_s": t_lu}
+            "assembly_s": t_asm, "lu_s": t_lu, "rows": rows}
 
 
 def dist_setup(n_gpus):
@@ -273,9 +275,15 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
+        # W untimed samples (the first sizes the slice), then K timed ones; each is a bounded sample of the step
         cb = cpu_baseline(w, wake, W, V)
-        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": world, "steps": 1, "warmup": 0,
-                "ms_per_step": cb["value"] * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        for _ in range(max(0, args.warmup - 1)):
+            cpu_baseline(w, wake, W, V, rows=cb["rows"])
+        runs = [cpu_baseline(w, wake, W, V, rows=cb["rows"]) for _ in range(max(1, args.steps))]
+        cb = dict(runs[-1], value=statistics.mean(r["value"] for r in runs))
+        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": world, "steps": len(runs),
+                "warmup": max(1, args.warmup), "ms_per_step": cb["value"] * 1e3, "higher_is_better": False,
+                "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
                 "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
