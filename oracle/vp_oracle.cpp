@@ -324,7 +324,7 @@ static void vertex_pieces(Rule& out, const Vec p[3], int k, const Rule& base, co
         append_piece(out, base, Corners{b[k], b[i], b[j]}, frac);
         return;
     }
-    int m = int(std::ceil(th * 180.0 / M_PI / corner_angle));
+    int m = int(std::ceil(th * (180.0 / M_PI) / corner_angle));  // rad2deg(θ) = θ * (180 / π), as Julia rounds it
     std::vector<double> ts(m + 1);
     ts[0] = 0;
     ts[m] = 1;

@@ -1048,7 +1048,7 @@ __device__ __noinline__ void vertex_pieces(PairCtx& pc, Acc& acc, const v3<doubl
         if constexpr (kAdj<Acc>) piece_end(pc, acc);
         return;
     }
-    int m = int(ceil(th * 180.0 / vp_pi<double>() / pc.a->corner_angle));
+    int m = int(ceil(th * (180.0 / vp_pi<double>()) / pc.a->corner_angle));  // rad2deg(θ) = θ * (180 / π), as Julia
     double nu = vnorm(u), nv = vnorm(v);
     double t0 = 0;
     // adjoint: tangents of the split parameters
