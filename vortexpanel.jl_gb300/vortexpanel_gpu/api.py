@@ -148,11 +148,49 @@ class DeviceSystem:
             self.h = None
 
 
+def radon7():
+    """The 7-point degree-5 triangle rule of Radon (rules.jl:76-92, n = 7): barycentrics (7 x 3), weights (sum 1)"""
+    s = math.sqrt(15.0)
+    a, b = (6 - s) / 21, (6 + s) / 21
+    lam = [(1 / 3, 1 / 3, 1 / 3)]
+    for p in (a, b):
+        lam += [(1 - 2 * p, p, p), (p, 1 - 2 * p, p), (p, p, 1 - 2 * p)]
+    w = [9 / 40] + [(155 - s) / 1200] * 3 + [(155 + s) / 1200] * 3
+    return np.array(lam), np.array(w)
+
+
+def test_weights(test, lam):
+    """ψ at barycentrics lam (n x 3) (assemble.jl:52-58): hat λ, onering 1, dual the indicator of the largest λ
+    (ties shared)"""
+    lam = np.asarray(lam, float)
+    if test == "hat":
+        return lam.copy()
+    if test == "onering":
+        return np.ones_like(lam)
+    if test == "dual":
+        ind = (np.abs(lam - lam.max(axis=1, keepdims=True)) < 1e-12).astype(float)
+        return ind / ind.sum(axis=1, keepdims=True)
+    raise ValueError(f"test must be :hat, :onering or :dual, not {test}")
+
+
+def external_rhs(els: Elements, dm, external, test="hat"):
+    """The external velocity field's part of b (assemble.jl:423-427): -∫ψ_a n·u_ext dA over every test triangle
+    by the 7-point rule, added into the slots. `external` maps points (n x 3) to velocities (n x 3)."""
+    lam, w = radon7()
+    X = np.einsum("qk,tkd->tqd", lam, els.corners.reshape(-1, 3, 3))
+    U = np.asarray(external(X.reshape(-1, 3)), float).reshape(X.shape)
+    un = np.einsum("tqd,td->tq", U, els.n)
+    rows = -np.einsum("q,t,tq,qa->ta", w, els.area, un, test_weights(test, lam))
+    b = np.zeros(dm.nslot)
+    np.add.at(b, dm.corner_slot, rows)
+    return b
+
+
 def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, wake=None, ctx=None):
-    """A, b and stats (assemble.jl:377-447). A is a DeviceSystem; b and stats are on the host."""
+    """A, b and stats (assemble.jl:377-447). A is a DeviceSystem; b and stats are on the host. `external`, if given,
+    is a velocity field (e.g. particles), a function of points (n x 3) returning velocities (n x 3): its part of b is
+    added on the host (external_rhs) to the b of the device, which then differs from A.rhs()."""
     opts = opts or AssemblyOptions()
-    if external is not None:
-        raise ValueError("external velocity fields are not supported by the GPU path")
     ctx = ctx or default_context()
     o = opts.c_struct()
     x, px = _dp(g.x)
@@ -180,7 +218,10 @@ def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, 
     A = DeviceSystem(ctx, h, dm.nslot, dm.nslot + nw)
     stats = {"pairs": dict(zip(TIER_NAMES, list(st.pairs))), "points": dict(zip(TIER_NAMES, list(st.points))),
              "time": st.time_ms / 1e3, "points_fp64": st.points_fp64}
-    return A, A.rhs(), stats
+    b = A.rhs()
+    if external is not None:
+        b = b + external_rhs(els, dm, external, opts.test)
+    return A, b, stats
 
 
 # ---- the bordered solve ------------------------------------------------------------------------------------------------
