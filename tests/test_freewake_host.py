@@ -94,3 +94,43 @@ def test_merging_conserves_vorticity():
             merged = True
             assert len(st.particles) < n0 + 2 * len(topo.segments) + 4
     assert merged
+
+
+def test_state_checkpoint_round_trip(tmp_path):
+    # the wake state through named arrays and an .npz file, then on with the same conversions as the original
+    w = meshes.wing(10, 6, aspect=6.0)
+    st, topo = _state(w, nrow=8)
+    core = fw.CoreRule(fw.FreeWakeOptions(dt=0.05), np.array([1.0, 0, 0]))
+    merge = [3] * len(topo.segments)
+    fw.convert_oldest(st, topo, core, merge)
+    np.savez(tmp_path / "wake.npz", **st.to_arrays())
+    with np.load(tmp_path / "wake.npz") as d:
+        back = fw.FreeWakeState.from_arrays({k: d[k] for k in d.files})
+    for _ in range(3):
+        fw.convert_oldest(st, topo, core, merge)
+        fw.convert_oldest(back, topo, core, merge)
+    assert len(back.x) == len(st.x) and back.conversions == st.conversions
+    assert all(np.array_equal(a, b) for a, b in zip(back.x, st.x))
+    assert all(np.array_equal(a, b) for a, b in zip(back.mu, st.mu))
+    for k in ("particles", "mu_line", "tag", "group", "batch_rows", "batch_length", "batch_width"):
+        assert np.array_equal(getattr(back, k), getattr(st, k)), k
+
+
+def test_sim_checkpoint_restore():
+    # FreeWakeSim.checkpoint / restore on the host fields alone (the device parts of a simulation are not touched)
+    w = meshes.wing(10, 6, aspect=6.0)
+    st, topo = _state(w, nrow=4)
+    sim = object.__new__(fw.FreeWakeSim)
+    sim.state, sim.topo, sim.n, sim.t = st, topo, 5, 0.25
+    sim.mu, sim.mu_w = np.arange(w.dm.nslot, dtype=float), np.ones(topo.nte)
+    sim.cp, sim.I_prev, sim.history = np.zeros(w.g.ntri), np.array([1.0, 2.0, 3.0]), [{"n": 4}]
+    ck = sim.checkpoint()
+    other = object.__new__(fw.FreeWakeSim)
+    other.topo, other.mu = topo, np.zeros(w.dm.nslot)
+    other.restore(ck)
+    assert (other.n, other.t, other.history) == (5, 0.25, [{"n": 4}])
+    assert np.array_equal(other.mu, sim.mu) and np.array_equal(other.I_prev, sim.I_prev)
+    assert all(np.array_equal(a, b) for a, b in zip(other.state.x, st.x))
+    other.mu = np.zeros(w.dm.nslot + 1)
+    with pytest.raises(ValueError):
+        other.restore(ck)

@@ -143,6 +143,25 @@ class FreeWakeState:
         self.tag = self.tag[keep]
         self.group = self.group[keep]
 
+    def to_arrays(self) -> dict:
+        """the state as named arrays (a checkpoint; the reference keeps it in memory only)"""
+        nr = len(self.x)
+        return {"nte": np.array(self.nte), "nstrips": np.array(self.nstrips),
+                "x": np.array(self.x).reshape(nr, self.nte, 3), "mu": np.array(self.mu).reshape(nr, self.nte),
+                "mu_line": self.mu_line, "particles": self.particles, "conversions": np.array(self.conversions),
+                "tag": self.tag, "group": self.group, "batch_rows": self.batch_rows,
+                "batch_length": self.batch_length, "batch_width": self.batch_width}
+
+    @classmethod
+    def from_arrays(cls, d) -> "FreeWakeState":
+        st = cls(int(d["nte"]), int(d["nstrips"]))
+        st.x = [np.array(r, float) for r in d["x"]]
+        st.mu = [np.array(r, float) for r in d["mu"]]
+        st.conversions = int(d["conversions"])
+        for k in ("mu_line", "particles", "tag", "group", "batch_rows", "batch_length", "batch_width"):
+            setattr(st, k, np.array(d[k]))
+        return st
+
 
 def _nondegenerate(p, q, r):
     return np.linalg.norm(np.cross(q - p, r - p)) > 1e-12 * max((q - p) @ (q - p), (r - p) @ (r - p), (r - q) @ (r - q))
@@ -488,6 +507,22 @@ class FreeWakeSim:
         d = self.V / np.linalg.norm(self.V)
         limit = (self.edge @ d).max() + self.opts.delete_beyond * self.te.span
         self.state.keep_particles(self.state.particles[:, :3] @ d <= limit)
+
+    def checkpoint(self) -> dict:
+        """the simulation's evolving state (wake, step count, time, last solution, impulse, history): restore() on a
+        FreeWakeSim built with the same body, options and assembly continues from it"""
+        return {"state": self.state.to_arrays(), "n": self.n, "t": self.t, "mu": self.mu.copy(),
+                "mu_w": self.mu_w.copy(), "cp": self.cp.copy(), "I_prev": self.I_prev.copy(),
+                "history": list(self.history)}
+
+    def restore(self, ckpt: dict):
+        if ckpt["state"]["x"].shape[1:] != (self.topo.nte, 3) or ckpt["mu"].shape != self.mu.shape:
+            raise ValueError("the checkpoint is of another wing or DOF map")
+        self.state = FreeWakeState.from_arrays(ckpt["state"])
+        self.n, self.t = int(ckpt["n"]), float(ckpt["t"])
+        self.mu, self.mu_w, self.cp = ckpt["mu"].copy(), ckpt["mu_w"].copy(), ckpt["cp"].copy()
+        self.I_prev = ckpt["I_prev"].copy()
+        self.history = list(ckpt["history"])
 
     def run(self, nsteps, progress=None):
         """take nsteps steps (step.jl:205-216); returns the history"""
