@@ -143,7 +143,7 @@ int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset);
  *   mode 1: s = w·m (m: 3 per point) and its derivatives with respect to x and the triangle's corners (1 + 3 + 9);
  *   mode 2: the filament from tri[0:3] to tri[3:6] with end weights ca = tri[6], cb = tri[7]: s = ca va·m + cb vb·m
  *           (segment.jl:15-25) and its derivatives with respect to x and the two ends (1 + 3 + 6).
- * precision VP_FP64 or VP_MIXED (the FP32 kernels, without the FP64 guard). */
+ * precision VP_FP64 or VP_MIXED (the FP32 kernels, without the FP64 guard); any other value returns VP_ERR_ARG. */
 int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const double* tri, const double* x, const double* m,
                    int side, double kernel_far, double* out);
 
@@ -152,8 +152,9 @@ int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const double* tr
  * caching allocator) and leaves little outside it, or a stepping loop that cannot afford cudaMalloc/cudaFree, which
  * synchronise the device. Inputs and outputs are staged through a fixed device array of VP_STATIC_POINTS_MAX points
  * (about 0.45 MB, held by every device that loads the library until the process exits); n above that returns
- * VP_ERR_ARG. The array's
- * address is looked up on the first call for each device, which must come before any stream capture on that device.
+ * VP_ERR_ARG, and so does a precision other than VP_FP64 or VP_MIXED. The array's address is looked up on the first
+ * call for each device, which must come before any stream capture on that device, and again on the first call after
+ * the device's CUDA context has changed (a cudaDeviceReset). The caller's current device is restored on return.
  * Calls that overlap in time on one device share the array and race: serialise them. */
 #define VP_STATIC_POINTS_MAX 2048
 int vp_eval_points_static(vp_ctx* ctx, int mode, int precision, int n, const double* tri, const double* x,

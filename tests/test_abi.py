@@ -45,3 +45,11 @@ def test_bindings_match_the_header_arity():
     assert len(protos) >= 20
     bad = [(n, len(args), protos[n]) for n, _, args in _lib.SIGNATURES if n in protos and len(args) != protos[n]]
     assert not bad, bad
+
+
+def test_static_points_limit_matches_the_header():
+    # the Python layer's limit is the header's VP_STATIC_POINTS_MAX
+    from vortexpanel_gpu import api
+    src = open(os.path.join(ROOT, "include", "vortexpanel_gpu.h")).read()
+    m = re.search(r"#define\s+VP_STATIC_POINTS_MAX\s+(\d+)", src)
+    assert m and int(m.group(1)) == api.STATIC_POINTS_MAX

@@ -88,3 +88,17 @@ def test_dimension_mismatch(vp, wing):
     w, wake, W, V, els, sig, A, b, ref = wing
     with pytest.raises(ValueError):
         vp.factorize_galerkin(w.dm, A)  # A has wake columns, W missing
+
+
+def test_external_field_end_to_end(vp, sphere):
+    # a uniform external velocity U0 through assemble(..., external=) equals the freestream V + U0: the device b plus
+    # the host's 7-point term (exact for a constant field on hat functions), and the solution of either
+    g, dm, V, els, sig, A, b, ref = sphere
+    U0 = np.array([0.2, -0.1, 0.05])
+    sig2 = vp.source_strengths(els, V + U0)
+    A1, b1, _ = vp.assemble(g, dm, els, sig2, V, external=lambda X: np.tile(U0, (len(X), 1)))
+    A2, b2, _ = vp.assemble(g, dm, els, sig2, V + U0)
+    assert np.max(np.abs(b1 - b2)) < 1e-13 * np.max(np.abs(b2))
+    s1 = vp.solve_galerkin(vp.factorize_galerkin(dm, A1), b1)
+    s2 = vp.solve_galerkin(dm, A2, b2)
+    assert np.max(np.abs(s1["q"] - s2["q"])) < 1e-11 * np.max(np.abs(s2["q"]))

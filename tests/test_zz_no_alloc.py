@@ -37,8 +37,30 @@ def test_static_matches_allocating_entry(vp):
     assert np.allclose(got3, ref3, rtol=1e-12, atol=1e-14 * np.abs(ref3).max())
 
 
-def test_static_rejects_oversize(vp):
+def test_static_call_allocates_nothing(vp):
+    # after a first call (which looks up the array's address), further calls leave the device's free memory as it was
+    torch = pytest.importorskip("torch")
+    api = vp.api
+    tri, x, m = _case(np.random.default_rng(5), api.STATIC_POINTS_MAX)
+    api.eval_points_static(1, tri, x, m)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for mode in (0, 1, 2, 1):
+        api.eval_points_static(mode, tri, x, m)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0, (free0, free1)
+
+
+def test_static_rejects_oversize_and_bad_precision(vp):
     api = vp.api
     tri, x, _ = _case(np.random.default_rng(1), api.STATIC_POINTS_MAX + 1)
     with pytest.raises(ValueError, match="above"):
         api.eval_points_static(0, tri, x)
+    ctx = api.default_context()
+    out = np.zeros((4, 3))
+    t4, x4 = np.ascontiguousarray(tri[:4]), np.ascontiguousarray(x[:4])
+    code = vp._lib.load().vp_eval_points_static(ctx.h, 0, 7, 4, t4.ctypes.data_as(vp._lib.D),
+                                               x4.ctypes.data_as(vp._lib.D), None, 0, 10.0,
+                                               out.ctypes.data_as(vp._lib.D))
+    assert code == vp._lib.VP_ERR_ARG

@@ -86,6 +86,23 @@ struct vp_factor {
 
 int vp_fail(vp_ctx* ctx, int code, const std::string& msg);
 
+// Makes a context's device current for the length of a call and gives the caller's current device back on return.
+struct DeviceGuard {
+    int prev = -1;
+    cudaError_t set(int device) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) {
+            prev = -1;
+            return e;
+        }
+        return prev == device ? cudaSuccess : cudaSetDevice(device);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 #define VP_CUDA(ctx, call)                                                                            \
     do {                                                                                              \
         cudaError_t e_ = (call);                                                                      \

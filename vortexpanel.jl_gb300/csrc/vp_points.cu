@@ -3,6 +3,8 @@
 #include "vp_adjoint_common.cuh"
 #include "vp_internal.h"
 
+#include <cuda.h>
+
 #include <mutex>
 
 namespace {
@@ -103,6 +105,9 @@ extern "C" int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const
                               const double* m, int side, double kernel_far, double* out) {
     if (!ctx || !tri || !x || !out || n <= 0 || mode < 0 || mode > 2) return vp_fail(ctx, VP_ERR_ARG, "bad argument");
     if (mode > 0 && !m) return vp_fail(ctx, VP_ERR_ARG, "m is needed");
+    if (precision != VP_FP64 && precision != VP_MIXED) return vp_fail(ctx, VP_ERR_ARG, "precision must be VP_FP64 or VP_MIXED");
+    DeviceGuard dg;
+    if (dg.set(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
     const int nout = mode == 0 ? 3 : (mode == 1 ? 13 : 10);
     double *dt, *dx, *dm = nullptr, *dout;
     int r;
@@ -130,11 +135,13 @@ extern "C" int vp_eval_points(vp_ctx* ctx, int mode, int precision, int n, const
 // vp_eval_points_static: the same evaluation as vp_eval_points with no device allocation, for callers that cannot
 // allocate while they run (a host whose device memory sits in its own pool, a loop that cannot afford the device
 // synchronisation of cudaMalloc/cudaFree). Inputs and outputs are staged through one file-scope device array sized
-// for VP_STATIC_POINTS_MAX points; its address is looked up once per device with cudaGetSymbolAddress on the first
-// call for that device, so that first call has to be made before any stream capture on the device. Calls that
-// overlap in time on one device (from two streams or two host threads) share the array and race: the caller
-// serialises them. No part of the array has to start at zero: points_kernel writes every output slot of the n points
-// it is given, and the inputs are copied in before the launch.
+// for VP_STATIC_POINTS_MAX points. Its address is looked up with cudaGetSymbolAddress on the first call for each device
+// (with that device current), so that first call has to be made before any stream capture on the device; the address
+// is kept with the id of the CUDA context it was looked up in and looked up again when the device's current context
+// changes (after a cudaDeviceReset, say), because the array then lives at a new address. Calls that overlap in time on
+// one device (from two streams or two host threads) share the array and race: the caller serialises them. No part of
+// the array has to start at zero: points_kernel writes every output slot of the n points it is given, and the inputs
+// are copied in before the launch. The caller's current device is restored on return.
 namespace {
 
 constexpr size_t kStaticTri = size_t(9) * VP_STATIC_POINTS_MAX;   // triangle (or filament) rows
@@ -150,6 +157,33 @@ static __device__ __align__(256) double g_points_scratch[kStaticDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_scratch_mu;
 double* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_scratch_ctx_id[kMaxDevices] = {};
+
+// the unique id of the calling thread's current CUDA context (cuCtxGetId, reached through the runtime's driver entry
+// points so that the library needs no link to libcuda); 0 when it cannot be had
+unsigned long long current_context_id() {
+    typedef CUresult (*GetCurrent)(CUcontext*);
+    typedef CUresult (*GetId)(CUcontext, unsigned long long*);
+    static GetCurrent get_current = nullptr;
+    static GetId get_id = nullptr;
+    static bool resolved = false;
+    if (!resolved) {  // called under g_scratch_mu
+        cudaDriverEntryPointQueryResult q1, q2;
+        void *a = nullptr, *b = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+            q1 == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+            q2 == cudaDriverEntryPointSuccess) {
+            get_current = reinterpret_cast<GetCurrent>(a);
+            get_id = reinterpret_cast<GetId>(b);
+        }
+        resolved = true;
+    }
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+    return id;
+}
 
 }  // namespace
 
@@ -157,20 +191,24 @@ extern "C" int vp_eval_points_static(vp_ctx* ctx, int mode, int precision, int n
                                      const double* m, int side, double kernel_far, double* out) {
     if (!ctx || !tri || !x || !out || n <= 0 || mode < 0 || mode > 2) return vp_fail(ctx, VP_ERR_ARG, "bad argument");
     if (mode > 0 && !m) return vp_fail(ctx, VP_ERR_ARG, "m is needed");
+    if (precision != VP_FP64 && precision != VP_MIXED) return vp_fail(ctx, VP_ERR_ARG, "precision must be VP_FP64 or VP_MIXED");
     if (n > VP_STATIC_POINTS_MAX)
         return vp_fail(ctx, VP_ERR_ARG, "vp_eval_points_static: n = " + std::to_string(n) + " is above " +
                                             std::to_string(VP_STATIC_POINTS_MAX));
     if (ctx->device < 0 || ctx->device >= kMaxDevices) return vp_fail(ctx, VP_ERR_ARG, "device index");
-    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    DeviceGuard dg;
+    if (dg.set(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
     double* base;
     {
         std::lock_guard<std::mutex> lk(g_scratch_mu);
-        if (!g_scratch_addr[ctx->device]) {
+        const unsigned long long id = current_context_id();
+        if (!g_scratch_addr[ctx->device] || id == 0 || id != g_scratch_ctx_id[ctx->device]) {
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_points_scratch);
             if (e != cudaSuccess)
                 return vp_fail(ctx, VP_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
             g_scratch_addr[ctx->device] = static_cast<double*>(p);
+            g_scratch_ctx_id[ctx->device] = id;
         }
         base = g_scratch_addr[ctx->device];
     }
