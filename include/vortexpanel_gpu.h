@@ -86,6 +86,8 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
 int vp_system_shape(const vp_system* sys, int* nrows, int* ncols);
 /* Copy A (row-major, nrows x ncols) and/or b (nrows) to the host; either pointer may be NULL. */
 int vp_system_download(vp_ctx* ctx, const vp_system* sys, double* A, double* b);
+/* Copy rows [r0, r1) of A (row-major, (r1 - r0) x ncols) and/or of b to the host; either pointer may be NULL. */
+int vp_system_download_rows(vp_ctx* ctx, const vp_system* sys, int r0, int r1, double* A, double* b);
 void vp_system_free(vp_system* sys);
 
 /* factorize_galerkin (src/assembly/solve.jl:81-87): the bordered system (solve.jl:15-38) of the reduction
@@ -177,6 +179,33 @@ int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, con
                     const int* tris, const int* corner_slot, int nslot, int nsheet, const double* sheet_x,
                     const double* sheet_mu, int nseg, const double* seg_x, const double* seg_gamma, int nblob,
                     const double* blobs, double* rhs);
+
+/* consistency (src/assembly/solve.jl:111-115): the quadrature diagnostics of the assembled system in terms of
+ * A Cf, Cf = [C; W] (C: CSR nslot x nq; W: CSR nwake x nq of the wake rows, nwake = 0 without wake columns):
+ * out[0] = max |row sum| / |A Cf|_inf, out[1] = max |column sum| / |A Cf|_inf, out[2] = |sum b| / sum |b|.
+ * FP64 on the GPU, summed in a fixed order. */
+int vp_consistency(vp_ctx* ctx, const vp_system* sys, int nq, const int* C_rowptr, const int* C_col,
+                   const double* C_val, int nwake, const int* W_rowptr, const int* W_col, const double* W_val,
+                   double* out);
+
+/* The gradient route's surface loads in FP64 on the GPU:
+ *   gradient_velocity (src/post/Post.jl:72-73): u = V - (V.n)n + grad mu on every triangle (u: ntri x 3, may be NULL);
+ *   pressure_coefficient (Post.jl:82-84): cp = 1 - (|u|^2 + 2 dmu/dt)/|V|^2 with dmu/dt the mean of the corners'
+ *     slot values of dmudt (nslot; NULL for steady flow) (cp: ntri, may be NULL);
+ *   pressure_force (src/post/forces.jl:11-20): F = -sum cp A n and M = sum (c - origin) x (-cp A n) (3 each; origin may
+ *     be NULL for 0).
+ * corners: ntri x 9; corner_slot: ntri x 3; mu: nslot. */
+int vp_surface_loads(vp_ctx* ctx, int ntri, const double* corners, const int* corner_slot, int nslot,
+                     const double* mu, const double* dmudt, const double* vinf, const double* origin, double* u,
+                     double* cp, double* F, double* M);
+/* pressure_force(els, cp; origin) (src/post/forces.jl:11-20) of a given cp (ntri), FP64 on the GPU. */
+int vp_pressure_force(vp_ctx* ctx, int ntri, const double* corners, const double* cp, const double* origin, double* F,
+                      double* M);
+/* kutta_joukowski_force and trefftz_drag (src/post/forces.jl:34-39,53-81) of the doublets mu_w (nte) at the wake's
+ * trailing edge nodes te_x (nte x 3), along nline lines (line_ptr: nline + 1 offsets into line_nodes, 0-based node
+ * indices; line_closed: nline flags): F_kj (3) and D_trefftz (1), in units of q∞. FP64 on the GPU. */
+int vp_wake_loads(vp_ctx* ctx, int nte, const double* te_x, int nline, const int* line_ptr, const int* line_nodes,
+                  const int* line_closed, const double* mu_w, const double* vinf, double* F_kj, double* D_trefftz);
 
 /* Condition estimate and size of a factorization. */
 int vp_factor_info(const vp_factor* F, int* n, double* cond);

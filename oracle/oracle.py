@@ -89,6 +89,9 @@ def lib():
             _lib.vpo_assemble.argtypes = [ctypes.POINTER(_Opts), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
                                           ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I,
                                           ctypes.c_int, ctypes.c_int, D, D, L, L, ctypes.c_int]
+            _lib.vpo_assemble_list.argtypes = [ctypes.POINTER(_Opts), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
+                                               ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I,
+                                               ctypes.c_int, I, D, D, L, L, ctypes.c_int]
         return _lib
 
 
@@ -214,9 +217,11 @@ def source_strengths(g, V):
     return -n @ np.asarray(V, float)
 
 
-def assemble(g, dm, sigma, V, wake=None, rows=None, nthreads=0, **kw):
+def assemble(g, dm, sigma, V, wake=None, rows=None, tests=None, nthreads=0, **kw):
     """A (nslot x (nslot + nwake)), b (nslot) and the per-tier pair and point counts (assemble.jl:377-447).
-    ``rows = (t0, t1)`` assembles only the rows of test triangles t0..t1-1 (a sample for timing)."""
+    ``rows = (t0, t1)`` assembles only the rows of test triangles t0..t1-1 (a sample for timing); ``tests`` (an array
+    of triangle indices) only those test triangles' rows, so that the rows of every slot whose triangles are all
+    among them are complete."""
     o = options(**kw)
     x, px = _d(g.x)
     tris, pt = _i(g.tris)
@@ -239,10 +244,17 @@ def assemble(g, dm, sigma, V, wake=None, rows=None, nthreads=0, **kw):
     b, pb = _d(np.zeros(dm.nslot))
     P = np.zeros(6, np.int64)
     Q = np.zeros(6, np.int64)
-    t0, t1 = (0, g.ntri) if rows is None else rows
-    r = lib().vpo_assemble(ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(g.touch_pairs), ptp, ps, pV, nw,
-                           pwx, nwt, pwt, nf, pwf, t0, t1, pA, pb, P.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)),
-                           Q.ctypes.data_as(ctypes.POINTER(ctypes.c_longlong)), nthreads)
+    LL = ctypes.POINTER(ctypes.c_longlong)
+    if tests is not None:
+        tl, ptl = _i(np.asarray(tests, np.int32))
+        r = lib().vpo_assemble_list(ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(g.touch_pairs), ptp,
+                                    ps, pV, nw, pwx, nwt, pwt, nf, pwf, len(tl), ptl, pA, pb, P.ctypes.data_as(LL),
+                                    Q.ctypes.data_as(LL), nthreads)
+    else:
+        t0, t1 = (0, g.ntri) if rows is None else rows
+        r = lib().vpo_assemble(ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(g.touch_pairs), ptp, ps, pV,
+                               nw, pwx, nwt, pwt, nf, pwf, t0, t1, pA, pb, P.ctypes.data_as(LL), Q.ctypes.data_as(LL),
+                               nthreads)
     if r != 0:
         raise ValueError("degenerate triangle")
     return A, b, {"pairs": dict(zip(TIERS, P.tolist())), "points": dict(zip(TIERS, Q.tolist()))}

@@ -730,11 +730,40 @@ int vpo_pair_block(const double* Tx, const double* Sx, const double* lam, const 
 // assemble (assemble.jl:377-447) over the test triangles [t0, t1): rows of A (nslot x (nslot + nwnode), row-major)
 // and b are accumulated (the caller zeroes them). pairs/points: 6 counters per tier (self, edge, vertex, contact,
 // near, far). Returns 0, or -1 for a degenerate triangle.
+static int assemble_tests(const vpo_options* po, int ntri, const double* x, const int* tris, const int* corner_slot,
+                          int nslot, int ntouch, const int* touch_pairs, const double* sigma, const double* V,
+                          int nwnode, const double* wx, int nwtri, const int* wtris, int nfil, const int* fil, int t0,
+                          int t1, const int* tlist, double* A, double* b, long long* pairs, long long* points,
+                          int nthreads);
+
 int vpo_assemble(const vpo_options* po, int nnode, const double* x, int ntri, const int* tris, const int* corner_slot,
                  int nslot, int ntouch, const int* touch_pairs, const double* sigma, const double* V, int nwnode,
                  const double* wx, int nwtri, const int* wtris, int nfil, const int* fil, int t0, int t1, double* A,
                  double* b, long long* pairs, long long* points, int nthreads) {
     (void)nnode;
+    return assemble_tests(po, ntri, x, tris, corner_slot, nslot, ntouch, touch_pairs, sigma, V, nwnode, wx, nwtri,
+                          wtris, nfil, fil, t0, t1, nullptr, A, b, pairs, points, nthreads);
+}
+
+// assemble over the test triangles tlist[0 .. ntest): the rows of every slot whose one-ring lies in the list are
+// complete (a sample of rows anywhere on a large mesh)
+int vpo_assemble_list(const vpo_options* po, int nnode, const double* x, int ntri, const int* tris,
+                      const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
+                      const double* V, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
+                      const int* fil, int ntest, const int* tlist, double* A, double* b, long long* pairs,
+                      long long* points, int nthreads) {
+    (void)nnode;
+    for (int k = 0; k < ntest; ++k)
+        if (tlist[k] < 0 || tlist[k] >= ntri) return -2;
+    return assemble_tests(po, ntri, x, tris, corner_slot, nslot, ntouch, touch_pairs, sigma, V, nwnode, wx, nwtri,
+                          wtris, nfil, fil, 0, ntest, tlist, A, b, pairs, points, nthreads);
+}
+
+static int assemble_tests(const vpo_options* po, int ntri, const double* x, const int* tris, const int* corner_slot,
+                          int nslot, int ntouch, const int* touch_pairs, const double* sigma, const double* V,
+                          int nwnode, const double* wx, int nwtri, const int* wtris, int nfil, const int* fil, int t0,
+                          int t1, const int* tlist, double* A, double* b, long long* pairs, long long* points,
+                          int nthreads) {
     Options o = to_opts(po);
     TierRules rules = tier_rules(o);
     std::vector<FlatTri> els, wels;
@@ -752,7 +781,7 @@ int vpo_assemble(const vpo_options* po, int nnode, const double* x, int ntri, co
     const Vec ti = test_integrals(o.test);
     long long P[6] = {0}, Q[6] = {0};
     if (t0 < 0) t0 = 0;
-    if (t1 > ntri) t1 = ntri;
+    if (!tlist && t1 > ntri) t1 = ntri;
 #ifdef _OPENMP
     if (nthreads > 0) omp_set_num_threads(nthreads);
 #else
@@ -764,7 +793,8 @@ int vpo_assemble(const vpo_options* po, int nnode, const double* x, int ntri, co
         Rule rbuf;
         long long myP[6] = {0}, myQ[6] = {0};
 #pragma omp for schedule(dynamic, 4)
-        for (int t = t0; t < t1; ++t) {
+        for (int it = t0; it < t1; ++it) {
+            const int t = tlist ? tlist[it] : it;
             const FlatTri& T = els[t];
             std::fill(buf.begin(), buf.end(), 0.0);
             double rows[3] = {0, 0, 0};

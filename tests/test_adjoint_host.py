@@ -1,12 +1,14 @@
 """The explicit parts of the adjoint gradients (host code, no GPU): the derivatives of CL of the gradient route
 (Post.jl:72-84, forces.jl:11-20) and of CDi of the Trefftz plane (forces.jl:53-81) with respect to the doublet
-values, the node coordinates and alpha, against central finite differences of the same host formulas."""
+values, the node coordinates and alpha, against central finite differences of the oracle's restatement of the
+loads."""
 import math
 
 import numpy as np
 import pytest
 
-from vortexpanel_gpu import api, meshes
+import oracle as O
+from vortexpanel_gpu import meshes
 from vortexpanel_gpu.adjoint import cdi_trefftz, cl_pressure
 
 
@@ -19,9 +21,9 @@ def _cl(w, x, mu, a):
     g = meshes.Geometry(x, w.g.tris)
     V = np.array([math.cos(a), 0.0, math.sin(a)])
     eL = np.array([-math.sin(a), 0.0, math.cos(a)])
-    els = api.build_elements(g)
-    cp = api.pressure_coefficient(api.gradient_velocity(els, w.dm, mu, V), V)
-    return float(api.pressure_force(els, cp)[0] @ eL / (w.span * w.chord))
+    els = O.elements(g)
+    cp = O.pressure_coefficient(O.gradient_velocity(g, w.dm, mu, V, els=els), V)
+    return float(O.pressure_force(els, cp)[0] @ eL / (w.span * w.chord))
 
 
 def test_cl_explicit_derivatives(small_wing):
@@ -63,7 +65,7 @@ def test_cdi_explicit_derivatives(small_wing):
     def cdi(X, mu, al):
         t = meshes.WakeTE(wte.node, X, wte.lines, wte.closed)
         VV = np.array([math.cos(al), 0.0, math.sin(al)])
-        return api.trefftz_drag(t, mu, VV) / S
+        return O.trefftz_drag(t, mu, VV) / S
 
     CDi, dmu, gx, dal = cdi_trefftz(wte, muw, V, dV, S)
     assert abs(CDi - cdi(wte.x, muw, a)) <= 1e-13 * max(1.0, abs(CDi))

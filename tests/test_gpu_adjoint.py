@@ -1,11 +1,11 @@
 """Adjoint gradients through the C ABI (vp_solve_transposed, vp_adjoint) against central finite differences of the
 GPU's FP64 forward path (assemble + factorize + solve + loads), step 1e-6 chord, on a small lifting wing with its
 rigid wake: dCL/dx and dCDi/dx at seeded random nodes, trailing edge and tip nodes among them, and d/dalpha."""
-import dataclasses
 import math
 
 import numpy as np
 import pytest
+import wingcase
 
 from vortexpanel_gpu import api, meshes
 from vortexpanel_gpu.adjoint import wing_gradients
@@ -13,31 +13,10 @@ from vortexpanel_gpu.adjoint import wing_gradients
 pytestmark = pytest.mark.gpu
 
 
-def _corner_angles(g):
-    x, t = g.x, g.tris
-    out = []
-    for k in range(3):
-        u = x[t[:, (k + 1) % 3]] - x[t[:, k]]
-        v = x[t[:, (k + 2) % 3]] - x[t[:, k]]
-        c = np.einsum("ij,ij->i", u, v) / (np.linalg.norm(u, axis=1) * np.linalg.norm(v, axis=1))
-        out.append(np.degrees(np.arccos(np.clip(c, -1, 1))))
-    return np.concatenate(out)
-
-
 @pytest.fixture(scope="module")
 def case():
-    """The wing with its nodes moved in x and y by up to 2e-3 chord: the extruded wing's quads have corners of
-    exactly 90 degrees, where the vertex rule switches from one piece to wedges (assemble.jl:102-125), so that the
-    discrete loads jump under a rounding-level move and finite differences across the switch mean nothing"""
-    w = meshes.wing(12, 6, aspect=6.0)
-    rng = np.random.default_rng(20)
-    x = w.g.x.copy()
-    x[:, :2] += rng.uniform(-2e-3, 2e-3, (len(x), 2)) * w.chord
-    w = dataclasses.replace(w, g=dataclasses.replace(w.g, x=x))
-    te = w.dm.wake_te
-    w = dataclasses.replace(w, dm=dataclasses.replace(w.dm, wake_te=meshes.WakeTE(te.node, x[te.node].copy(), te.lines,
-                                                                                   te.closed)))
-    ang = _corner_angles(w.g)
+    w = wingcase.jittered(meshes.wing(12, 6, aspect=6.0))
+    ang = wingcase.corner_angles(w.g)
     # no corner within 0.01 degrees of a switch of the vertex rule (90, and 150 for corner_angle = 75), wedges present
     assert np.abs(ang - 90).min() > 1e-2 and np.abs(ang - 150).min() > 1e-2 and (ang > 90.5).any()
     wake = meshes.build_wake(w.g, w.dm, (1.0, 0.0, 0.0), length=1.0)
@@ -45,25 +24,8 @@ def case():
     return w, wake, W
 
 
-def _moved(w, wake, x):
-    """the wing with its nodes at x; the wake rows keep their offsets from the trailing edge nodes"""
-    wte = w.dm.wake_te
-    te = meshes.WakeTE(wte.node, x[wte.node].copy(), wte.lines, wte.closed)
-    d = np.array([1.0, 0.0, 0.0])
-    wk = dataclasses.replace(wake, x=te.x[wake.te] + wake.rows[wake.row][:, None] * d)
-    return dataclasses.replace(w, g=dataclasses.replace(w.g, x=x), dm=dataclasses.replace(w.dm, wake_te=te)), wk
-
-
-def _loads(w, wake, W, a):
-    V = np.array([math.cos(a), 0.0, math.sin(a)])
-    eL = np.array([-math.sin(a), 0.0, math.cos(a)])
-    els = api.build_elements(w.g)
-    sig = api.source_strengths(els, V)
-    A, b, _ = api.assemble(w.g, w.dm, els, sig, V, wake=wake)
-    s = api.solve_galerkin(api.factorize_galerkin(w.dm, A, W=W), b)
-    S = w.span * w.chord
-    cp = api.pressure_coefficient(api.gradient_velocity(els, w.dm, s["mu"], V), V)
-    return float(api.pressure_force(els, cp)[0] @ eL / S), float(api.trefftz_drag(w.dm.wake_te, w.dm.K @ s["q"], V) / S)
+_moved = wingcase.moved
+_loads = wingcase.loads
 
 
 def _nodes(w):

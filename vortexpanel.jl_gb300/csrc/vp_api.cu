@@ -170,6 +170,17 @@ int vp_system_download(vp_ctx* ctx, const vp_system* sys, double* A, double* b) 
     return VP_OK;
 }
 
+int vp_system_download_rows(vp_ctx* ctx, const vp_system* sys, int r0, int r1, double* A, double* b) {
+    if (!ctx || !sys) return vp_fail(ctx, VP_ERR_ARG, "null argument");
+    if (r0 < 0 || r1 > sys->nslot || r0 > r1) return vp_fail(ctx, VP_ERR_ARG, "rows out of range");
+    if (r0 == r1) return VP_OK;
+    if (A)
+        VP_CUDA(ctx, vp_d2h(ctx, A, sys->A + size_t(r0) * sys->ncols, sizeof(double) * size_t(r1 - r0) * sys->ncols));
+    if (b) VP_CUDA(ctx, vp_d2h(ctx, b, sys->b + r0, sizeof(double) * (r1 - r0)));
+    VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return VP_OK;
+}
+
 void vp_system_free(vp_system* sys) {
     if (!sys) return;
     if (sys->A) cudaFree(sys->A);

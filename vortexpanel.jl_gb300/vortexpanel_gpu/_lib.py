@@ -41,6 +41,7 @@ SIGNATURES = [
       ctypes.POINTER(vp_assembly_stats)]),
     ("vp_system_shape", ctypes.c_int, [ctypes.c_void_p, I, I]),
     ("vp_system_download", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, D, D]),
+    ("vp_system_download_rows", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, D]),
     ("vp_system_free", None, [ctypes.c_void_p]),
     ("vp_factorize", ctypes.c_int,
      [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, I, I, D, ctypes.c_int, I, I, D, ctypes.c_int, I, D,
@@ -65,6 +66,11 @@ SIGNATURES = [
     ("vp_explicit_rhs", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D,
                                        ctypes.c_int, I, I, ctypes.c_int, ctypes.c_int, D, D, ctypes.c_int, D, D,
                                        ctypes.c_int, D, D]),
+    ("vp_consistency", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, I, I, D, ctypes.c_int, I, I, D,
+                                      D]),
+    ("vp_surface_loads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, D, I, ctypes.c_int, D, D, D, D, D, D, D, D]),
+    ("vp_pressure_force", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, D, D, D, D, D]),
+    ("vp_wake_loads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, D, ctypes.c_int, I, I, I, D, D, D, D]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]

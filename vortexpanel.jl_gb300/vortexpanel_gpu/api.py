@@ -130,6 +130,14 @@ class DeviceSystem:
         check(self.ctx.h, load().vp_system_download(self.ctx.h, self.h, A.ctypes.data_as(D), None))
         return A
 
+    def download_rows(self, r0, r1):
+        """rows [r0, r1) of A and of b"""
+        A = np.zeros((r1 - r0, self.ncols))
+        b = np.zeros(r1 - r0)
+        check(self.ctx.h, load().vp_system_download_rows(self.ctx.h, self.h, r0, r1, A.ctypes.data_as(D),
+                                                         b.ctypes.data_as(D)))
+        return A, b
+
     def rhs(self):
         b = np.zeros(self.nslot)
         check(self.ctx.h, load().vp_system_download(self.ctx.h, self.h, None, b.ctypes.data_as(D)))
@@ -377,73 +385,104 @@ def surface_velocity(els: Elements, dm, sigma, mu, V, wake=None, mu_wake=None, k
     return u
 
 
-def gradient_velocity(els: Elements, dm, mu, V):
-    """V∞ - (V∞·n)n + ∇μ on every triangle (Post.jl:72-73)"""
-    V = np.asarray(V, float)
-    m = element_values(dm, mu)
-    grad = sum(m[:, k:k + 1] * els.gradl[k] for k in range(3))
-    return V - (els.n @ V)[:, None] * els.n + grad
+def surface_loads(els: Elements, dm, mu, V, dmudt=None, origin=(0.0, 0.0, 0.0), ctx=None):
+    """The gradient route in one FP64 pass on the GPU (vp_surface_loads): u = V∞ - (V∞·n)n + ∇μ per triangle
+    (Post.jl:72-73), Cp = 1 - (|u|² + 2 ∂μ/∂t)/|V∞|² with the element mean of the slot values dmudt (Post.jl:82-84),
+    and the force and moment -Σ Cp A n, Σ (c - origin) × (-Cp A n) (forces.jl:11-20). Returns a dict u, cp, F, M."""
+    ctx = ctx or default_context()
+    c, pc = _dp(els.corners)
+    cs, pcs = _ip(dm.corner_slot)
+    m, pm = _dp(mu)
+    if m.shape != (dm.nslot,):
+        raise ValueError(f"μ has {m.shape[0]} entries, expected {dm.nslot}")
+    dd, pdd = (None, None) if dmudt is None else _dp(dmudt)
+    VV, pV = _dp(V)
+    o, po = _dp(origin)
+    nt = c.shape[0]
+    u, cp, F, M = np.zeros((nt, 3)), np.zeros(nt), np.zeros(3), np.zeros(3)
+    check(ctx.h, load().vp_surface_loads(ctx.h, nt, pc, pcs, dm.nslot, pm, pdd, pV, po, u.ctypes.data_as(D),
+                                         cp.ctypes.data_as(D), F.ctypes.data_as(D), M.ctypes.data_as(D)))
+    return dict(u=u, cp=cp, F=F, M=M)
+
+
+def gradient_velocity(els: Elements, dm, mu, V, ctx=None):
+    """V∞ - (V∞·n)n + ∇μ on every triangle (Post.jl:72-73), FP64 on the GPU"""
+    return surface_loads(els, dm, mu, V, ctx=ctx)["u"]
 
 
 def pressure_coefficient(u, V, dmudt=None):
+    """1 - (|u|² + 2 ∂μ/∂t)/|V∞|² at given velocities (Post.jl:82-84); surface_loads gives it from μ on the GPU"""
     V = np.asarray(V, float)
-    s = np.einsum("ij,ij->i", u, u)
+    s = np.einsum("ij,ij->i", np.asarray(u, float), np.asarray(u, float))
     if dmudt is not None:
         s = s + 2 * np.asarray(dmudt)
     return 1 - s / (V @ V)
 
 
-def pressure_force(els: Elements, cp, origin=(0.0, 0.0, 0.0)):
-    f = -(np.asarray(cp) * els.area)[:, None] * els.n
-    return f.sum(axis=0), np.cross(els.centroid - np.asarray(origin, float), f).sum(axis=0)
+def pressure_force(els: Elements, cp, origin=(0.0, 0.0, 0.0), ctx=None):
+    """Force and moment about origin, in units of q∞, of a Cp constant on each triangle (forces.jl:11-20), FP64 on the
+    GPU (vp_pressure_force)"""
+    ctx = ctx or default_context()
+    c, pc = _dp(els.corners)
+    cc, pcc = _dp(cp)
+    if cc.shape != (c.shape[0],):
+        raise ValueError(f"cp has {cc.shape[0]} entries, expected {c.shape[0]}")
+    o, po = _dp(origin)
+    F, M = np.zeros(3), np.zeros(3)
+    check(ctx.h, load().vp_pressure_force(ctx.h, c.shape[0], pc, pcc, po, F.ctypes.data_as(D), M.ctypes.data_as(D)))
+    return F, M
 
 
-def _te_segments(wte):
-    out = []
-    for line, closed in zip(wte.lines, wte.closed):
-        m = len(line)
-        for i in range(m if closed else m - 1):
-            out.append((line[i], line[(i + 1) % m]))
-    return out
+def wake_loads(wte, mu_w, V, ctx=None):
+    """(F_kj, D_trefftz): kutta_joukowski_force and trefftz_drag (forces.jl:34-39,53-81) of the trailing edge
+    doublets mu_w, in units of q∞, FP64 on the GPU (vp_wake_loads)"""
+    ctx = ctx or default_context()
+    x, px = _dp(wte.x)
+    mw, pmw = _dp(mu_w)
+    if mw.shape != (x.shape[0],):
+        raise ValueError(f"μ_w has {mw.shape[0]} entries, expected {x.shape[0]}")
+    lines = [np.asarray(L, np.int32) for L in wte.lines]
+    ptr, pptr = _ip(np.concatenate([[0], np.cumsum([len(L) for L in lines])]) if lines else np.zeros(1))
+    nodes, pnodes = _ip(np.concatenate(lines) if lines else np.zeros(1))
+    closed, pclosed = _ip(np.asarray([bool(c) for c in wte.closed], np.int32) if lines else np.zeros(1))
+    VV, pV = _dp(V)
+    F, Dv = np.zeros(3), ctypes.c_double()
+    check(ctx.h, load().vp_wake_loads(ctx.h, x.shape[0], px, len(lines), pptr, pnodes, pclosed, pmw, pV,
+                                      F.ctypes.data_as(D), ctypes.byref(Dv)))
+    return F, Dv.value
 
 
-def kutta_joukowski_force(wte, mu_w, V):
-    """(2/|V∞|²) V∞ × ∫μ_w dl along the trailing edge lines (forces.jl:34-39)"""
-    V = np.asarray(V, float)
-    G = np.zeros(3)
-    for a, b in _te_segments(wte):
-        G += (mu_w[a] + mu_w[b]) / 2 * (wte.x[b] - wte.x[a])
-    return 2 / (V @ V) * np.cross(V, G)
+def kutta_joukowski_force(wte, mu_w, V, ctx=None):
+    """(2/|V∞|²) V∞ × ∫μ_w dl along the trailing edge lines (forces.jl:34-39), FP64 on the GPU"""
+    return wake_loads(wte, mu_w, V, ctx=ctx)[0]
 
 
-def trefftz_drag(wte, mu_w, V):
-    """Induced drag in the Trefftz plane, in units of q∞ (forces.jl:53-81)"""
-    V = np.asarray(V, float)
-    d = V / np.linalg.norm(V)
-    P = lambda x: x - (x @ d) * d  # noqa: E731
-    vort, strips = [], []
-    for line, closed in zip(wte.lines, wte.closed):
-        m = len(line)
-        nseg = m if closed else m - 1
-        G = [(mu_w[line[i]] + mu_w[line[(i + 1) % m]]) / 2 for i in range(nseg)]
-        for i in range(m):
-            before = G[i - 1] if i > 0 else (G[nseg - 1] if closed else 0.0)
-            after = G[i] if i < nseg else 0.0
-            vort.append((P(wte.x[line[i]]), after - before))
-        for i in range(nseg):
-            strips.append((P(wte.x[line[i]]), P(wte.x[line[(i + 1) % m]]), G[i]))
-    if not strips:
-        return 0.0
-    pv = np.array([v[0] for v in vort])
-    dG = np.array([v[1] for v in vort])
-    Dsum = 0.0
-    for a, b, Gk in strips:
-        c, l = (a + b) / 2, np.linalg.norm(b - a)
-        n = np.cross(d, (b - a) / l)
-        r = c - pv
-        v = (dG[:, None] / (4 * math.pi) * np.cross(d, r) / np.einsum("ij,ij->i", r, r)[:, None]).sum(axis=0)
-        Dsum += Gk * (n @ v) * l
-    return 2 * Dsum / (V @ V)
+def trefftz_drag(wte, mu_w, V, ctx=None):
+    """Induced drag in the Trefftz plane, in units of q∞ (forces.jl:53-81), FP64 on the GPU"""
+    return wake_loads(wte, mu_w, V, ctx=ctx)[1]
+
+
+def consistency(dm, A: DeviceSystem, b=None, W=None, ctx=None):
+    """Row, column and right hand side sum defects of A [C; W] (solve.jl:111-115), FP64 on the GPU
+    (vp_consistency). b defaults to the device's own; a host b given here (an external field's) enters the rhs
+    defect."""
+    ctx = ctx or A.ctx
+    keepC, (cp, cc, cv) = _csr_parts(dm.C)
+    nw = 0 if W is None else W.shape[0]
+    if A.ncols != dm.nslot + nw:
+        raise ValueError(f"A is {A.shape}, expected ({dm.nslot}, {dm.nslot + nw})")
+    if W is not None:
+        keepW, (wp, wc, wv) = _csr_parts(W)
+    else:
+        wp = wc = wv = None
+    out = np.zeros(3)
+    check(ctx.h, load().vp_consistency(ctx.h, A.h, dm.nq, cp, cc, cv, nw, wp, wc, wv, out.ctypes.data_as(D)))
+    res = dict(rows=float(out[0]), columns=float(out[1]), rhs=float(out[2]))
+    if b is not None:
+        bb = np.asarray(b, float)
+        if not np.array_equal(bb, A.rhs()):
+            res["rhs"] = float(abs(bb.sum()) / np.abs(bb).sum())
+    return res
 
 
 # ---- diagnostics -----------------------------------------------------------------------------------------------------
