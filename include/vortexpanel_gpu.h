@@ -207,6 +207,109 @@ int vp_pressure_force(vp_ctx* ctx, int ntri, const double* corners, const double
 int vp_wake_loads(vp_ctx* ctx, int nte, const double* te_x, int nline, const int* line_ptr, const int* line_nodes,
                   const int* line_closed, const double* mu_w, const double* vinf, double* F_kj, double* D_trefftz);
 
+/* The free wake as a simulation resident on the GPU: FreeWakeSim(g, dm, V∞; opts, assembly), step!(sim), run!(sim, n)
+ * (src/freewake/step.jl:8-58,113-146,205-216) over the state of src/freewake/state.jl:132-147 (node rows newest first
+ * with their shed doublets, mu_line, particles with their merge tags and the strips' merge batches). The host resolves
+ * FreeWakeOptions (state.jl:25-48: te_len, max_rows, merge_rows, the core rule, delete_beyond), builds the trailing
+ * edge panel (te_panel), assembles the body with it and factors the bordered matrix (vp_assemble, vp_factorize); the
+ * set-up hands those and the DOF map to the simulation. A step allocates nothing: the particle arrays hold
+ * particle_capacity particles and grow (a reallocation) only when a step could overflow them. */
+typedef struct vp_freewake vp_freewake;
+
+typedef struct {
+    /* FreeWakeOptions, resolved: the time step; free panel rows kept before the oldest is converted (max_rows); the
+     * CoreRule (state.jl:64-92: core_mode 0 auto, 1 scaled, 2 the fixed radius core_value; overlap, core_factor and
+     * core_floor); advection 0 free, 1 freestream; particles with x.V/|V| above delete_limit are removed
+     * (delete_beyond spans past the trailing edge; +inf keeps all) */
+    double dt;
+    int keep_rows;
+    int core_mode;
+    double overlap, core_factor, core_floor, core_value;
+    int advection;
+    double delete_limit;
+    vp_assembly_options assembly; /* the explicit right hand side's tiers and the precision of the step */
+    /* the body (vp_assemble's inputs), its bordered factorization with the trailing edge panel and that system's b */
+    int nnode;
+    const double* x;
+    int ntri;
+    const int* tris;
+    const int* corner_slot;
+    int nslot;
+    const double* sigma;
+    const double* vinf;
+    const vp_factor* factor;
+    const double* b0;
+    /* the DOF map: C (CSR nslot x nq) gives mu = C q, K (CSR nte x nq) the trailing edge doublets mu_w = K q */
+    int nq;
+    const int* C_rowptr;
+    const int* C_col;
+    const double* C_val;
+    int nte;
+    const int* K_rowptr;
+    const int* K_col;
+    const double* K_val;
+    /* the wake's trailing edge nodes (nte x 3) and lines (as in vp_wake_loads), for Kutta-Joukowski */
+    const double* te_x;
+    int nline;
+    const int* line_ptr;
+    const int* line_nodes;
+    const int* line_closed;
+    /* Topology (state.jl:99-121): strips (nstrip x 2 trailing edge nodes), the first and last nodes of open lines */
+    int nstrip;
+    const int* strips;
+    int nfirst;
+    const int* first_nodes;
+    int nlast;
+    const int* last_nodes;
+    /* the trailing edge panel: its downstream edge (nte x 3, where new rows are shed), and as a rigid wake its nodes
+     * (npw x 3) with the trailing edge node of each (pw_te), triangles (npt x 3) and filaments (npf x 2) */
+    const double* edge;
+    int npw;
+    const double* pw_x;
+    const int* pw_te;
+    int npt;
+    const int* pt_tris;
+    int npf;
+    const int* pf;
+    const int* merge;      /* merge_rows per strip (nstrip), or NULL for no merging */
+    int particle_capacity; /* particles held before the first reallocation */
+} vp_freewake_setup;
+
+/* step!'s record (step.jl:137-139): forces in units of q∞ */
+typedef struct {
+    int n;
+    double t;
+    double F_pressure[3], M_pressure[3], F_kj[3], F_impulse[3], Omega[3], I[3];
+    int rows, particles;
+    double lambda, umax;
+} vp_freewake_record;
+
+typedef struct {
+    int n;            /* steps taken */
+    double t;         /* simulated time */
+    int nrows;        /* node rows (free panel rows + 1; 0 before the first step) */
+    int nparticles;
+    int conversions;
+    double I_prev[3]; /* the last step's impulse (the next F_impulse's backward difference) */
+} vp_freewake_counts;
+
+int vp_freewake_create(vp_ctx* ctx, const vp_freewake_setup* setup, vp_freewake** out);
+/* step!(sim) (step.jl:113-146); rec may be NULL. */
+int vp_freewake_step(vp_freewake* fw, vp_freewake_record* rec);
+int vp_freewake_info(const vp_freewake* fw, vp_freewake_counts* counts);
+/* The state to host arrays (any pointer may be NULL): rows_x (nrows x nte x 3, newest first), rows_mu (nrows x
+ * nte), mu_line (nte), particles (nparticles x 7: x, alpha, delta), tag, group (nparticles), batch_rows,
+ * batch_length, batch_width (nstrip), and the last step's mu (nslot), mu_w (nte) and cp (ntri). */
+int vp_freewake_get_state(const vp_freewake* fw, double* rows_x, double* rows_mu, double* mu_line, double* particles,
+                          int* tag, signed char* group, int* batch_rows, double* batch_length, double* batch_width,
+                          double* mu, double* mu_w, double* cp);
+/* Restore a state taken by vp_freewake_get_state from a simulation of the same body and options (a checkpoint). */
+int vp_freewake_set_state(vp_freewake* fw, const vp_freewake_counts* counts, const double* rows_x,
+                          const double* rows_mu, const double* mu_line, const double* particles, const int* tag,
+                          const signed char* group, const int* batch_rows, const double* batch_length,
+                          const double* batch_width, const double* mu, const double* mu_w, const double* cp);
+void vp_freewake_free(vp_freewake* fw);
+
 /* Condition estimate and size of a factorization. */
 int vp_factor_info(const vp_factor* F, int* n, double* cond);
 void vp_factor_free(vp_factor* F);

@@ -863,3 +863,130 @@ static int assemble_tests(const vpo_options* po, int ntri, const double* x, cons
 }
 
 }  // extern "C"
+
+// ---- the free wake's kernels (src/assembly/explicit.jl, src/post/Post.jl, src/freewake/step.jl) ----
+extern "C" {
+
+// explicit_rhs (explicit.jl:31-85): -int psi_i n.u_src dA per slot of known sheets (nsheet x 9 corners, sheet_mu
+// nsheet x 3), filaments (nseg x 6 ends, seg_g nseg x 2) and particles (nblob x 7: x, alpha, delta). rhs (nslot) is
+// accumulated (the caller zeroes it). Returns -1 for a degenerate body triangle or sheet.
+int vpo_explicit_rhs(const vpo_options* po, const double* x, int ntri, const int* tris, const int* corner_slot,
+                     int nsheet, const double* sheet_x, const double* sheet_mu, int nseg, const double* seg_x,
+                     const double* seg_g, int nblob, const double* blobs, double* rhs, int nthreads) {
+    Options o = to_opts(po);
+    TierRules rules = tier_rules(o);
+    std::vector<FlatTri> els;
+    if (!build_elements(ntri, x, tris, els)) return -1;
+    std::vector<FlatTri> sheets(nsheet);
+    for (int s = 0; s < nsheet; ++s)
+        if (!make_flat_tri(vec_at(sheet_x + 9 * s, 0), vec_at(sheet_x + 9 * s, 1), vec_at(sheet_x + 9 * s, 2), sheets[s]))
+            return -1;
+    std::vector<Segment> segs(nseg);
+    for (int f = 0; f < nseg; ++f) segs[f] = Segment{vec_at(seg_x + 6 * f, 0), vec_at(seg_x + 6 * f, 1)};
+    std::vector<Blob> bl(nblob);
+    for (int k = 0; k < nblob; ++k) bl[k] = Blob{vec_at(blobs + 7 * k, 0), vec_at(blobs + 7 * k + 3, 0), blobs[7 * k + 6]};
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel
+    {
+        Rule rbuf;
+        std::vector<Vec> ufar(rules.far.size());
+#pragma omp for schedule(dynamic, 4)
+        for (int t = 0; t < ntri; ++t) {
+            const FlatTri& T = els[t];
+            double rows[3] = {0, 0, 0};
+            for (int s = 0; s < nsheet; ++s) {
+                int tier;
+                const Rule* rule = wake_pair_rule(T, sheets[s], rules, o, rbuf, tier);
+                double blk[3][3], rb[3];
+                pair_block(T, sheets[s], *rule, 0.0, o.test, 0, o.kernel_far, blk, rb);
+                const double* m = sheet_mu + 3 * s;
+                for (int a = 0; a < 3; ++a) rows[a] -= blk[a][0] * m[0] + blk[a][1] * m[1] + blk[a][2] * m[2];
+            }
+            for (int f = 0; f < nseg; ++f) {
+                int tier;
+                const Rule* rule = segment_rule(T, segs[f], rules, o, rbuf, tier);
+                double ca[3], cb[3];
+                segment_block(T, segs[f], *rule, o.test, ca, cb);
+                for (int a = 0; a < 3; ++a) rows[a] -= ca[a] * seg_g[2 * f] + cb[a] * seg_g[2 * f + 1];
+            }
+            for (auto& u : ufar) u = Vec();
+            for (int k = 0; k < nblob; ++k) {
+                const Blob& b = bl[k];
+                if (norm(b.x - T.c) > o.far_ratio * std::max(T.diam, b.delta)) {
+                    for (size_t q = 0; q < rules.far.size(); ++q)
+                        ufar[q] += blob_velocity(point(T, rules.far.lam[q]), b.x, b.al, b.delta);
+                } else {
+                    near_rule(rbuf, T, b, rules.near_, o.near_ratio, o.near_depth);
+                    for (size_t q = 0; q < rbuf.size(); ++q) {
+                        const Bary& l = rbuf.lam[q];
+                        double un = rbuf.w[q] * T.area * dot(blob_velocity(point(T, l), b.x, b.al, b.delta), T.n);
+                        Vec psi = test_weights(o.test, l);
+                        for (int a = 0; a < 3; ++a) rows[a] -= un * psi[a];
+                    }
+                }
+            }
+            if (nblob > 0)
+                for (size_t q = 0; q < rules.far.size(); ++q) {
+                    double un = rules.far.w[q] * T.area * dot(ufar[q], T.n);
+                    Vec psi = test_weights(o.test, rules.far.lam[q]);
+                    for (int a = 0; a < 3; ++a) rows[a] -= un * psi[a];
+                }
+            const int* ct = corner_slot + 3 * t;
+#pragma omp critical(vpo_rhs)
+            for (int a = 0; a < 3; ++a) rhs[ct[a]] += rows[a];
+        }
+    }
+    return 0;
+}
+
+// body_velocity (Post.jl:92-112): sum over the triangles of sigma_s w_s + gamma_s x w_s at the points X (npts x 3)
+int vpo_body_velocity(const double* corners, int ntri, const double* sigma, const double* gamma, double kernel_far,
+                      int npts, const double* X, double* U, int nthreads) {
+    std::vector<SourceTri<double>> src(ntri);
+    for (int t = 0; t < ntri; ++t)
+        if (!make_source_tri(vec_at(corners + 9 * t, 0), vec_at(corners + 9 * t, 1), vec_at(corners + 9 * t, 2), src[t]))
+            return -1;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < npts; ++i) {
+        const Vec x = vec_at(X, i);
+        Vec acc;
+        for (int t = 0; t < ntri; ++t) {
+            Vec w = source_velocity(src[t], x, 0, kernel_far);
+            acc += sigma[t] * w + cross(vec_at(gamma, t), w);
+        }
+        U[3 * i] = acc.x;
+        U[3 * i + 1] = acc.y;
+        U[3 * i + 2] = acc.z;
+    }
+    return 0;
+}
+
+// blob_velocities (step.jl:176-187): the direct sum of every blob (nblob x 7) at every point
+void vpo_blob_velocities(int nblob, const double* blobs, int npts, const double* X, double* U, int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < npts; ++i) {
+        const Vec x = vec_at(X, i);
+        Vec acc;
+        for (int k = 0; k < nblob; ++k)
+            acc += blob_velocity(x, vec_at(blobs + 7 * k, 0), vec_at(blobs + 7 * k + 3, 0), blobs[7 * k + 6]);
+        U[3 * i] = acc.x;
+        U[3 * i + 1] = acc.y;
+        U[3 * i + 2] = acc.z;
+    }
+}
+
+}  // extern "C"

@@ -1,14 +1,17 @@
-"""The free wake's host bookkeeping (no GPU): core radii and sheet vorticity as the reference's tests state them
+"""The free wake's oracle bookkeeping (no GPU), pinned to the reference's tests: core radii and sheet vorticity
 (test/freewake/test_freewake.jl:15-40), and conversion of panel rows into particles conserving the total vorticity and
 its first moment (:80-98), merging conserving the total vorticity (:100-128), on wake rows built from the generated
-wing with seeded doublets."""
+wing with seeded doublets. The product's option checks and the core of its set-up (first particles, merged batches)
+against the oracle's CoreRule."""
 import math
 
 import numpy as np
 import pytest
 
+import freewake_oracle as fw
+
 from vortexpanel_gpu import api, meshes
-from vortexpanel_gpu import freewake as fw
+from vortexpanel_gpu import freewake as pfw
 
 
 def test_core_radius():
@@ -34,12 +37,31 @@ def test_sheet_vorticity():
 
 
 def test_options():
-    with pytest.raises(ValueError):
-        fw.FreeWakeOptions(dt=0.0).check()
-    with pytest.raises(ValueError):
-        fw.FreeWakeOptions(dt=0.1, advection="x").check()
-    with pytest.raises(NotImplementedError):
-        fw.FreeWakeOptions(dt=0.1, te_direction="bisector").check()
+    for F in (fw.FreeWakeOptions, pfw.FreeWakeOptions):
+        with pytest.raises(ValueError):
+            F(dt=0.0).check()
+        with pytest.raises(ValueError):
+            F(dt=0.1, advection="x").check()
+        with pytest.raises(ValueError):
+            F(dt=0.1, core=-1.0).check()
+        with pytest.raises(NotImplementedError):
+            F(dt=0.1, te_direction="bisector").check()
+
+
+@pytest.mark.parametrize("core", ["auto", "scaled", 0.05])
+def test_product_core_of_quad_matches_oracle(core):
+    V = np.array([0.9, 0.0, 0.2])
+    o = np.zeros(3)
+    ref = fw.CoreRule(fw.FreeWakeOptions(dt=0.02, core=core), V)
+    params = pfw.core_params(pfw.FreeWakeOptions(dt=0.02, core=core), V)
+    for w, l in ((0.25, 0.06), (0.02, 0.3), (0.1, 0.0)):
+        assert math.isclose(pfw.core_of_quad(params, w, l), ref.tri(o, o + [w, 0, 0], o + [w, l, 0]), rel_tol=1e-15)
+
+
+def test_product_topology_matches_oracle():
+    w = meshes.wing(10, 6, aspect=6.0)
+    a, b = fw.Topology.of(w.dm), pfw.Topology.of(w.dm)
+    assert (a.nte, a.segments, a.first_nodes, a.last_nodes) == (b.nte, b.strips, b.first_nodes, b.last_nodes)
 
 
 def _state(w, nrow=6, seed=3):
@@ -114,23 +136,3 @@ def test_state_checkpoint_round_trip(tmp_path):
     assert all(np.array_equal(a, b) for a, b in zip(back.mu, st.mu))
     for k in ("particles", "mu_line", "tag", "group", "batch_rows", "batch_length", "batch_width"):
         assert np.array_equal(getattr(back, k), getattr(st, k)), k
-
-
-def test_sim_checkpoint_restore():
-    # FreeWakeSim.checkpoint / restore on the host fields alone (the device parts of a simulation are not touched)
-    w = meshes.wing(10, 6, aspect=6.0)
-    st, topo = _state(w, nrow=4)
-    sim = object.__new__(fw.FreeWakeSim)
-    sim.state, sim.topo, sim.n, sim.t = st, topo, 5, 0.25
-    sim.mu, sim.mu_w = np.arange(w.dm.nslot, dtype=float), np.ones(topo.nte)
-    sim.cp, sim.I_prev, sim.history = np.zeros(w.g.ntri), np.array([1.0, 2.0, 3.0]), [{"n": 4}]
-    ck = sim.checkpoint()
-    other = object.__new__(fw.FreeWakeSim)
-    other.topo, other.mu = topo, np.zeros(w.dm.nslot)
-    other.restore(ck)
-    assert (other.n, other.t, other.history) == (5, 0.25, [{"n": 4}])
-    assert np.array_equal(other.mu, sim.mu) and np.array_equal(other.I_prev, sim.I_prev)
-    assert all(np.array_equal(a, b) for a, b in zip(other.state.x, st.x))
-    other.mu = np.zeros(w.dm.nslot + 1)
-    with pytest.raises(ValueError):
-        other.restore(ck)

@@ -151,3 +151,23 @@ inline cudaError_t vp_d2h(vp_ctx* ctx, void* h, const void* d, size_t bytes) {
 
 // linear algebra (vp_linalg.cu)
 int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F);
+
+// Device buffers of one right hand side's solve, allocated once by a caller that solves repeatedly (the free wake's
+// steps): vp_solve_work_alloc sizes them for the factorization, vp_solve_work_free releases them.
+struct SolveWork {
+    int n = 0;
+    double *work64 = nullptr, *rhs = nullptr, *res = nullptr;
+    float *f = nullptr, *fw = nullptr;
+};
+int vp_solve_work_alloc(vp_ctx* ctx, const vp_factor* F, SolveWork* w);
+void vp_solve_work_free(SolveWork* w);
+// solve_galerkin(F, b) for one right hand side on the device, with no allocation: b (nslot, device) -> x (n, device:
+// q, then the border unknowns); lambda_k = se_k x[nq + k]. Stream-ordered on the context's stream; the mixed path's
+// refinement reads its residual norms back to the host.
+int vp_solve_dev(vp_ctx* ctx, const vp_factor* F, const double* d_b, double* d_x, SolveWork* w);
+
+// post-processing (vp_post.cu): u, cp and the summed force and moment of the gradient route on device data, launched
+// without a synchronisation; d_part: 6 doubles per 256 triangles, d_out6: F then M
+int vp_post_surface_launch(vp_ctx* ctx, int ntri, const double* d_corners, const int* d_slot, const double* d_mu,
+                           const double* d_dmudt, const double* vinf, const double* origin, double* d_u, double* d_cp,
+                           double* d_part, double* d_out6);

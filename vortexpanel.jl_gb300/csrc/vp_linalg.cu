@@ -427,7 +427,8 @@ int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F) {
 
 // ------------------------------------------------------------------------------------------------------------------
 
-static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool trans, int* iters);
+static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool trans, int* iters,
+                      SolveWork* ws = nullptr);
 
 extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, int nq, const int* C_rowptr,
                             const int* C_col, const double* C_val, int nwake, const int* W_rowptr, const int* W_col,
@@ -635,29 +636,64 @@ extern "C" int vp_factorize(vp_ctx* ctx, const vp_system* sys, int precision, in
     return VP_OK;
 }
 
-// solve in place (x holds the right hand side on entry); VP_MIXED refines with FP64 residuals of M
-static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool trans, int* iters) {
+int vp_solve_work_alloc(vp_ctx* ctx, const vp_factor* F, SolveWork* w) {
+    const size_t n = size_t(F->n);
+    int r;
+    w->n = F->n;
+    if ((r = vp_alloc(ctx, &w->work64, n)) || (r = vp_alloc(ctx, &w->rhs, n)) || (r = vp_alloc(ctx, &w->res, n)) ||
+        (r = vp_alloc(ctx, &w->f, n)) || (r = vp_alloc(ctx, &w->fw, n))) {
+        vp_solve_work_free(w);
+        return r;
+    }
+    return VP_OK;
+}
+
+void vp_solve_work_free(SolveWork* w) {
+    cudaFree(w->work64);
+    cudaFree(w->rhs);
+    cudaFree(w->res);
+    cudaFree(w->f);
+    cudaFree(w->fw);
+    *w = SolveWork();
+}
+
+// solve in place (x holds the right hand side on entry); VP_MIXED refines with FP64 residuals of M. With ws (one
+// right hand side) its buffers are used and nothing is allocated.
+static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool trans, int* iters, SolveWork* ws) {
     const int n = F->n;
     const int* d_perm = F->perm;
     const double norm1 = F->norm1;
     const size_t tot = size_t(n) * nrhs;
     int r;
+    if (ws && (nrhs != 1 || ws->n != n)) return vp_fail(ctx, VP_ERR_ARG, "solve workspace does not fit");
     if (F->precision == VP_FP64) {
         double* work;
-        if ((r = vp_alloc(ctx, &work, tot))) return r;
+        if (ws) {
+            work = ws->work64;
+        } else if ((r = vp_alloc(ctx, &work, tot))) {
+            return r;
+        }
         r = lu_solve<double>(ctx, F, F->LU64, d_perm, nrhs, x, work, trans);
-        cudaFree(work);
+        if (!ws) cudaFree(work);
         if (iters) *iters = 1;
         return r;
     }
     // mixed: x0 = LU32^-1 rhs; r = rhs - M x; x += LU32^-1 r until the residual is at FP64 rounding level
     double *rhs, *res;
     float *f, *fw;
-    if ((r = vp_alloc(ctx, &rhs, tot))) return r;
-    if ((r = vp_alloc(ctx, &res, tot))) { cudaFree(rhs); return r; }
-    if ((r = vp_alloc(ctx, &f, tot))) { cudaFree(rhs); cudaFree(res); return r; }
-    if ((r = vp_alloc(ctx, &fw, tot))) { cudaFree(rhs); cudaFree(res); cudaFree(f); return r; }
+    if (ws) {
+        rhs = ws->rhs;
+        res = ws->res;
+        f = ws->f;
+        fw = ws->fw;
+    } else {
+        if ((r = vp_alloc(ctx, &rhs, tot))) return r;
+        if ((r = vp_alloc(ctx, &res, tot))) { cudaFree(rhs); return r; }
+        if ((r = vp_alloc(ctx, &f, tot))) { cudaFree(rhs); cudaFree(res); return r; }
+        if ((r = vp_alloc(ctx, &fw, tot))) { cudaFree(rhs); cudaFree(res); cudaFree(f); return r; }
+    }
     auto cleanup = [&]() {
+        if (ws) return;
         cudaFree(rhs);
         cudaFree(res);
         cudaFree(f);
@@ -714,6 +750,14 @@ static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool
         return vp_fail(ctx, VP_ERR_NOCONV, "iterative refinement did not converge");
     }
     return VP_OK;
+}
+
+int vp_solve_dev(vp_ctx* ctx, const vp_factor* F, const double* d_b, double* d_x, SolveWork* w) {
+    const int n = F->n;
+    ctb_kernel<<<(n + 255) / 256, 256, 0, ctx->stream>>>(F->nq, n, F->nslot, 1, F->Ct_ptr, F->Ct_col, F->Ct_val, d_b, d_x);
+    ctx->launches++;
+    VP_CUDA(ctx, cudaGetLastError());
+    return solve_core(ctx, F, 1, d_x, false, nullptr, w);
 }
 
 extern "C" int vp_solve(vp_ctx* ctx, const vp_factor* F, int nrhs, const double* b, double* q, double* lambda) {

@@ -365,6 +365,34 @@ extern "C" int vp_consistency(vp_ctx* ctx, const vp_system* sys, int nq, const i
     return VP_OK;
 }
 
+// the gradient route's surface kernel and the ordered sum of its blocks on device data, launched on the context's
+// stream without a synchronisation (the free wake's loads); d_part holds 6 doubles per block of 256 triangles
+int vp_post_surface_launch(vp_ctx* ctx, int ntri, const double* d_corners, const int* d_slot, const double* d_mu,
+                           const double* d_dmudt, const double* vinf, const double* origin, double* d_u, double* d_cp,
+                           double* d_part, double* d_out6) {
+    const int nb = std::max(1, (ntri + RB - 1) / RB);
+    SurfArgs a{};
+    a.ntri = ntri;
+    a.corners = d_corners;
+    a.slot = d_slot;
+    a.mu = d_mu;
+    a.dmudt = d_dmudt;
+    a.cp_in = nullptr;
+    for (int z = 0; z < 3; ++z) {
+        a.V[z] = vinf[z];
+        a.o[z] = origin ? origin[z] : 0.0;
+    }
+    a.V2 = a.V[0] * a.V[0] + a.V[1] * a.V[1] + a.V[2] * a.V[2];
+    a.u_out = d_u;
+    a.cp_out = d_cp;
+    a.part = d_part;
+    surface_kernel<<<nb, RB, 0, ctx->stream>>>(a);
+    sum_parts_kernel<<<1, 32, 0, ctx->stream>>>(nb, 6, d_part, d_out6);
+    ctx->launches += 2;
+    VP_CUDA(ctx, cudaGetLastError());
+    return VP_OK;
+}
+
 static int surface_common(vp_ctx* ctx, int ntri, const double* corners, const int* corner_slot, int nslot,
                           const double* mu, const double* dmudt, const double* cp_in, const double* vinf,
                           const double* origin, double* u, double* cp, double* F, double* M) {

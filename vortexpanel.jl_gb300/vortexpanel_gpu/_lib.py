@@ -29,6 +29,35 @@ class vp_assembly_stats(ctypes.Structure):
                 ("points_fp64", ctypes.c_longlong)]
 
 
+class vp_freewake_setup(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("keep_rows", ctypes.c_int), ("core_mode", ctypes.c_int),
+                ("overlap", ctypes.c_double), ("core_factor", ctypes.c_double), ("core_floor", ctypes.c_double),
+                ("core_value", ctypes.c_double), ("advection", ctypes.c_int), ("delete_limit", ctypes.c_double),
+                ("assembly", vp_assembly_options), ("nnode", ctypes.c_int), ("x", D), ("ntri", ctypes.c_int),
+                ("tris", I), ("corner_slot", I), ("nslot", ctypes.c_int), ("sigma", D), ("vinf", D),
+                ("factor", ctypes.c_void_p), ("b0", D), ("nq", ctypes.c_int), ("C_rowptr", I), ("C_col", I),
+                ("C_val", D), ("nte", ctypes.c_int), ("K_rowptr", I), ("K_col", I), ("K_val", D), ("te_x", D),
+                ("nline", ctypes.c_int), ("line_ptr", I), ("line_nodes", I), ("line_closed", I),
+                ("nstrip", ctypes.c_int), ("strips", I), ("nfirst", ctypes.c_int), ("first_nodes", I),
+                ("nlast", ctypes.c_int), ("last_nodes", I), ("edge", D), ("npw", ctypes.c_int), ("pw_x", D),
+                ("pw_te", I), ("npt", ctypes.c_int), ("pt_tris", I), ("npf", ctypes.c_int), ("pf", I), ("merge", I),
+                ("particle_capacity", ctypes.c_int)]
+
+
+class vp_freewake_record(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("t", ctypes.c_double), ("F_pressure", ctypes.c_double * 3),
+                ("M_pressure", ctypes.c_double * 3), ("F_kj", ctypes.c_double * 3), ("F_impulse", ctypes.c_double * 3),
+                ("Omega", ctypes.c_double * 3), ("I", ctypes.c_double * 3), ("rows", ctypes.c_int),
+                ("particles", ctypes.c_int), ("lam", ctypes.c_double), ("umax", ctypes.c_double)]
+
+
+class vp_freewake_counts(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("t", ctypes.c_double), ("nrows", ctypes.c_int), ("nparticles", ctypes.c_int),
+                ("conversions", ctypes.c_int), ("I_prev", ctypes.c_double * 3)]
+
+
+B8 = ctypes.POINTER(ctypes.c_byte)
+
 # (name, restype, argtypes) of every entry point declared in include/vortexpanel_gpu.h
 SIGNATURES = [
     ("vp_default_options", None, [ctypes.POINTER(vp_assembly_options)]),
@@ -71,6 +100,14 @@ SIGNATURES = [
     ("vp_surface_loads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, D, I, ctypes.c_int, D, D, D, D, D, D, D, D]),
     ("vp_pressure_force", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, D, D, D, D, D]),
     ("vp_wake_loads", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, D, ctypes.c_int, I, I, I, D, D, D, D]),
+    ("vp_freewake_create", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_freewake_setup),
+                                          ctypes.POINTER(ctypes.c_void_p)]),
+    ("vp_freewake_step", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_freewake_record)]),
+    ("vp_freewake_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_freewake_counts)]),
+    ("vp_freewake_get_state", ctypes.c_int, [ctypes.c_void_p, D, D, D, D, I, B8, I, D, D, D, D, D]),
+    ("vp_freewake_set_state", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_freewake_counts), D, D, D, D, I, B8,
+                                             I, D, D, D, D, D]),
+    ("vp_freewake_free", None, [ctypes.c_void_p]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]

@@ -1,12 +1,14 @@
-"""Free wake with vortex particles: FreeWakeSim, step!, run! of src/freewake (state.jl, step.jl) on the GPU path.
+"""Free wake with vortex particles: FreeWakeSim, step!, run! (src/freewake/step.jl) as a simulation resident on the GPU.
 
-The trailing edge panel (a one-row rigid wake closed by its downstream filament) is assembled with the body and the
-bordered matrix factored once (assemble, factorize_galerkin); every step then changes only the right hand side. The
-host keeps the wake's bookkeeping as the reference does (node rows from the newest to the oldest with the doublets
-they were shed with, conversion of the oldest row into particles, merging, deletion); the device does the work that
-scales: the explicit right hand side of the free rows and particles (vp_explicit_rhs), the solve, the body's velocity
-at the wake points (vp_body_velocity) and the blob N-body sum (vp_blob_velocities).
+The host resolves the options as the reference does (te_len, max_rows, merge_rows, the core rule, delete_beyond;
+src/freewake/state.jl:25-92, step.jl:35-58), builds the trailing edge panel, assembles the body with it and factors
+the bordered matrix once (assemble, factorize_galerkin). vp_freewake_create then takes the body, the factors, the DOF
+map and the wake's topology, and every step (vp_freewake_step) runs on the device with no allocation: the free wake's
+elements, explicit_rhs through the assembly's tiers, the solve, the loads, the velocities (body kernels and the blob
+N-body sum), forward Euler, shedding, conversion of the oldest row into particles with merging, and deletion. The
+host receives the step's record.
 
+The one-shot entries blob_velocities, body_velocity and explicit_rhs evaluate the same kernels on host arrays.
 Blobs are arrays of 7 columns: position (3), strength alpha (3), core delta.
 """
 from __future__ import annotations
@@ -18,9 +20,9 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib, api, meshes
-from ._lib import D, check, load
+from ._lib import D, I, check, load
 
-# ---- options and core rule (state.jl:1-92) ----------------------------------------------------------------------------
+# ---- options (state.jl:25-48) and their resolution ---------------------------------------------------------------
 
 
 @dataclass
@@ -41,11 +43,12 @@ class FreeWakeOptions:
     delete_beyond: float = math.inf
 
     def check(self):
+        """check_options (state.jl:50-60): ValueError for the reference's ArgumentError"""
         if not self.dt > 0:
             raise ValueError("dt must be positive")
-        if not (self.max_rows == "auto" or (isinstance(self.max_rows, int) and self.max_rows >= 0)):
+        if self.max_rows != "auto" and not (isinstance(self.max_rows, int) and self.max_rows >= 0):
             raise ValueError("max_rows must be 'auto' or at least 0")
-        if not (self.merge_rows == "auto" or (isinstance(self.merge_rows, int) and self.merge_rows >= 1)):
+        if self.merge_rows != "auto" and not (isinstance(self.merge_rows, int) and self.merge_rows >= 1):
             raise ValueError("merge_rows must be 'auto' or at least 1")
         if self.advection not in ("free", "freestream"):
             raise ValueError(f"advection must be 'free' or 'freestream', not {self.advection}")
@@ -54,280 +57,77 @@ class FreeWakeOptions:
                                       "does not carry; use 'freestream'")
         if self.te_direction != "freestream":
             raise ValueError("te_direction must be 'freestream' or 'bisector'")
-        if not (self.core in ("auto", "scaled") or (isinstance(self.core, (int, float)) and self.core > 0)):
+        if isinstance(self.core, str):
+            if self.core not in ("auto", "scaled"):
+                raise ValueError(f"core must be 'auto', 'scaled' or a positive number, not {self.core}")
+        elif not self.core > 0:
             raise ValueError(f"core must be 'auto', 'scaled' or a positive number, not {self.core}")
         if not (self.overlap > 0 and self.core_factor > 0):
             raise ValueError("overlap and core_factor must be positive")
         return self
 
 
-class CoreRule:
-    """CoreRule (state.jl:64-92): the core of a triangle's particle (p, q, r) or of a filament's blobs (a, b)"""
+_CORE_MODES = {"auto": 0, "scaled": 1}
 
-    def __init__(self, o: FreeWakeOptions, V):
-        self.floor = float(o.core_floor if o.core_floor is not None else np.linalg.norm(V) * o.dt)
-        self.overlap, self.factor = float(o.overlap), float(o.core_factor)
-        self.mode = "fixed" if isinstance(o.core, (int, float)) else o.core
-        self.value = float(o.core) if self.mode == "fixed" else 0.0
 
-    def tri(self, p, q, r):
-        if self.mode == "fixed":
-            return self.value
-        if self.mode == "auto":
-            return self.overlap * max(np.linalg.norm(q - p), np.linalg.norm(r - q), np.linalg.norm(p - r)) / 2
-        return max(self.factor * math.sqrt(np.linalg.norm(np.cross(q - p, r - p))), self.floor)
+def core_params(o: FreeWakeOptions, V):
+    """the CoreRule (state.jl:64-92) as (mode, overlap, factor, floor, value): mode 0 auto, 1 scaled, 2 fixed; the
+    floor defaults to |V∞| dt"""
+    floor = float(o.core_floor if o.core_floor is not None else np.linalg.norm(V) * o.dt)
+    if isinstance(o.core, str):
+        return _CORE_MODES[o.core], float(o.overlap), float(o.core_factor), floor, 0.0
+    return 2, float(o.overlap), float(o.core_factor), floor, float(o.core)
 
-    def seg(self, a, b):
-        if self.mode == "fixed":
-            return self.value
-        if self.mode == "auto":
-            return self.overlap * np.linalg.norm(b - a) / 2
-        return max(self.factor * np.linalg.norm(b - a) / 2, self.floor)
+
+def core_of_quad(params, width, length):
+    """the rule's core of a triangle of a width x length quad: (w,0,0), (w,l,0) from the origin, as the reference
+    sizes the first particles and merged batches (step.jl:68-73, state.jl:360)"""
+    mode, overlap, factor, floor, value = params
+    if mode == 2:
+        return value
+    if mode == 0:
+        return overlap * max(width, length, math.hypot(width, length)) / 2
+    return max(factor * math.sqrt(width * length), floor)
 
 
 @dataclass
 class Topology:
-    """Strips (A, B) of neighbouring wake trailing edge nodes and the end nodes of open lines (state.jl:99-121)"""
+    """the wake's strips (A, B) of neighbouring trailing edge nodes (closed lines wrap around) and the end nodes of
+    open lines (state.jl:99-121)"""
     nte: int
-    segments: list
+    strips: list
     first_nodes: list
     last_nodes: list
 
     @staticmethod
     def of(dm):
         wte = dm.wake_te
-        segs, firsts, lasts = [], [], []
+        strips, firsts, lasts = [], [], []
         for line, closed in zip(wte.lines, wte.closed):
             line = [int(v) for v in line]
-            m = len(line)
-            segs += [(line[i], line[i + 1]) for i in range(m - 1)]
+            strips += list(zip(line[:-1], line[1:]))
             if closed:
-                segs.append((line[m - 1], line[0]))
+                strips.append((line[-1], line[0]))
             else:
                 firsts.append(line[0])
-                lasts.append(line[m - 1])
-        return Topology(len(wte.node), segs, firsts, lasts)
+                lasts.append(line[-1])
+        return Topology(len(wte.node), strips, firsts, lasts)
 
 
-# ---- state and vortex elements (state.jl:132-369) ----------------------------------------------------------------------
+# ---- one-shot device entries ---------------------------------------------------------------------------------------
+
+_PREC = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}
 
 
 @dataclass
-class FreeWakeState:
-    """Node rows x from the newest to the oldest, the doublets mu they were shed with, mu_line, particles (N x 7),
-    conversions and the merge bookkeeping (state.jl:132-147)"""
-    nte: int
-    nstrips: int = 0
-    x: list = field(default_factory=list)
-    mu: list = field(default_factory=list)
-    mu_line: np.ndarray = None
-    particles: np.ndarray = None
-    conversions: int = 0
-    tag: np.ndarray = None
-    group: np.ndarray = None
-    batch_rows: np.ndarray = None
-    batch_length: np.ndarray = None
-    batch_width: np.ndarray = None
-
-    def __post_init__(self):
-        self.mu_line = np.zeros(self.nte)
-        self.particles = np.zeros((0, 7))
-        self.tag = np.zeros(0, int)
-        self.group = np.zeros(0, np.int8)
-        self.batch_rows = np.zeros(self.nstrips, int)
-        self.batch_length = np.zeros(self.nstrips)
-        self.batch_width = np.zeros(self.nstrips)
-
-    def keep_particles(self, keep):
-        self.particles = self.particles[keep]
-        self.tag = self.tag[keep]
-        self.group = self.group[keep]
-
-    def to_arrays(self) -> dict:
-        """the state as named arrays (a checkpoint; the reference keeps it in memory only)"""
-        nr = len(self.x)
-        return {"nte": np.array(self.nte), "nstrips": np.array(self.nstrips),
-                "x": np.array(self.x).reshape(nr, self.nte, 3), "mu": np.array(self.mu).reshape(nr, self.nte),
-                "mu_line": self.mu_line, "particles": self.particles, "conversions": np.array(self.conversions),
-                "tag": self.tag, "group": self.group, "batch_rows": self.batch_rows,
-                "batch_length": self.batch_length, "batch_width": self.batch_width}
-
-    @classmethod
-    def from_arrays(cls, d) -> "FreeWakeState":
-        st = cls(int(d["nte"]), int(d["nstrips"]))
-        st.x = [np.array(r, float) for r in d["x"]]
-        st.mu = [np.array(r, float) for r in d["mu"]]
-        st.conversions = int(d["conversions"])
-        for k in ("mu_line", "particles", "tag", "group", "batch_rows", "batch_length", "batch_width"):
-            setattr(st, k, np.array(d[k]))
-        return st
-
-
-def _nondegenerate(p, q, r):
-    return np.linalg.norm(np.cross(q - p, r - p)) > 1e-12 * max((q - p) @ (q - p), (r - p) @ (r - p), (r - q) @ (r - q))
-
-
-class WakeElements:
-    """Triangles (corners, corner doublets; the nondegenerate ones also as sheets for the right hand side) and filament
-    segments with their end circulations (state.jl:162-200)"""
-
-    def __init__(self):
-        self.corners, self.corner_mu, self.sheets, self.sheet_mu, self.segments, self.segment_g = [], [], [], [], [], []
-
-    def add_sheet(self, p, q, r, mp, mq, mr):
-        self.corners.append((p, q, r))
-        self.corner_mu.append((mp, mq, mr))
-        if _nondegenerate(p, q, r):
-            self.sheets.append((p, q, r))
-            self.sheet_mu.append((mp, mq, mr))
-
-    def add_segment(self, a, b, ga, gb):
-        self.segments.append((a, b))
-        self.segment_g.append((ga, gb))
-
-
-def panel_row(e, st, topo, i):
-    """sheets and tip sides of the panel row between node rows i and i + 1 (state.jl:203-218), 0-based"""
-    x0, x1, m0, m1 = st.x[i], st.x[i + 1], st.mu[i], st.mu[i + 1]
-    for A, B in topo.segments:
-        e.add_sheet(x0[A], x1[A], x0[B], m0[A], m1[A], m0[B])
-        e.add_sheet(x1[A], x1[B], x0[B], m1[A], m1[B], m0[B])
-    for k in topo.first_nodes:
-        e.add_segment(x1[k], x0[k], m1[k], m0[k])
-    for k in topo.last_nodes:
-        e.add_segment(x0[k], x1[k], m0[k], m1[k])
-
-
-def far_end(e, st, topo, i):
-    """the far end filament along node row i, B -> A, strength mu - mu_line (state.jl:221-230)"""
-    x, mu = st.x[i], st.mu[i]
-    for A, B in topo.segments:
-        gA, gB = mu[A] - st.mu_line[A], mu[B] - st.mu_line[B]
-        if gA == 0 and gB == 0:
-            continue
-        e.add_segment(x[B], x[A], gB, gA)
-
-
-def vortex_elements(st: FreeWakeState, topo: Topology):
-    """the free wake's vortex elements (state.jl:241-253)"""
-    e = WakeElements()
-    nr = len(st.x)
-    for i in range(nr - 1):
-        panel_row(e, st, topo, i)
-    if nr >= 1:
-        for A, B in topo.segments:
-            e.add_segment(st.x[0][A], st.x[0][B], st.mu[0][A], st.mu[0][B])
-        far_end(e, st, topo, nr - 1)
-    return e
-
-
-def rigid_elements(w: meshes.RigidWake, mu_w):
-    """vortex elements of a rigid wake with the doublets mu_w of its trailing edge nodes (state.jl:256-265)"""
-    e = WakeElements()
-    mn = np.asarray(mu_w)[w.te]
-    for t in w.tris:
-        e.add_sheet(w.x[t[0]], w.x[t[1]], w.x[t[2]], mn[t[0]], mn[t[1]], mn[t[2]])
-    for a, b in w.filaments:
-        e.add_segment(w.x[a], w.x[b], mn[a], mn[b])
-    return e
-
-
-def sheet_vorticity(p, q, r, mu):
-    """gamma A = sum over edges of (mu_a + mu_b)/2 (x_b - x_a) (state.jl:272)"""
-    return ((mu[0] + mu[1]) * (q - p) + (mu[1] + mu[2]) * (r - q) + (mu[2] + mu[0]) * (p - r)) / 2
-
-
-_GS = 1 / (2 * math.sqrt(3))
-
-
-def segment_blobs(a, b, ga, gb, delta):
-    """two blobs at the 2-point Gauss positions of a filament (blob.jl:31-38)"""
-    out = []
-    for xi in (0.5 - _GS, 0.5 + _GS):
-        al = (((1 - xi) * ga + xi * gb) / 2) * (b - a)
-        out.append(np.concatenate([a + xi * (b - a), al, [delta]]))
-    return out
-
-
-def free_wake_blobs(e: WakeElements, core: CoreRule):
-    """blob representation of vortex elements (state.jl:275-295)"""
-    rows = []
-    for (p, q, r), mu in zip(e.corners, e.corner_mu):
-        rows.append(np.concatenate([(p + q + r) / 3, sheet_vorticity(p, q, r, mu), [core.tri(p, q, r)]]))
-    for (a, b), (ga, gb) in zip(e.segments, e.segment_g):
-        rows += segment_blobs(a, b, ga, gb, core.seg(a, b))
-    return np.array(rows).reshape(-1, 7)
-
-
-def convert_oldest(st: FreeWakeState, topo: Topology, core: CoreRule, merge=None):
-    """convert the oldest panel row into particles (state.jl:300-343); returns the number created"""
-    nr = len(st.x)
-    if nr < 2:
-        return 0
-    e = WakeElements()
-    panel_row(e, st, topo, nr - 2)
-    far_end(e, st, topo, nr - 1)
-    blobs = free_wake_blobs(e, core)
-    tag, group = np.zeros(len(blobs), int), np.zeros(len(blobs), np.int8)
-    if merge is not None:
-        up, down = st.x[nr - 2], st.x[nr - 1]
-        for s, (A, B) in enumerate(topo.segments):
-            k = merge[s]
-            if k <= 1:
-                continue
-            m = k - st.batch_rows[s]
-            for h, (u, v) in enumerate(((1 / 3, 1 / 3), (2 / 3, 2 / 3))):
-                tag[2 * s + h] = s + 1
-                group[2 * s + h] = 1 if u + (m - 1 + v) / k < 1 else 2
-            st.batch_rows[s] += 1
-            st.batch_length[s] += (np.linalg.norm(down[A] - up[A]) + np.linalg.norm(down[B] - up[B])) / 2
-            st.batch_width[s] = np.linalg.norm(up[B] - up[A])
-    st.particles = np.vstack([st.particles, blobs])
-    st.tag = np.concatenate([st.tag, tag])
-    st.group = np.concatenate([st.group, group])
-    st.mu_line = st.mu[nr - 2].copy()
-    st.x.pop()
-    st.mu.pop()
-    st.conversions += 1
-    if merge is not None:
-        for s in range(len(topo.segments)):
-            if merge[s] > 1 and st.batch_rows[s] >= merge[s]:
-                merge_strip(st, s, core)
-    return len(blobs)
-
-
-def merge_strip(st: FreeWakeState, s: int, core: CoreRule):
-    """merge strip s's batch into one particle pair (state.jl:352-373)"""
-    idx = np.flatnonzero(st.tag == s + 1)
-    o = np.zeros(3)
-    delta = core.tri(o, o + np.array([st.batch_width[s], 0, 0]), o + np.array([st.batch_width[s], st.batch_length[s], 0]))
-    merged = []
-    for g in (1, 2):
-        sel = idx[st.group[idx] == g]
-        if len(sel) == 0:
-            continue
-        al = st.particles[sel, 3:6].sum(axis=0)
-        w = np.linalg.norm(st.particles[sel, 3:6], axis=1)
-        x = (w[:, None] * st.particles[sel, :3]).sum(axis=0) / w.sum() if w.sum() > 0 else st.particles[sel, :3].mean(axis=0)
-        merged.append(np.concatenate([x, al, [delta]]))
-    st.keep_particles(st.tag != s + 1)
-    if merged:
-        st.particles = np.vstack([st.particles, np.array(merged)])
-        st.tag = np.concatenate([st.tag, np.zeros(len(merged), int)])
-        st.group = np.concatenate([st.group, np.zeros(len(merged), np.int8)])
-    st.batch_rows[s] = 0
-    st.batch_length[s] = 0.0
-
-
-def vorticity_moments(blobs):
-    """total vorticity and impulse of a set of blobs (state.jl:381-385)"""
-    b = np.asarray(blobs).reshape(-1, 7)
-    return b[:, 3:6].sum(axis=0), np.cross(b[:, :3], b[:, 3:6]).sum(axis=0) / 2
-
-
-# ---- device calls ----------------------------------------------------------------------------------------------------
-
-_PREC = {"fp64": _lib.VP_FP64, "mixed": _lib.VP_MIXED}
+class ExplicitSources:
+    """ExplicitSources (explicit.jl:10-18) as arrays: sheets (n x 9 corners) with their corner doublets (n x 3),
+    filament segments (n x 6 ends) with their end circulations (n x 2), and blobs (n x 7)"""
+    sheets: np.ndarray = field(default_factory=lambda: np.zeros((0, 9)))
+    sheet_mu: np.ndarray = field(default_factory=lambda: np.zeros((0, 3)))
+    segments: np.ndarray = field(default_factory=lambda: np.zeros((0, 6)))
+    segment_gamma: np.ndarray = field(default_factory=lambda: np.zeros((0, 2)))
+    blobs: np.ndarray = field(default_factory=lambda: np.zeros((0, 7)))
 
 
 def blob_velocities(blobs, X, precision="fp64", ctx=None):
@@ -355,39 +155,54 @@ def body_velocity(g, sigma, gamma, X, kernel_far=10.0, precision="fp64", ctx=Non
     return U
 
 
-def explicit_rhs(g, dm, e: WakeElements, blobs, opts: api.AssemblyOptions = None, ctx=None):
-    """-int psi_i n.u dA of the known sheets, filaments and particles, per slot (explicit.jl:31-85), on the GPU"""
+def explicit_rhs(g, dm, src: ExplicitSources, opts: api.AssemblyOptions = None, ctx=None):
+    """-int psi_i n.u dA of known sheets, filaments and particles per slot (explicit.jl:31-85), on the GPU"""
     opts = opts or api.AssemblyOptions()
     ctx = ctx or api.default_context()
     o = opts.c_struct()
     x, px = api._dp(g.x)
     tr, pt = api._ip(g.tris)
     cs, pc = api._ip(dm.corner_slot)
-    sx = np.ascontiguousarray(np.array([np.concatenate(t) for t in e.sheets]).reshape(-1, 9))
-    sm = np.ascontiguousarray(np.array(e.sheet_mu, float).reshape(-1, 3))
-    fx = np.ascontiguousarray(np.array([np.concatenate(s) for s in e.segments]).reshape(-1, 6))
-    fg = np.ascontiguousarray(np.array(e.segment_g, float).reshape(-1, 2))
-    b = np.ascontiguousarray(np.asarray(blobs, float).reshape(-1, 7))
+    sx, psx = api._dp(np.asarray(src.sheets, float).reshape(-1, 9))
+    sm, psm = api._dp(np.asarray(src.sheet_mu, float).reshape(-1, 3))
+    fx, pfx = api._dp(np.asarray(src.segments, float).reshape(-1, 6))
+    fg, pfg = api._dp(np.asarray(src.segment_gamma, float).reshape(-1, 2))
+    b, pb = api._dp(np.asarray(src.blobs, float).reshape(-1, 7))
     rhs = np.zeros(dm.nslot)
-    check(ctx.h, load().vp_explicit_rhs(ctx.h, ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(sx),
-                                       sx.ctypes.data_as(D), sm.ctypes.data_as(D), len(fx), fx.ctypes.data_as(D),
-                                       fg.ctypes.data_as(D), len(b), b.ctypes.data_as(D), rhs.ctypes.data_as(D)))
+    check(ctx.h, load().vp_explicit_rhs(ctx.h, ctypes.byref(o), g.nnode, px, g.ntri, pt, pc, dm.nslot, len(sx), psx,
+                                       psm, len(fx), pfx, pfg, len(b), pb, rhs.ctypes.data_as(D)))
     return rhs
 
 
-# ---- the simulation (step.jl) ----------------------------------------------------------------------------------------
+# ---- the device-resident simulation ----------------------------------------------------------------------------------
+
+vp_freewake_setup, vp_freewake_record, vp_freewake_counts = (_lib.vp_freewake_setup, _lib.vp_freewake_record,
+                                                              _lib.vp_freewake_counts)
 
 
-def sheet_strengths(els, dm, mu):
-    """the vortex sheet gamma of every triangle: sum_b mu_b gamma_b (Post.jl:19-23)"""
-    m = api.element_values(dm, mu)
-    return sum(m[:, k:k + 1] * els.gam[k] for k in range(3))
+@dataclass
+class WakeState:
+    """the device state as host arrays (FreeWakeState, state.jl:132-147): node rows x and their doublets mu, newest
+    first, mu_line, particles (N x 7), conversions, and the merge bookkeeping"""
+    x: list
+    mu: list
+    mu_line: np.ndarray
+    particles: np.ndarray
+    conversions: int
+    tag: np.ndarray
+    group: np.ndarray
+    batch_rows: np.ndarray
+    batch_length: np.ndarray
+    batch_width: np.ndarray
 
 
 class FreeWakeSim:
-    """FreeWakeSim(g, dm, V∞; opts, assembly) (step.jl:8-58) with step() and run(n) (step.jl:113-216)"""
+    """FreeWakeSim(g, dm, V∞; opts, assembly) (step.jl:35-58) with step() and run(n) (step.jl:113-216). The state lives
+    on the GPU; `state` copies it to the host. `capacity` sizes the particle arrays up front (they grow by
+    reallocation between steps when a step could overflow them)."""
 
-    def __init__(self, g, dm, V, opts: FreeWakeOptions, assembly: api.AssemblyOptions = None, ctx=None):
+    def __init__(self, g, dm, V, opts: FreeWakeOptions, assembly: api.AssemblyOptions = None, ctx=None,
+                 capacity: int = 4096):
         opts.check()
         self.g, self.dm, self.V = g, dm, np.asarray(V, float)
         self.opts = opts
@@ -399,135 +214,182 @@ class FreeWakeSim:
         te_len = opts.te_len if opts.te_len is not None else 0.3 * np.linalg.norm(self.V) * opts.dt
         self.te = meshes.te_panel(g, dm, self.V, length=te_len)
         A, self.b0, _ = api.assemble(g, dm, self.els, self.sigma, self.V, opts=self.assembly, wake=self.te, ctx=self.ctx)
-        self.F = api.factorize_galerkin(dm, A, W=meshes.wake_rows(dm, self.te.te), precision=self.precision, ctx=self.ctx)
+        self.F = api.factorize_galerkin(dm, A, W=meshes.wake_rows(dm, self.te.te), precision=self.precision,
+                                        ctx=self.ctx)
         del A
         self.topo = Topology.of(dm)
         nte = self.topo.nte
-        self.edge = self.te.x[nte:2 * nte].copy()  # the trailing edge panel's downstream edge (its row 1)
-        self.core = CoreRule(opts, self.V)
+        self.edge = np.ascontiguousarray(self.te.x[nte:2 * nte])  # the panel's downstream edge (its row 1)
+        self.core = core_params(opts, self.V)
         row = np.linalg.norm(self.V) * opts.dt
-        te_rows1 = self.te.rows[1]
-        if opts.max_rows == "auto":
-            self.keep_rows = self._rows_for_distance(3, te_rows1, row)
+        widths = [float(np.linalg.norm(self.edge[B] - self.edge[A])) for A, B in self.topo.strips]
+        if opts.max_rows == "auto":  # rows_for_distance(3, ...) (step.jl:80-82)
+            first = core_of_quad(self.core, max(widths), row)
+            self.keep_rows = max(0, math.ceil((3 * first - self.te.rows[1]) / row - 0.5))
         else:
             self.keep_rows = int(opts.max_rows)
-        widths = [np.linalg.norm(self.edge[B] - self.edge[A]) for A, B in self.topo.segments]
         if opts.merge_rows == "auto":
             self.merge = [max(1, int(round(w / row))) for w in widths]
         elif opts.merge_rows == 1:
             self.merge = None
         else:
             self.merge = [int(opts.merge_rows)] * len(widths)
-        self.state = FreeWakeState(nte, len(self.topo.segments))
-        self.n, self.t = 0, 0.0
-        self.mu = np.zeros(dm.nslot)
-        self.mu_w = np.zeros(nte)
-        self.cp = np.zeros(g.ntri)
-        self.I_prev = np.zeros(3)
+        d = self.V / np.linalg.norm(self.V)
+        delete = float((self.edge @ d).max() + opts.delete_beyond * self.te.span) if math.isfinite(
+            opts.delete_beyond) else math.inf
         self.history = []
+        self._create(delete, capacity)
 
-    def _first_core(self, row):
-        w = max(np.linalg.norm(self.edge[B] - self.edge[A]) for A, B in self.topo.segments)
-        o = np.zeros(3)
-        return self.core.tri(o, o + np.array([w, 0, 0]), o + np.array([w, row, 0]))
+    def _create(self, delete_limit, capacity):
+        g, dm, o = self.g, self.dm, self.opts
+        keep = []  # arrays the set-up points into, alive for the call
 
-    def _rows_for_distance(self, cores, te_len, row):
-        """the fewest rows that create the first particles at least `cores` cores behind the trailing edge
-        (step.jl:80-82)"""
-        return max(0, math.ceil((cores * self._first_core(row) - te_len) / row - 0.5))
+        def dp(a):
+            a = np.ascontiguousarray(np.asarray(a, float))
+            keep.append(a)
+            return a.ctypes.data_as(D)
 
-    def _te_blobs(self, mu_w):
-        return free_wake_blobs(rigid_elements(self.te, mu_w), self.core)
+        def ip(a):
+            a = np.ascontiguousarray(np.asarray(a, np.int32))
+            if a.size == 0:
+                a = np.zeros(1, np.int32)
+            keep.append(a)
+            return a.ctypes.data_as(I)
+
+        s = vp_freewake_setup()
+        s.dt, s.keep_rows = float(o.dt), int(self.keep_rows)
+        s.core_mode, s.overlap, s.core_factor, s.core_floor, s.core_value = self.core
+        s.advection = 0 if o.advection == "free" else 1
+        s.delete_limit = delete_limit
+        s.assembly = self.assembly.c_struct()
+        s.nnode, s.x, s.ntri, s.tris, s.corner_slot = g.nnode, dp(g.x), g.ntri, ip(g.tris), ip(dm.corner_slot)
+        s.nslot, s.sigma, s.vinf, s.factor, s.b0 = dm.nslot, dp(self.sigma), dp(self.V), self.F.h, dp(self.b0)
+        C, K = dm.C.tocsr(), dm.K.tocsr()
+        s.nq, s.C_rowptr, s.C_col, s.C_val = dm.nq, ip(C.indptr), ip(C.indices), dp(C.data if C.nnz else [0.0])
+        s.nte, s.K_rowptr, s.K_col, s.K_val = self.topo.nte, ip(K.indptr), ip(K.indices), dp(K.data if K.nnz else [0.0])
+        wte = dm.wake_te
+        lines = [np.asarray(L, np.int32) for L in wte.lines]
+        s.te_x = dp(wte.x)
+        s.nline = len(lines)
+        s.line_ptr = ip(np.concatenate([[0], np.cumsum([len(L) for L in lines])]))
+        s.line_nodes = ip(np.concatenate(lines) if lines else [])
+        s.line_closed = ip([int(bool(c)) for c in wte.closed])
+        s.nstrip, s.strips = len(self.topo.strips), ip(np.asarray(self.topo.strips).reshape(-1))
+        s.nfirst, s.first_nodes = len(self.topo.first_nodes), ip(self.topo.first_nodes)
+        s.nlast, s.last_nodes = len(self.topo.last_nodes), ip(self.topo.last_nodes)
+        s.edge = dp(self.edge)
+        te = self.te
+        s.npw, s.pw_x, s.pw_te = len(te.x), dp(te.x), ip(te.te)
+        s.npt, s.pt_tris = len(te.tris), ip(np.asarray(te.tris).reshape(-1))
+        s.npf, s.pf = len(te.filaments), ip(np.asarray(te.filaments).reshape(-1))
+        s.merge = ip(self.merge) if self.merge is not None else None
+        s.particle_capacity = int(capacity)
+        h = ctypes.c_void_p()
+        check(self.ctx.h, load().vp_freewake_create(self.ctx.h, ctypes.byref(s), ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                load().vp_freewake_free(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+    # -- the steps --
+    def counts(self):
+        c = vp_freewake_counts()
+        check(self.ctx.h, load().vp_freewake_info(self.h, ctypes.byref(c)))
+        return c
+
+    @property
+    def n(self):
+        return self.counts().n
+
+    @property
+    def t(self):
+        return self.counts().t
 
     def step(self):
-        """one time step in MESA's order (step.jl:113-146); returns the step's record"""
-        st, o, dm = self.state, self.opts, self.dm
-        we = vortex_elements(st, self.topo)
-        rhs = explicit_rhs(self.g, dm, we, st.particles, opts=self.assembly, ctx=self.ctx)
-        sol = api.solve_galerkin(self.F, self.b0 + rhs)
-        mu_w = dm.K @ sol["q"]
-        loads = self._loads(sol, mu_w, we)
-        if not st.x:
-            st.x.append(self.edge.copy())
-            st.mu.append(mu_w.copy())
-        X = np.vstack(st.x + [st.particles[:, :3]])
-        U = self._velocities(sol, mu_w, we, X)
-        nrow = sum(len(r) for r in st.x)
-        k = 0
-        for r in st.x:
-            r += o.dt * U[k:k + len(r)]
-            k += len(r)
-        st.particles[:, :3] += o.dt * U[nrow:]
-        st.x.insert(0, self.edge.copy())
-        st.mu.insert(0, mu_w.copy())
-        while len(st.x) - 1 > self.keep_rows:
-            convert_oldest(st, self.topo, self.core, self.merge)
-        if math.isfinite(o.delete_beyond):
-            self._delete_far()
-        rec = dict(n=self.n, t=self.t, **loads, rows=len(st.x) - 1, particles=len(st.particles),
-                   lam=float(np.atleast_1d(sol["lam"])[0]) if np.size(sol["lam"]) else 0.0,
-                   umax=float(np.linalg.norm(U, axis=1).max()) if len(U) else 0.0)
+        """step!(sim) (step.jl:113-146): one time step on the GPU; returns its record"""
+        r = vp_freewake_record()
+        check(self.ctx.h, load().vp_freewake_step(self.h, ctypes.byref(r)))
+        mu_w = np.zeros(self.topo.nte)
+        check(self.ctx.h, load().vp_freewake_get_state(self.h, None, None, None, None, None, None, None, None, None,
+                                                       None, mu_w.ctypes.data_as(D), None))
+        rec = dict(n=r.n, t=r.t, mu_w=mu_w, F_pressure=np.array(r.F_pressure), M_pressure=np.array(r.M_pressure),
+                   F_kj=np.array(r.F_kj), F_impulse=np.array(r.F_impulse), Omega=np.array(r.Omega), I=np.array(r.I),
+                   rows=r.rows, particles=r.particles, lam=r.lam, umax=r.umax)
         self.history.append(rec)
-        self.mu, self.mu_w = sol["mu"], mu_w
-        self.n += 1
-        self.t += o.dt
         return rec
 
-    def _loads(self, sol, mu_w, we):
-        """the loads of the solved state (step.jl:149-163)"""
-        dm, els, V = self.dm, self.els, self.V
-        u = api.gradient_velocity(els, dm, sol["mu"], V)
-        dmu = np.zeros(dm.nslot) if self.n == 0 else (sol["mu"] - self.mu) / self.opts.dt
-        cp = api.pressure_coefficient(u, V, api.element_values(dm, dmu).mean(axis=1))
-        self.cp = cp
-        Fp, Mp = api.pressure_force(els, cp)
-        Fkj = api.kutta_joukowski_force(dm.wake_te, mu_w, V)
-        gam = sheet_strengths(els, dm, sol["mu"])
-        body = np.hstack([els.centroid, gam * els.area[:, None], np.zeros((len(els.area), 1))])
-        blobs = np.vstack([body, self._te_blobs(mu_w), free_wake_blobs(we, self.core), self.state.particles])
-        Om, I = vorticity_moments(blobs)
-        Fimp = np.full(3, np.nan) if self.n == 0 else -(2 / (V @ V)) * (I - self.I_prev) / self.opts.dt
-        self.I_prev = I
-        return dict(mu_w=mu_w, F_pressure=Fp, M_pressure=Mp, F_kj=Fkj, F_impulse=Fimp, Omega=Om, I=I)
-
-    def _velocities(self, sol, mu_w, we, X):
-        """V∞ + the body (exact kernels) + every wake element as blobs at the points X (step.jl:166-173)"""
-        V = self.V
-        if self.opts.advection == "freestream":
-            return np.tile(V, (len(X), 1))
-        gam = sheet_strengths(self.els, self.dm, sol["mu"])
-        ub = body_velocity(self.g, self.sigma, gam, X, kernel_far=self.assembly.kernel_far, precision=self.precision,
-                           ctx=self.ctx)
-        blobs = np.vstack([self._te_blobs(mu_w), free_wake_blobs(we, self.core), self.state.particles])
-        uw = blob_velocities(blobs, X, precision=self.precision, ctx=self.ctx)
-        return V + ub + uw
-
-    def _delete_far(self):
-        """remove the particles beyond delete_beyond spans downstream of the trailing edge (step.jl:190-195)"""
-        d = self.V / np.linalg.norm(self.V)
-        limit = (self.edge @ d).max() + self.opts.delete_beyond * self.te.span
-        self.state.keep_particles(self.state.particles[:, :3] @ d <= limit)
-
-    def checkpoint(self) -> dict:
-        """the simulation's evolving state (wake, step count, time, last solution, impulse, history): restore() on a
-        FreeWakeSim built with the same body, options and assembly continues from it"""
-        return {"state": self.state.to_arrays(), "n": self.n, "t": self.t, "mu": self.mu.copy(),
-                "mu_w": self.mu_w.copy(), "cp": self.cp.copy(), "I_prev": self.I_prev.copy(),
-                "history": list(self.history)}
-
-    def restore(self, ckpt: dict):
-        if ckpt["state"]["x"].shape[1:] != (self.topo.nte, 3) or ckpt["mu"].shape != self.mu.shape:
-            raise ValueError("the checkpoint is of another wing or DOF map")
-        self.state = FreeWakeState.from_arrays(ckpt["state"])
-        self.n, self.t = int(ckpt["n"]), float(ckpt["t"])
-        self.mu, self.mu_w, self.cp = ckpt["mu"].copy(), ckpt["mu_w"].copy(), ckpt["cp"].copy()
-        self.I_prev = ckpt["I_prev"].copy()
-        self.history = list(ckpt["history"])
-
     def run(self, nsteps, progress=None):
-        """take nsteps steps (step.jl:205-216); returns the history"""
+        """run!(sim, n) (step.jl:205-216): take nsteps steps; returns the history"""
         for _ in range(nsteps):
             rec = self.step()
             if progress is not None:
                 progress(self, rec)
         return self.history
+
+    # -- the state on the host --
+    def _get(self):
+        c = self.counts()
+        nte, ns = self.topo.nte, len(self.topo.strips)
+        a = dict(rows_x=np.zeros((c.nrows, nte, 3)), rows_mu=np.zeros((c.nrows, nte)), mu_line=np.zeros(nte),
+                 particles=np.zeros((c.nparticles, 7)), tag=np.zeros(c.nparticles, np.int32),
+                 group=np.zeros(c.nparticles, np.int8), batch_rows=np.zeros(ns, np.int32), batch_length=np.zeros(ns),
+                 batch_width=np.zeros(ns), mu=np.zeros(self.dm.nslot), mu_w=np.zeros(nte), cp=np.zeros(self.g.ntri))
+        ptr = {k: (v.ctypes.data_as(I) if v.dtype == np.int32 else
+                   v.ctypes.data_as(ctypes.POINTER(ctypes.c_byte)) if v.dtype == np.int8 else v.ctypes.data_as(D))
+               for k, v in a.items()}
+        check(self.ctx.h, load().vp_freewake_get_state(
+            self.h, ptr["rows_x"], ptr["rows_mu"], ptr["mu_line"], ptr["particles"], ptr["tag"], ptr["group"],
+            ptr["batch_rows"], ptr["batch_length"], ptr["batch_width"], ptr["mu"], ptr["mu_w"], ptr["cp"]))
+        return c, a
+
+    @property
+    def state(self) -> WakeState:
+        c, a = self._get()
+        return WakeState(x=list(a["rows_x"]), mu=list(a["rows_mu"]), mu_line=a["mu_line"], particles=a["particles"],
+                         conversions=c.conversions, tag=a["tag"], group=a["group"], batch_rows=a["batch_rows"],
+                         batch_length=a["batch_length"], batch_width=a["batch_width"])
+
+    @property
+    def mu(self):
+        return self._get()[1]["mu"]
+
+    @property
+    def cp(self):
+        """the pressure coefficient of the last step"""
+        return self._get()[1]["cp"]
+
+    def checkpoint(self) -> dict:
+        """the simulation's evolving state as named arrays, and its history: restore() on a FreeWakeSim of the same
+        body, options and assembly continues from it"""
+        c, a = self._get()
+        a.update(n=np.array(c.n), t=np.array(c.t), nrows=np.array(c.nrows), conversions=np.array(c.conversions),
+                 I_prev=np.array(c.I_prev))
+        return {"state": a, "history": list(self.history)}
+
+    def restore(self, ckpt: dict):
+        a = ckpt["state"]
+        nte = self.topo.nte
+        if a["rows_x"].shape[1:] != (nte, 3) or a["mu"].shape != (self.dm.nslot,):
+            raise ValueError("the checkpoint is of another wing or DOF map")
+        c = vp_freewake_counts()
+        c.n, c.t, c.nrows = int(a["n"]), float(a["t"]), int(a["nrows"])
+        c.nparticles, c.conversions = len(a["particles"]), int(a["conversions"])
+        for z in range(3):
+            c.I_prev[z] = float(a["I_prev"][z])
+        arr = {k: np.ascontiguousarray(v) for k, v in a.items()}
+        tag = np.ascontiguousarray(arr["tag"], np.int32)
+        group = np.ascontiguousarray(arr["group"], np.int8)
+        brows = np.ascontiguousarray(arr["batch_rows"], np.int32)
+        part = np.ascontiguousarray(arr["particles"], float).reshape(-1, 7)
+        check(self.ctx.h, load().vp_freewake_set_state(
+            self.h, ctypes.byref(c), arr["rows_x"].ctypes.data_as(D), arr["rows_mu"].ctypes.data_as(D),
+            arr["mu_line"].ctypes.data_as(D), part.ctypes.data_as(D), tag.ctypes.data_as(I),
+            group.ctypes.data_as(ctypes.POINTER(ctypes.c_byte)), brows.ctypes.data_as(I),
+            arr["batch_length"].ctypes.data_as(D), arr["batch_width"].ctypes.data_as(D), arr["mu"].ctypes.data_as(D),
+            arr["mu_w"].ctypes.data_as(D), arr["cp"].ctypes.data_as(D)))
+        self.history = list(ckpt["history"])
