@@ -1,10 +1,15 @@
-"""Benchmark of the Galerkin hot path on the 25k-triangle lifting wing.
+"""Benchmark of the Galerkin hot path on the 25k-triangle lifting wing, and of the free wake.
 
 Workload: rectangular wing of aspect ratio 8, NACA 0012 section, 112 full-cosine chordwise x 56 full-cosine spanwise
 panels per side (25,088 surface + 444 cap triangles, 12.9k unknowns), rigid wake 2.5 spans (20 chords) long along +x
 with tip filaments, alpha = 5 deg. One step = assemble (all tiers) + factorize (bordered LU) + solve + loads (CL by
-pressure, CDi by Trefftz) through the library, in mixed precision (FP32 far/near tiers and LU, FP64 touching tiers and
-refinement). The plain FP64 GPU path is timed on the same workload for the comparison, with |dCL| and |dCDi|.
+pressure, CDi by Trefftz) + the adjoint gradients of CL and CDi with respect to every node and alpha, through the
+library, in mixed precision (FP32 far/near tiers and LU, FP64 touching tiers and refinement). The plain FP64 GPU path
+is timed on the same workload for the comparison, with |dCL| and |dCDi|. The free wake line runs 500 steps of the
+6,556-triangle wing at alpha 8 deg (dt 0.02, core 0.05) on the GPU and times step! at the end.
+
+The reference arm (--impl reference) runs the reference's path on the host cores: the oracle (C++ restatement of the
+assembly) and LAPACK through scipy, whole unsampled steps (no adjoint: the reference has none).
 
 Every N > 1 rank runs an independent replica (the solve of one wing does not shard in this build).
 
@@ -149,45 +154,74 @@ def nbody(vp, ctx, n=400_000, reps=3):
                          "unit": "TFLOP/s", "frac": ach / peak, "peak_source": "nominal"}}
 
 
-def cpu_baseline(w, wake, W, V, budget_s=20.0, rows=None):
-    """The oracle (C++ restatement of the reference's assembly, OpenMP over test triangles as assemble.jl:395, and the
-    reference's LAPACK dgetrf/dgetrs through scipy) on a bounded sample: the rows of a slice of test triangles, and
-    the LU of a leading principal block; scaled to the full step (rows linearly, the LU by n^3). The slice grows
-    until it takes about budget_s / 4, unless `rows` fixes it (the returned "rows" of an earlier sample)."""
+def cpu_step(w, wake, W, V):
+    """One step of the reference's path on all host cores, unsampled: the oracle (the C++ restatement of the
+    reference's assembly, OpenMP over test triangles as assemble.jl:395) assembles every row of A and b, then the
+    bordered matrix, the reference's LAPACK dgetrf and dgecon through scipy, the solve, and the loads (CL by the pressure
+    route, CDi by Trefftz). The reference has no adjoint (it differentiates with ForwardDiff), so the CPU step has
+    none."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    import scipy.linalg as sla
 
     oracle.build()
-    from vortexpanel_gpu import api
-
-    els = api.build_elements(w.g)
-    sig = api.source_strengths(els, V)
-    nt = w.g.ntri
     cores = os.cpu_count() or 1
-    # assembly: grow the slice until it takes a measurable time
-    fixed = rows is not None
-    rows = rows if fixed else max(8, nt // 2000)
-    while True:
-        t0 = time.perf_counter()
-        oracle.assemble(w.g, w.dm, sig, V, wake=wake, rows=(nt // 2, nt // 2 + rows), nthreads=cores)
-        ta = time.perf_counter() - t0
-        if fixed or ta > budget_s / 4 or rows >= nt // 4:
-            break
-        rows = min(nt // 4, int(rows * max(2.0, (budget_s / 4) / max(ta, 1e-3))))
-    t_asm = ta * nt / rows
-    n = w.dm.nq + 1
-    m = min(n, 4000)
-    M = np.random.default_rng(1).standard_normal((m, m)) + m * np.eye(m)
     t0 = time.perf_counter()
-    lu = sla.lu_factor(M, check_finite=False)
-    sla.lu_solve(lu, np.ones(m), check_finite=False)
-    tl = time.perf_counter() - t0
-    t_lu = tl * (n / m) ** 3
-    return {"value": t_asm + t_lu, "unit": "s", "cores": cores, "kind": "port",
-            "sample": f"oracle assembly of {rows} of {nt} test-triangle rows ({ta:.1f} s, scaled x{nt / rows:.0f}) + "
-                      f"scipy/LAPACK dgetrf of a {m}x{m} block ({tl:.2f} s, scaled by (n/m)^3 to n={n})",
-            "assembly_s": t_asm, "lu_s": t_lu, "rows": rows}
+    sig = oracle.source_strengths(w.g, V)
+    A, b, _ = oracle.assemble(w.g, w.dm, sig, V, wake=wake, nthreads=cores)
+    t1 = time.perf_counter()
+    sol = oracle.solve_galerkin(w.dm, A, b, W=W)
+    del A
+    t2 = time.perf_counter()
+    els = oracle.elements(w.g)
+    cp = oracle.pressure_coefficient(oracle.gradient_velocity(w.g, w.dm, sol["mu"], V, els=els), V)
+    a = math.radians(ALPHA)
+    S = w.span * w.chord
+    CL = float(oracle.pressure_force(els, cp)[0] @ np.array([-math.sin(a), 0.0, math.cos(a)]) / S)
+    CDi = float(oracle.trefftz_drag(w.dm.wake_te, w.dm.K @ sol["q"], V) / S)
+    t3 = time.perf_counter()
+    return {"value": t3 - t0, "unit": "s", "cores": cores, "kind": "port", "assembly_s": t1 - t0,
+            "factor_solve_s": t2 - t1, "loads_s": t3 - t2, "CL": CL, "CDi": CDi}
+
+
+CPU_SAMPLE = ("the whole step, unsampled: oracle assembly of all {ntri} test-triangle rows ({asm:.1f} s), bordered matrix "
+              "+ scipy/LAPACK dgetrf + dgecon + solve ({fs:.1f} s), loads ({ld:.2f} s); no adjoint (the reference "
+              "differentiates with ForwardDiff and has no adjoint)")
+
+
+def freewake_bench(vp, ctx, steps=500):
+    """The free wake of the wing of 40 x 40 panels per side (6,556 triangles), alpha = 8 deg, |V∞| = 1, dt = 0.02
+    chord, particle core 0.05 chord, mixed precision, `steps` steps of the device-resident FreeWakeSim from an
+    impulsive start: the time per step! at the end of the run (the last 50 steps: wall time per call and device time
+    from CUDA events) at its particle count, beside the reference's published 1.8 s per step at 32,684 particles
+    (its README, 16 threads)"""
+    from vortexpanel_gpu import freewake as fwk
+
+    w = vp.meshes.wing(40, 40, aspect=8.0)
+    a = math.radians(8.0)
+    V = np.array([math.cos(a), 0.0, math.sin(a)])
+    eL = np.array([-math.sin(a), 0.0, math.cos(a)])
+    t0 = time.perf_counter()
+    sim = fwk.FreeWakeSim(w.g, w.dm, V, fwk.FreeWakeOptions(dt=0.02, core=0.05),
+                          assembly=vp.AssemblyOptions(precision="mixed"), ctx=ctx, capacity=50_000)
+    t_setup = time.perf_counter() - t0
+    last = min(50, steps)
+    t0 = time.perf_counter()
+    for _ in range(steps - last):
+        sim.step()
+    ctx.phase_times(reset=True)
+    t1 = time.perf_counter()
+    for _ in range(last):
+        rec = sim.step()
+    t2 = time.perf_counter()
+    ph, launches = ctx.phase_times(reset=True)
+    S = w.span * w.chord
+    return {"workload": f"wing AR8 NACA0012 40x40/side ({w.g.ntri} tris), alpha 8 deg, dt 0.02, core 0.05, mixed",
+            "steps": steps, "particles": rec["particles"], "rows": rec["rows"], "setup_s": t_setup,
+            "run_s": t2 - t0, "ms_per_step_wall": (t2 - t1) / last * 1e3,
+            "ms_per_step_device": (ph["wake"] + ph["solve"]) / last, "launches_per_step": launches / last,
+            "CL_pressure_last": float(rec["F_pressure"] @ eL / S), "CL_kj_last": float(rec["F_kj"] @ eL / S),
+            "reference_published": {"ms_per_step": 1800.0, "particles": 32684,
+                                    "source": "VortexPanel.jl README, free wake L2, 16 threads, author's CPU"}}
 
 
 def dist_setup(n_gpus):
@@ -260,6 +294,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--freewake-steps", type=int, default=500)
     ap.add_argument("--workload", default="wing25k", choices=list(SIZES),
                     help="wing25k (the measured configuration); medium (56x28 per side) and small (28x14) for profiler captures")
     args = ap.parse_args()
@@ -275,17 +310,23 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # W untimed samples (the first sizes the slice), then K timed ones; each is a bounded sample of the step
-        cb = cpu_baseline(w, wake, W, V)
-        for _ in range(max(0, args.warmup - 1)):
-            cpu_baseline(w, wake, W, V, rows=cb["rows"])
-        runs = [cpu_baseline(w, wake, W, V, rows=cb["rows"]) for _ in range(max(1, args.steps))]
+        # the reference's path on the host cores, whole steps of about half a minute each: at most one untimed and
+        # three timed, so that the run ends in a few minutes whatever --steps and --warmup ask for
+        nw, nt = min(1, args.warmup), min(3, max(1, args.steps))
+        for _ in range(nw):
+            cpu_step(w, wake, W, V)
+        runs = [cpu_step(w, wake, W, V) for _ in range(nt)]
         cb = dict(runs[-1], value=statistics.mean(r["value"] for r in runs))
-        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": world, "steps": len(runs),
-                "warmup": max(1, args.warmup), "ms_per_step": cb["value"] * 1e3, "higher_is_better": False,
+        sample = CPU_SAMPLE.format(ntri=w.g.ntri, asm=cb["assembly_s"], fs=cb["factor_solve_s"], ld=cb["loads_s"])
+        sample += f"; {nt} timed steps after {nw} untimed (asked for {args.steps} and {args.warmup})"
+        line = {"metric": METRIC, "value": cb["value"], "unit": "s", "n_gpus": world, "steps": nt,
+                "warmup": nw, "requested_steps": args.steps, "requested_warmup": args.warmup,
+                "ms_per_step": cb["value"] * 1e3, "higher_is_better": False,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic", "config": config, "impl": "reference",
-                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "cpu_baseline": {"value": cb["value"], "unit": "s", "cores": cb["cores"], "kind": "port",
+                                 "sample": sample},
+                "CL": cb["CL"], "CDi": cb["CDi"],
                 "e2e": {"value": cb["value"], "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -351,9 +392,14 @@ def main():
             "kernels": kernels}
     line.update(fp)
     line["nbody"] = nbody(vp, ctx)
+    if args.freewake_steps > 0:
+        line["freewake"] = freewake_bench(vp, ctx, args.freewake_steps)
     if not args.no_cpu_baseline:
-        cb = cpu_baseline(w, wake, W, V)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cb = cpu_step(w, wake, W, V)
+        line["cpu_baseline"] = {"value": cb["value"], "unit": "s", "cores": cb["cores"], "kind": "port",
+                                "sample": CPU_SAMPLE.format(ntri=w.g.ntri, asm=cb["assembly_s"],
+                                                            fs=cb["factor_solve_s"], ld=cb["loads_s"]) +
+                                "; one step"}
     print(json.dumps(line))
 
 
