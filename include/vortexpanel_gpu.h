@@ -310,6 +310,12 @@ int vp_freewake_set_state(vp_freewake* fw, const vp_freewake_counts* counts, con
                           const double* batch_width, const double* mu, const double* mu_w, const double* cp);
 void vp_freewake_free(vp_freewake* fw);
 
+/* Diagnostics (no counterpart in the reference): C -= A B for FP32 column-major host arrays A (m x k, lda), B (k x n,
+ * ldb), C (m x n, ldc) through the tensor-core GEMM of the mixed-precision LU's trailing updates (each operand split
+ * into three bf16 pieces, six tcgen05 products accumulated in FP32). */
+int vp_gemm_sub_f32(vp_ctx* ctx, int m, int n, int k, const float* A, int lda, const float* B, int ldb, float* C,
+                    int ldc);
+
 /* Condition estimate and size of a factorization. */
 int vp_factor_info(const vp_factor* F, int* n, double* cond);
 void vp_factor_free(vp_factor* F);

@@ -105,6 +105,7 @@ void vp_ctx_destroy(vp_ctx* ctx) {
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     vp_phase_flush(ctx);
     if (ctx->d_flag) cudaFree(ctx->d_flag);
+    vp_tc_work_free(&ctx->tc);
     if (ctx->blas) cublasDestroy(ctx->blas);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

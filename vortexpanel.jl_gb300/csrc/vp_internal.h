@@ -28,6 +28,15 @@ enum {
     PH_COUNT
 };
 
+// buffers of the tensor-core GEMM of the LU's trailing updates (vp_tcgemm.cu): the bf16 pieces of its operands,
+// grown to the largest update seen, and its error word
+struct TcWork {
+    void* pieces = nullptr;  // bf16 elements
+    size_t cap = 0;          // elements
+    int* err = nullptr;
+    bool attr_set = false;
+};
+
 struct vp_ctx {
     int device = 0;
     int nsm = 0;
@@ -40,6 +49,7 @@ struct vp_ctx {
     long long launches = 0;
     long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies made by the library
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    TcWork tc;
 };
 
 // record the start/end of a phase on the context's stream; vp_phase_flush() accumulates the elapsed times
@@ -165,6 +175,15 @@ void vp_solve_work_free(SolveWork* w);
 // q, then the border unknowns); lambda_k = se_k x[nq + k]. Stream-ordered on the context's stream; the mixed path's
 // refinement reads its residual norms back to the host.
 int vp_solve_dev(vp_ctx* ctx, const vp_factor* F, const double* d_b, double* d_x, SolveWork* w);
+
+// the tensor-core GEMM (vp_tcgemm.cu): C -= A B, FP32 column-major, as three-piece bf16 splits with six tcgen05
+// products accumulated in FP32 in TMEM; stream-ordered, errors of its bounded waits read by vp_tc_gemm_check
+bool vp_tc_gemm_enabled();
+bool vp_tc_gemm_fits(int m, int n, int k);
+int vp_tc_gemm_sub(vp_ctx* ctx, int m, int n, int k, const float* A, int lda, const float* B, int ldb, float* C,
+                   int ldc);
+int vp_tc_gemm_check(vp_ctx* ctx);
+void vp_tc_work_free(TcWork* w);
 
 // post-processing (vp_post.cu): u, cp and the summed force and moment of the gradient route on device data, launched
 // without a synchronisation; d_part: 6 doubles per 256 triangles, d_out6: F then M

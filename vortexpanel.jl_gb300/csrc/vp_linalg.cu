@@ -6,8 +6,10 @@
 //  - LU with partial pivoting (the reference calls LAPACK dgetrf): recursive (left half, swap, TRSM, GEMM, right
 //    half). Its leaf panels (m x 16 columns) are factored by one thread-block cluster of 8 CTAs that holds the panel
 //    in distributed shared memory: per column, every CTA finds its pivot candidate, one cluster barrier, every CTA
-//    reads the 8 candidates and the pivot row through DSMEM, swaps and updates its rows. TRSM and GEMM are cuBLAS
-//    in FP64 (VP_FP64) and FP32 (VP_MIXED);
+//    reads the 8 candidates and the pivot row through DSMEM, swaps and updates its rows. TRSM is cuBLAS; the
+//    trailing-update GEMM is cuBLAS DGEMM for VP_FP64 and, for VP_MIXED, the tensor-core GEMM of vp_tcgemm.cu
+//    (three-piece bf16 split, six tcgen05 products accumulated in FP32 in TMEM) for updates of at least one
+//    128 x 128 x 64 tile, cuBLAS SGEMM for the smaller ones;
 //  - VP_MIXED keeps the FP64 bordered matrix and refines every solve with FP64 residuals (iterative refinement) to
 //    FP64 accuracy;
 //  - the 1-norm condition estimate of dgecon (Hager/Higham, as LAPACK dlacn2) from solves with M and M'.
@@ -272,6 +274,9 @@ int gemm_sub<double>(vp_ctx* ctx, int m, int n, int k, const double* A, int lda,
 template <>
 int gemm_sub<float>(vp_ctx* ctx, int m, int n, int k, const float* A, int lda, const float* B, int ldb, float* C,
                     int ldc) {
+    // the trailing updates large enough for a 128 x 128 tile run on the tensor cores (three-piece bf16 split, FP32
+    // accumulation in TMEM: FP32-class products); the small ones on cuBLAS
+    if (vp_tc_gemm_enabled() && vp_tc_gemm_fits(m, n, k)) return vp_tc_gemm_sub(ctx, m, n, k, A, lda, B, ldb, C, ldc);
     const float one = 1.0f, mone = -1.0f;
     VP_BLAS(ctx, cublasSgemm(ctx->blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &mone, A, lda, B, ldb, &one, C, ldc));
     return VP_OK;
@@ -409,6 +414,7 @@ int vp_lu_factor(vp_ctx* ctx, int precision, int n, double* M64, vp_factor* F) {
         int lw = leaf_width<float>(n);
         if (!lw) return vp_fail(ctx, VP_ERR_ARG, "matrix too large for the LU panel");
         r = rgetrf<float>(ctx, F->LU32, n, 0, n, lw, F->ipiv, d_info);
+        if (!r) r = vp_tc_gemm_check(ctx);
     }
     if (r) {
         cudaFree(d_info);

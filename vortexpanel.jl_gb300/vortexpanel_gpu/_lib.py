@@ -108,6 +108,8 @@ SIGNATURES = [
     ("vp_freewake_set_state", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(vp_freewake_counts), D, D, D, D, I, B8,
                                              I, D, D, D, D, D]),
     ("vp_freewake_free", None, [ctypes.c_void_p]),
+    ("vp_gemm_sub_f32", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, F32, ctypes.c_int,
+                                       F32, ctypes.c_int, F32, ctypes.c_int]),
     ("vp_factor_info", ctypes.c_int, [ctypes.c_void_p, I, D]),
     ("vp_factor_free", None, [ctypes.c_void_p]),
 ]
