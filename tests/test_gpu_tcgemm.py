@@ -1,9 +1,10 @@
 """The tensor-core GEMM of the mixed-precision LU's trailing updates (vp_gemm_sub_f32 through the C ABI: C -= A B,
 FP32 column-major, each operand split into three bf16 pieces, six tcgen05 products accumulated in FP32 in TMEM)
-against the FP64 product of the same FP32 inputs. FP32-class accuracy: within 2e-6 of max |A||B| (a bf16 product
-would be ~4e-3 off, a two-piece split ~1e-5), with ragged sizes, leading dimensions larger than the rows, and k
-below, at and above one 64-wide slice; and the bordered LU with the tensor cores against the same LU on cuBLAS
-SGEMM: the refined solutions agree to FP64 rounding."""
+against the FP64 product of the same FP32 inputs. FP32-class accuracy: its error is within 3x that of an FP32 GEMM
+of the same inputs (numpy's, FP32 accumulation) and within 1e-5 of max |A||B|; a plain bf16 product (2^-8 per term)
+or a two-piece split (2^-16) would be hundreds of times worse per term. Ragged sizes, leading dimensions larger than
+the rows, and k below, at and above one 64-wide slice. And the bordered LU with the tensor cores against the same LU
+on cuBLAS SGEMM: the refined solutions agree to FP64 rounding."""
 import ctypes
 import os
 import subprocess
@@ -45,7 +46,8 @@ def test_tensor_core_gemm_is_fp32_class(vp, m, n, k, pad):
     ref = C.astype(np.float64) - A.astype(np.float64) @ B.astype(np.float64)
     scale = (np.abs(A).astype(np.float64) @ np.abs(B).astype(np.float64)).max()
     err = np.abs(got - ref).max() / scale
-    assert err < 2e-6, err
+    err32 = np.abs((C - A @ B).astype(np.float64) - ref).max() / scale  # an FP32 GEMM's error on the same inputs
+    assert err < 3 * err32 + 1e-9 and err < 1e-5, (err, err32)
     # the padded leading dimensions' extra rows of C are untouched: only the m x n block changes
     assert np.isfinite(got).all()
 

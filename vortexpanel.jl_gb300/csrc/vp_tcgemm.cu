@@ -5,16 +5,18 @@
 // Each FP32 operand is split into three bf16 pieces, x = x1 + x2 + x3, each piece the bf16 rounding of what the
 // previous ones leave (3 x 8 significant bits cover FP32's 24). The six products whose orders reach FP32's precision,
 // A1B1 + A1B2 + A2B1 + A1B3 + A2B2 + A3B1, are accumulated in FP32 in tensor memory (the dropped A2B3, A3B2, A3B3 lie
-// below 2^-24 |A||B|), so the factors keep FP32 accuracy and the FP64 refinement converges as with FP32 factors.
+// below 2^-24 |A||B|), so the factors keep FP32 accuracy and the FP64 refinement converges as with FP32 factors. A1B1
+// and the five smaller products go to two accumulators, added in the epilogue, so that the small terms are not
+// rounded against the large sum at every step.
 //
 // Layout: a split kernel writes the pieces K-major (A3[p][row][k], B3[p][col][k], bf16, k padded to 64, rows to
 // 128). One CTA per 128 x 128 tile of C, 128 threads:
 //   - thread 0 stages 64-wide k-slices of the six operand tiles with TMA (cp.async.bulk.tensor, 128-byte swizzle, this
 //     GPU's own memory, no multicast) into two shared-memory stages of 96 KB, paced by mbarriers;
-//   - thread 32 issues tcgen05.mma (kind::f16, bf16 operands, M 128, N 128, K 16) into a 128-column FP32 accumulator
-//     in TMEM, 24 per k-slice, and frees each stage with tcgen05.commit;
-//   - the four warps read the accumulator back with tcgen05.ld (warp w holds rows 32w..32w+31) and subtract it from C
-//     (coalesced along C's columns).
+//   - thread 32 issues tcgen05.mma (kind::f16, bf16 operands, M 128, N 128, K 16) into two 128-column FP32
+//     accumulators in TMEM, 24 per k-slice, and frees each stage with tcgen05.commit;
+//   - the four warps read the accumulators back with tcgen05.ld (warp w holds rows 32w..32w+31) and subtract their
+//     sum from C (coalesced along C's columns).
 // Every mbarrier wait has an iteration limit: a wait that gives up sets the error word, the CTA skips the rest of its
 // work and still frees its TMEM; the host reports VP_ERR_TIMEOUT.
 #include <cuda.h>
@@ -32,7 +34,7 @@ constexpr int TC_PIECES = 3, TC_STAGES = 2, TC_THREADS = 128;
 constexpr int TC_TILE_BYTES = TC_BM * TC_BK * 2;                       // 16 KB: one 128 x 64 bf16 tile
 constexpr int TC_STAGE_BYTES = 2 * TC_PIECES * TC_TILE_BYTES;          // 96 KB: three A and three B tiles
 constexpr int TC_SMEM = TC_STAGES * TC_STAGE_BYTES + 1024;             // + alignment to 1024 bytes
-constexpr int TC_TMEM_COLS = 128;                                      // FP32 accumulator 128 lanes x 128 columns
+constexpr int TC_TMEM_COLS = 256;  // two FP32 accumulators of 128 lanes x 128 columns: A1B1, and the five small products
 constexpr long long TC_WAIT_LIMIT = 1LL << 22;                         // iterations of a bounded mbarrier wait
 
 // the six products (A piece, B piece) of the three-piece split that reach FP32's precision
@@ -145,6 +147,19 @@ __device__ __forceinline__ void mma_bf16(uint32_t tmem, uint64_t ad, uint64_t bd
         : "memory");
 }
 
+// 32 consecutive FP32 columns of this warp's 32 TMEM lanes (one row per thread)
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* v) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+          "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]), "=r"(v[16]),
+          "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]), "=r"(v[24]),
+          "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+        : "r"(taddr)
+        : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -197,7 +212,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
             }
         }
     } else if (threadIdx.x == 32) {  // MMA issuer
-        int issued = 0;
+        int issued_hi = 0, issued_lo = 0;
         for (int kt = 0; kt < ktiles; ++kt) {
             const int s = kt % TC_STAGES;
             if (!mbar_wait(smem_u32(&full_bar[s]), uint32_t((kt / TC_STAGES) & 1), err)) {
@@ -209,7 +224,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
                 for (int q = 0; q < 6; ++q) {
                     const uint64_t ad = smem_desc(tileA(s, c_prod_a[q]) + uint32_t(kk * 32));
                     const uint64_t bd = smem_desc(tileB(s, c_prod_b[q]) + uint32_t(kk * 32));
-                    mma_bf16(tmem, ad, bd, issued++ > 0 ? 1u : 0u);
+                    if (q == 0)
+                        mma_bf16(tmem, ad, bd, issued_hi++ > 0 ? 1u : 0u);
+                    else
+                        mma_bf16(tmem + uint32_t(TC_BN), ad, bd, issued_lo++ > 0 ? 1u : 0u);
                 }
             mma_commit(smem_u32(&empty_bar[s]));
         }
@@ -223,24 +241,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (done && !s_fail) {
         const int row = m0 + warp * 32 + lane;
         for (int c0 = 0; c0 < TC_BN; c0 += 32) {
-            uint32_t v[32];
+            uint32_t v[32], u[32];
             const uint32_t taddr = tmem + (uint32_t(warp * 32) << 16) + uint32_t(c0);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-                "%14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
-                  "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]),
-                  "=r"(v[23]), "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]),
-                  "=r"(v[30]), "=r"(v[31])
-                : "r"(taddr)
-                : "memory");
+            tmem_ld32(taddr, v);
+            tmem_ld32(taddr + uint32_t(TC_BN), u);
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (row < m)
 #pragma unroll
                 for (int j = 0; j < 32; ++j) {
                     const int col = n0 + c0 + j;
-                    if (col < n) C[size_t(col) * ldc + row] -= __uint_as_float(v[j]);
+                    if (col < n) C[size_t(col) * ldc + row] -= __uint_as_float(v[j]) + __uint_as_float(u[j]);
                 }
         }
     }
