@@ -218,7 +218,9 @@ def freewake_bench(vp, ctx, steps=500):
     return {"workload": f"wing AR8 NACA0012 40x40/side ({w.g.ntri} tris), alpha 8 deg, dt 0.02, core 0.05, mixed",
             "steps": steps, "particles": rec["particles"], "rows": rec["rows"], "setup_s": t_setup,
             "run_s": t2 - t0, "ms_per_step_wall": (t2 - t1) / last * 1e3,
-            "ms_per_step_device": (ph["wake"] + ph["solve"]) / last, "launches_per_step": launches / last,
+            "ms_per_step_device": (ph["wake"] + ph["solve"] + ph["wake_rhs"] + ph["wake_vel"]) / last,
+            "phases_ms_per_step": {k: ph[k] / last for k in ("wake_rhs", "wake_vel", "solve", "wake")},
+            "launches_per_step": launches / last,
             "CL_pressure_last": float(rec["F_pressure"] @ eL / S), "CL_kj_last": float(rec["F_kj"] @ eL / S),
             "reference_published": {"ms_per_step": 1800.0, "particles": 32684,
                                     "source": "VortexPanel.jl README, free wake L2, 16 threads, author's CPU"}}

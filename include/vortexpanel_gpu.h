@@ -133,8 +133,8 @@ int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const do
  * since the last reset, measured with CUDA events on the context's stream, in the order setup, classify, far, near
  * (near tier and the adding of the pair blocks), reduce, lu, cond, solve, adjoint setup, adjoint far, adjoint near
  * (near tier, filaments, freestream), adjoint solve, free wake, near pairs (the touching and contact pairs of the
- * assembly), adjoint pairs (those of the adjoint) (n entries at most), and the number of this library's kernel
- * launches. */
+ * assembly), adjoint pairs (those of the adjoint), the free wake simulation's explicit right hand side and its
+ * velocities (n entries at most), and the number of this library's kernel launches. */
 int vp_phase_times(vp_ctx* ctx, double* ms, int n, long long* launches, int reset);
 /* Instrumentation (no counterpart in the reference): bytes copied host->device and device->host by the library. */
 int vp_transfer_bytes(vp_ctx* ctx, long long* h2d, long long* d2h, int reset);

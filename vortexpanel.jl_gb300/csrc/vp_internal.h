@@ -25,6 +25,8 @@ enum {
     PH_WAKE,        // free wake: blob sums, body velocity, explicit right hand side of particles
     PH_NEAR_PAIRS,  // near_kernel_pairs alone (the touching and contact pairs of the assembly)
     PH_ADJ_PAIRS,   // adj_pairs_kernel alone (the touching and contact pairs of the adjoint)
+    PH_WAKE_RHS,    // free wake simulation: the explicit right hand side kernels
+    PH_WAKE_VEL,    // free wake simulation: the body and blob velocities at the wake points
     PH_COUNT
 };
 

@@ -441,6 +441,238 @@ __global__ void csr_mv_kernel(int nrow, const int* __restrict__ p, const int* __
     y[i] = s;
 }
 
+// ---- the mixed path's FP32 kernels of the particles' right hand side and of the body velocity ----------------------
+// Both are N-body sums in FP32 with FP64 accumulation across tiles. Offsets are formed from hi/lo FP32 splits of the
+// FP64 positions ((x_hi - y_hi) + (x_lo - y_lo): the first difference is exact where it matters), so they keep FP64
+// accuracy near the wing. A 2-D grid spreads the targets over blocks and the sources over chunks; each chunk's
+// partial sums go to their own slot and are added in chunk order (no atomics, bit-reproducible). The rare pairs that
+// need the reference's near rule or FP64 (a particle within far_ratio of a test triangle, a point where the FP32 exact
+// kernel cancels, a distance within rounding of a switch) take the FP64 path of the same pair.
+
+constexpr int NB_CHUNK = 1024;  // sources per chunk of the 2-D N-body grids
+constexpr int NB_TPB = 128;     // targets per block
+
+__device__ __forceinline__ void split_hi_lo(double x, float& hi, float& lo) {
+    hi = float(x);
+    lo = float(x - double(hi));
+}
+
+// per particle: (x_hi, delta^2), (x_lo, delta), alpha / 4 pi
+__global__ void particle_prep_kernel(int n, const double* __restrict__ part, float4* __restrict__ ph,
+                                     float4* __restrict__ pl, float4* __restrict__ pa) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double* p = part + 7 * size_t(i);
+    float h[3], l[3];
+    for (int z = 0; z < 3; ++z) split_hi_lo(p[z], h[z], l[z]);
+    const float i4pi = 1.f / (4.f * vp_pi<float>());
+    ph[i] = make_float4(h[0], h[1], h[2], float(p[6] * p[6]));
+    pl[i] = make_float4(l[0], l[1], l[2], float(p[6]));
+    pa[i] = make_float4(float(p[3]) * i4pi, float(p[4]) * i4pi, float(p[5]) * i4pi, 0.f);
+}
+
+struct PRhsArgs {
+    int ntri, npart, nchunk;
+    const TriGeo* tri;
+    const double* part;  // npart x 7 (the FP64 path of near and ambiguous pairs)
+    const float4* ph;
+    const float4* pl;
+    const float4* pa;
+    ParticleRule pr;
+    double* out;         // nchunk x ntri x 3
+};
+
+// one thread per body test triangle (its far-rule points), the block's chunk of particles through shared memory:
+// -int psi_a n.u dA of every particle of the chunk (explicit.jl:63-76)
+__global__ void __launch_bounds__(NB_TPB) particle_rhs_kernel(PRhsArgs a) {
+    __shared__ float4 sh[NB_TPB], sl[NB_TPB], sa[NB_TPB];
+    const int t = blockIdx.x * NB_TPB + threadIdx.x;
+    const bool valid = t < a.ntri;
+    const TriGeo& Tr = a.tri[valid ? t : 0];
+    const int nf = a.pr.nfar;
+    float qh[NQMAX][3], ql[NQMAX][3];
+    double U[NQMAX][3];
+    float ch[3], cl[3];
+    for (int z = 0; z < 3; ++z) split_hi_lo(Tr.c[z], ch[z], cl[z]);
+#pragma unroll
+    for (int q = 0; q < NQMAX; ++q) {
+        const RulePt m = a.pr.rfar[q < nf ? q : 0];
+        const v3<double> x = tpoint(Tr, &m.l0);
+        split_hi_lo(x.x, qh[q][0], ql[q][0]);
+        split_hi_lo(x.y, qh[q][1], ql[q][1]);
+        split_hi_lo(x.z, qh[q][2], ql[q][2]);
+        U[q][0] = U[q][1] = U[q][2] = 0.0;
+    }
+    const float diam = float(Tr.diam), fr = float(a.pr.far_ratio);
+    double rows[3] = {0, 0, 0};
+    const int j0 = blockIdx.y * NB_CHUNK, j1 = min(a.npart, j0 + NB_CHUNK);
+    for (int b0 = j0; b0 < j1; b0 += NB_TPB) {
+        const int nb = min(NB_TPB, j1 - b0);
+        __syncthreads();
+        if (threadIdx.x < nb) {
+            sh[threadIdx.x] = a.ph[b0 + threadIdx.x];
+            sl[threadIdx.x] = a.pl[b0 + threadIdx.x];
+            sa[threadIdx.x] = a.pa[b0 + threadIdx.x];
+        }
+        __syncthreads();
+        if (!valid) continue;
+        float u[NQMAX][3];
+#pragma unroll
+        for (int q = 0; q < NQMAX; ++q) u[q][0] = u[q][1] = u[q][2] = 0.f;
+        for (int k = 0; k < nb; ++k) {
+            const float4 h = sh[k], l = sl[k], al = sa[k];
+            const float dx = (ch[0] - h.x) + (cl[0] - l.x), dy = (ch[1] - h.y) + (cl[1] - l.y),
+                        dz = (ch[2] - h.z) + (cl[2] - l.z);
+            const float d2 = dx * dx + dy * dy + dz * dz;
+            const float thr = fr * fmaxf(diam, l.w);
+            if (d2 > thr * thr * 1.00001f) {  // far, beyond rounding: the far rule's points in FP32
+#pragma unroll
+                for (int q = 0; q < NQMAX; ++q) {
+                    if (q >= nf) break;
+                    const float rx = (qh[q][0] - h.x) + (ql[q][0] - l.x), ry = (qh[q][1] - h.y) + (ql[q][1] - l.y),
+                                rz = (qh[q][2] - h.z) + (ql[q][2] - l.z);
+                    const float r2 = fmaf(rx, rx, fmaf(ry, ry, fmaf(rz, rz, h.w)));
+                    const float inv = rsqrtf(r2);
+                    const float sc = inv * inv * inv;
+                    u[q][0] = fmaf(sc, al.y * rz - al.z * ry, u[q][0]);
+                    u[q][1] = fmaf(sc, al.z * rx - al.x * rz, u[q][1]);
+                    u[q][2] = fmaf(sc, al.x * ry - al.y * rx, u[q][2]);
+                }
+            } else {  // near, or within rounding of the switch: the reference's decision and rule in FP64
+                particle_rows<float>(a.pr, Tr, a.part + 7 * size_t(b0 + k), rows);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < NQMAX; ++q)
+            for (int z = 0; z < 3; ++z) U[q][z] += double(u[q][z]);
+    }
+    if (!valid) return;
+#pragma unroll
+    for (int q = 0; q < NQMAX; ++q) {
+        if (q >= nf) break;
+        const RulePt m = a.pr.rfar[q];
+        const double un = (m.w * Tr.area) * (U[q][0] * Tr.n[0] + U[q][1] * Tr.n[1] + U[q][2] * Tr.n[2]);
+        const v3<double> psi = test_weights(a.pr.test_mode, m.l0, m.l1, m.l2);
+        rows[0] -= un * psi.x;
+        rows[1] -= un * psi.y;
+        rows[2] -= un * psi.z;
+    }
+    double* o = a.out + (size_t(blockIdx.y) * a.ntri + t) * 3;
+    o[0] = rows[0];
+    o[1] = rows[1];
+    o[2] = rows[2];
+}
+
+// out[i] += the chunks' partial sums of element i, in chunk order
+__global__ void add_chunks_kernel(int n, int nchunk, const double* __restrict__ part, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = out[i];
+    for (int c = 0; c < nchunk; ++c) v += part[size_t(c) * n + i];
+    out[i] = v;
+}
+
+// body triangles as FP32 sources: centroid hi (3) and lo (3), corner offsets (9), edge normals (9), edge lengths (3),
+// normal (3), area, diameter, sigma, gamma (3): 37 floats
+constexpr int BS32 = 37;
+
+__global__ void body_src32_kernel(int ntri, const BodySrc* __restrict__ bs, float* __restrict__ out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ntri) return;
+    const BodySrc& b = bs[t];
+    float* o = out + size_t(t) * BS32;
+    for (int z = 0; z < 3; ++z) split_hi_lo(b.c[z], o[z], o[3 + z]);
+    for (int k = 0; k < 9; ++k) {
+        o[6 + k] = float(b.d[k]);
+        o[15 + k] = float(b.nu[k]);
+    }
+    for (int k = 0; k < 3; ++k) {
+        o[24 + k] = float(b.len[k]);
+        o[27 + k] = float(b.n[k]);
+        o[33 + k] = float(b.gam[k]);
+    }
+    o[30] = float(b.area);
+    o[31] = float(b.diam);
+    o[32] = float(b.sigma);
+}
+
+struct BVelArgs {
+    int ntri, npts, nchunk;
+    const float* src32;    // ntri x BS32
+    const BodySrc* src64;  // the FP64 sources (guarded points, ambiguous far tests)
+    const double* X;       // npts x 3
+    double kernel_far;
+    double* out;           // nchunk x npts x 3
+};
+
+constexpr int BV_TILE = 64;
+
+// one thread per point, the block's chunk of body triangles through shared memory: sigma_s w_s + gamma_s x w_s
+// (body_velocity, Post.jl:92-112): the multipole beyond kernel_far diameters, the exact kernel in FP32 under the
+// guard within, FP64 where the guard refuses or the far switch is within rounding
+__global__ void __launch_bounds__(NB_TPB) body_vel_kernel(BVelArgs a) {
+    __shared__ float ss[BV_TILE * BS32];
+    const int i = blockIdx.x * NB_TPB + threadIdx.x;
+    const bool valid = i < a.npts;
+    const v3<double> x = valid ? ld3(a.X + 3 * size_t(i)) : mk3(0.0, 0.0, 0.0);
+    float xh[3], xl[3];
+    split_hi_lo(x.x, xh[0], xl[0]);
+    split_hi_lo(x.y, xh[1], xl[1]);
+    split_hi_lo(x.z, xh[2], xl[2]);
+    const float kf = float(a.kernel_far);
+    const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+    v3<double> acc = mk3(0.0, 0.0, 0.0);
+    const int s0 = blockIdx.y * NB_CHUNK, s1 = min(a.ntri, s0 + NB_CHUNK);
+    for (int t0 = s0; t0 < s1; t0 += BV_TILE) {
+        const int nt = min(BV_TILE, s1 - t0);
+        __syncthreads();
+        for (int k = threadIdx.x; k < nt * BS32; k += NB_TPB) ss[k] = a.src32[size_t(t0) * BS32 + k];
+        __syncthreads();
+        if (!valid) continue;
+        v3<float> part = mk3(0.f, 0.f, 0.f);
+        for (int k = 0; k < nt; ++k) {
+            const float* o = ss + k * BS32;
+            const v3<float> r = mk3((xh[0] - o[0]) + (xl[0] - o[3]), (xh[1] - o[1]) + (xl[1] - o[4]),
+                                    (xh[2] - o[2]) + (xl[2] - o[5]));
+            SrcKern<float> K;
+            for (int e = 0; e < 3; ++e) {
+                K.d[e] = mk3(o[6 + 3 * e], o[7 + 3 * e], o[8 + 3 * e]);
+                K.nu[e] = mk3(o[15 + 3 * e], o[16 + 3 * e], o[17 + 3 * e]);
+                K.len[e] = o[24 + e];
+            }
+            K.n = mk3(o[27], o[28], o[29]);
+            K.area = o[30];
+            K.diam = o[31];
+            const float fd = kf * K.diam;
+            const float r2 = dot(r, r);
+            v3<float> w;
+            bool ok = true;
+            if (r2 > fd * fd * 1.00001f) {
+                w = sv_far(K, r);
+            } else if (r2 < fd * fd * 0.99999f) {
+                ok = sv_exact3_guarded(K, r - K.d[0], r - K.d[1], r - K.d[2], 0, g, w);
+            } else {
+                ok = false;
+            }
+            if (ok) {
+                const v3<float> gm = mk3(o[33], o[34], o[35]);
+                part += o[32] * w + cross(gm, w);
+            } else {  // FP64: the reference's far switch and kernel for this pair
+                const BodySrc& b = a.src64[t0 + k];
+                SrcKern<double> K64 = kern_from<double>(b);
+                const v3<double> w64 = sv_rel(K64, x - mk3(b.c[0], b.c[1], b.c[2]), 0, a.kernel_far, 1e-12);
+                acc += b.sigma * w64 + cross(mk3(b.gam[0], b.gam[1], b.gam[2]), w64);
+            }
+        }
+        acc += mk3(double(part.x), double(part.y), double(part.z));
+    }
+    if (!valid) return;
+    double* out = a.out + (size_t(blockIdx.y) * a.npts + i) * 3;
+    out[0] = acc.x;
+    out[1] = acc.y;
+    out[2] = acc.z;
+}
+
 // ---- 3. the loads --------------------------------------------------------------------------------------------------
 
 // dmu/dt by backward difference (zero on the first step), the sheets gamma of the body triangles from mu
@@ -887,7 +1119,11 @@ struct vp_freewake {
     int* sheet_ok = nullptr;
     double *blobs = nullptr, *X = nullptr, *ub = nullptr, *uw = nullptr, *umax_part = nullptr;
     double *trow = nullptr, *rhs = nullptr, *x = nullptr, *mu = nullptr, *mu_prev = nullptr, *dmu = nullptr;
-    double *cp = nullptr, *surf_part = nullptr, *mom_part = nullptr, *rec = nullptr;  // rec: the record (see step)
+    double *cp = nullptr, *surf_part = nullptr, *mom_part = nullptr, *rec = nullptr;
+    // the mixed path's FP32 N-body kernels: the particles as FP32 splits, the chunks' partial sums, the body sources
+    float4 *ph = nullptr, *pl = nullptr, *pa = nullptr;
+    double *prhs = nullptr, *bvel = nullptr;
+    float* src32 = nullptr;  // rec: the record (see step)
     SolveWork sw;
     double I_prev[3] = {0, 0, 0};
     std::vector<double> h_rec;
@@ -928,16 +1164,21 @@ int ensure_capacity(vp_freewake* fw, int need) {
     if (need <= fw->cap) return VP_OK;
     vp_ctx* ctx = fw->ctx;
     const int cap = std::max(need, 2 * fw->cap);
-    double *part, *blobs, *X, *ub, *uw, *umax_part, *mom_part;
+    double *part, *blobs, *X, *ub, *uw, *umax_part, *mom_part, *prhs, *bvel;
+    float4 *ph, *pl, *pa;
     int* tag;
     signed char* group;
     int r;
     const size_t nb = blob_cap(fw, cap), npnt = point_cap(fw, cap);
+    const size_t pchunks = (size_t(cap) + NB_CHUNK - 1) / NB_CHUNK, bchunks = (size_t(fw->ntri) + NB_CHUNK - 1) / NB_CHUNK;
     if ((r = own_alloc(fw, &part, 7 * size_t(cap))) || (r = own_alloc(fw, &tag, size_t(cap))) ||
         (r = own_alloc(fw, &group, size_t(cap))) || (r = own_alloc(fw, &blobs, 7 * nb)) ||
         (r = own_alloc(fw, &X, 3 * npnt)) || (r = own_alloc(fw, &ub, 3 * npnt)) || (r = own_alloc(fw, &uw, 3 * npnt)) ||
         (r = own_alloc(fw, &umax_part, (npnt + 255) / 256 + 1)) ||
-        (r = own_alloc(fw, &mom_part, 6 * ((size_t(fw->ntri) + nb + 255) / 256 + 1))))
+        (r = own_alloc(fw, &mom_part, 6 * ((size_t(fw->ntri) + nb + 255) / 256 + 1))) ||
+        (r = own_alloc(fw, &ph, size_t(cap))) || (r = own_alloc(fw, &pl, size_t(cap))) ||
+        (r = own_alloc(fw, &pa, size_t(cap))) || (r = own_alloc(fw, &prhs, pchunks * fw->ntri * 3)) ||
+        (r = own_alloc(fw, &bvel, bchunks * npnt * 3)))
         return r;
     if (fw->np > 0) {
         VP_CUDA(ctx, cudaMemcpyAsync(part, fw->part, sizeof(double) * 7 * fw->np, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -946,10 +1187,12 @@ int ensure_capacity(vp_freewake* fw, int need) {
     }
     VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     for (void* p : {(void*)fw->part, (void*)fw->tag, (void*)fw->group, (void*)fw->blobs, (void*)fw->X, (void*)fw->ub,
-                    (void*)fw->uw, (void*)fw->umax_part, (void*)fw->mom_part})
+                    (void*)fw->uw, (void*)fw->umax_part, (void*)fw->mom_part, (void*)fw->ph, (void*)fw->pl,
+                    (void*)fw->pa, (void*)fw->prhs, (void*)fw->bvel})
         if (p) release(p, fw->owned);
     fw->part = part, fw->tag = tag, fw->group = group, fw->blobs = blobs, fw->X = X, fw->ub = ub, fw->uw = uw;
-    fw->umax_part = umax_part, fw->mom_part = mom_part;
+    fw->umax_part = umax_part, fw->mom_part = mom_part, fw->ph = ph, fw->pl = pl, fw->pa = pa, fw->prhs = prhs;
+    fw->bvel = bvel;
     fw->cap = cap;
     return VP_OK;
 }
@@ -1180,7 +1423,7 @@ extern "C" int vp_freewake_create(vp_ctx* ctx, const vp_freewake_setup* s, vp_fr
         (r = own_alloc(fw, &fw->mu, size_t(s->nslot))) || (r = own_alloc(fw, &fw->mu_prev, size_t(s->nslot))) ||
         (r = own_alloc(fw, &fw->dmu, size_t(s->nslot))) || (r = own_alloc(fw, &fw->cp, size_t(s->ntri))) ||
         (r = own_alloc(fw, &fw->surf_part, 6 * size_t((s->ntri + 255) / 256 + 1))) ||
-        (r = own_alloc(fw, &fw->rec, 32 + size_t(nte))))
+        (r = own_alloc(fw, &fw->rec, 32 + size_t(nte))) || (r = own_alloc(fw, &fw->src32, size_t(BS32) * s->ntri)))
         return fail(r);
     if ((r = vp_solve_work_alloc(ctx, F, &fw->sw))) return fail(r);
     VP_CUDA(ctx, cudaMemsetAsync(fw->mul, 0, sizeof(double) * nte, ctx->stream));
@@ -1241,16 +1484,31 @@ extern "C" int vp_freewake_step(vp_freewake* fw, vp_freewake_record* rec) {
     {
         RhsArgs ra{};
         ra.na = wake_near_args(fw, o);
-        ra.sheet_G = fw->sheet_G, ra.sheet_ok = fw->sheet_ok, ra.nsh = nsh, ra.nsg = nsg, ra.npart = fw->np;
+        // mixed: the particles go to the FP32 N-body kernel below; FP64: they stay in the warp kernel
+        ra.sheet_G = fw->sheet_G, ra.sheet_ok = fw->sheet_ok, ra.nsh = nsh, ra.nsg = nsg, ra.npart = mixed ? 0 : fw->np;
         ra.seg = fw->seg, ra.part = fw->part, ra.trow = fw->trow;
         ra.pr.rfar = fw->rule[R_FAR], ra.pr.nfar = fw->nrule[R_FAR], ra.pr.rnear = fw->rule[R_NEAR];
         ra.pr.nnear = fw->nrule[R_NEAR], ra.pr.test_mode = o.test, ra.pr.near_depth = o.near_depth;
         ra.pr.far_ratio = o.far_ratio, ra.pr.near_ratio = o.near_ratio;
         const int nb = (ntri + RHS_WARPS - 1) / RHS_WARPS;
+        vp_phase_end(ctx);
+        vp_phase_begin(ctx, PH_WAKE_RHS);
         if (mixed)
             wake_rhs_kernel<float><<<nb, 32 * RHS_WARPS, 0, ctx->stream>>>(ra);
         else
             wake_rhs_kernel<double><<<nb, 32 * RHS_WARPS, 0, ctx->stream>>>(ra);
+        if (mixed && fw->np > 0) {
+            particle_prep_kernel<<<(fw->np + 255) / 256, 256, 0, ctx->stream>>>(fw->np, fw->part, fw->ph, fw->pl, fw->pa);
+            PRhsArgs pa{};
+            pa.ntri = ntri, pa.npart = fw->np, pa.nchunk = (fw->np + NB_CHUNK - 1) / NB_CHUNK;
+            pa.tri = fw->tg, pa.part = fw->part, pa.ph = fw->ph, pa.pl = fw->pl, pa.pa = fw->pa, pa.pr = ra.pr;
+            pa.out = fw->prhs;
+            particle_rhs_kernel<<<dim3((ntri + NB_TPB - 1) / NB_TPB, pa.nchunk), NB_TPB, 0, ctx->stream>>>(pa);
+            add_chunks_kernel<<<(3 * ntri + 255) / 256, 256, 0, ctx->stream>>>(3 * ntri, pa.nchunk, fw->prhs, fw->trow);
+            ctx->launches += 3;
+        }
+        vp_phase_end(ctx);
+        vp_phase_begin(ctx, PH_WAKE);
         slot_gather_kernel<<<(nslot + 255) / 256, 256, 0, ctx->stream>>>(nslot, fw->sg_ptr, fw->sg_ent, fw->trow, fw->b0,
                                                                           fw->rhs);
         ctx->launches += 2;
@@ -1295,10 +1553,18 @@ extern "C" int vp_freewake_step(vp_freewake* fw, vp_freewake_record* rec) {
     gather_points_kernel<<<(npts + 255) / 256, 256, 0, ctx->stream>>>(pa);
     ctx->launches++;
     const bool freestream = s.advection == 1;
+    vp_phase_end(ctx);
+    vp_phase_begin(ctx, PH_WAKE_VEL);
     if (!freestream) {
         if (mixed) {
-            body_kernel<float><<<(npts + NB_THREADS - 1) / NB_THREADS, NB_THREADS, 0, ctx->stream>>>(
-                ntri, fw->bs, o.kernel_far, npts, fw->X, fw->ub);
+            body_src32_kernel<<<(ntri + 255) / 256, 256, 0, ctx->stream>>>(ntri, fw->bs, fw->src32);
+            BVelArgs ba{};
+            ba.ntri = ntri, ba.npts = npts, ba.nchunk = (ntri + NB_CHUNK - 1) / NB_CHUNK, ba.src32 = fw->src32;
+            ba.src64 = fw->bs, ba.X = fw->X, ba.kernel_far = o.kernel_far, ba.out = fw->bvel;
+            body_vel_kernel<<<dim3((npts + NB_TPB - 1) / NB_TPB, ba.nchunk), NB_TPB, 0, ctx->stream>>>(ba);
+            VP_CUDA(ctx, cudaMemsetAsync(fw->ub, 0, sizeof(double) * 3 * npts, ctx->stream));
+            add_chunks_kernel<<<(3 * npts + 255) / 256, 256, 0, ctx->stream>>>(3 * npts, ba.nchunk, fw->bvel, fw->ub);
+            ctx->launches += 3;
             if (nblob > 0)
                 blob_kernel<float><<<(npts + NB_THREADS * NB_PTS - 1) / (NB_THREADS * NB_PTS), NB_THREADS, 0,
                                      ctx->stream>>>(nblob, fw->blobs, npts, fw->X, fw->uw);
@@ -1312,6 +1578,8 @@ extern "C" int vp_freewake_step(vp_freewake* fw, vp_freewake_record* rec) {
         if (nblob == 0) VP_CUDA(ctx, cudaMemsetAsync(fw->uw, 0, sizeof(double) * 3 * npts, ctx->stream));
         ctx->launches += 2;
     }
+    vp_phase_end(ctx);
+    vp_phase_begin(ctx, PH_WAKE);
     const int nub = (npts + 255) / 256;
     advect_kernel<<<nub, 256, 0, ctx->stream>>>(pa, fw->V[0], fw->V[1], fw->V[2], freestream ? 1 : 0, s.dt, fw->ub,
                                                  fw->uw, fw->umax_part);

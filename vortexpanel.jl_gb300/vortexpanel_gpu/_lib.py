@@ -170,7 +170,7 @@ class Context:
         self.device = device
 
     PHASES = ("setup", "classify", "far", "near", "reduce", "lu", "cond", "solve", "adj_setup", "adj_far", "adj_near",
-              "adj_solve", "wake", "near_pairs", "adj_pairs")
+              "adj_solve", "wake", "near_pairs", "adj_pairs", "wake_rhs", "wake_vel")
 
     def phase_times(self, reset=False):
         """Device milliseconds per phase since the last reset, and the number of the library's kernel launches"""
