@@ -75,6 +75,46 @@ __device__ __forceinline__ T adj_point_far(AdjSums<T>& acc, const SrcKern<T>& S,
     return sv;
 }
 
+// the sums of one exact-kernel point for nk adjoint vectors (weights Wn[k]): velocity w, ds/dx gx, ds/dr_a g_a, the
+// edge logs L, their length derivatives dL and the solid angle Om. The sums may be of a narrower type than the point.
+template <class T>
+__device__ __forceinline__ void adj_acc_exact(AdjSums<T>* acc, int nk, const T* Wn, T l0, T l1, T l2, v3<T> w,
+                                              v3<T> gx, v3<T> g0, v3<T> g1, v3<T> g2, const T* L, const T* dL, T Om) {
+    for (int k = 0; k < nk; ++k) {
+        AdjSums<T>& a = acc[k];
+        const T wn = Wn[k];
+        a.Q += wn * w;
+        a.Xg[0] += (wn * l0) * gx;
+        a.Xg[1] += (wn * l1) * gx;
+        a.Xg[2] += (wn * l2) * gx;
+        a.Gr[0] += wn * g0;
+        a.Gr[1] += wn * g1;
+        a.Gr[2] += wn * g2;
+        for (int e = 0; e < 3; ++e) {
+            a.L[e] += wn * L[e];
+            a.N[e] += wn * dL[e];
+        }
+        a.O += wn * Om;
+    }
+}
+
+// the sums of one multipole point: velocity w, ds/dr gx, ds/d(second moments) gd, ds/d(area) ga
+template <class T>
+__device__ __forceinline__ void adj_acc_far(AdjSums<T>* acc, int nk, const T* Wn, T l0, T l1, T l2, v3<T> w, v3<T> gx,
+                                            const v3<T>* gd, T ga) {
+    for (int k = 0; k < nk; ++k) {
+        AdjSums<T>& a = acc[k];
+        const T wn = Wn[k];
+        a.Q += wn * w;
+        a.Xg[0] += (wn * l0) * gx;
+        a.Xg[1] += (wn * l1) * gx;
+        a.Xg[2] += (wn * l2) * gx;
+        a.Grf += wn * gx;
+        for (int b = 0; b < 3; ++b) a.Gd[b] += wn * gd[b];
+        a.A += wn * ga;
+    }
+}
+
 // several adjoint vectors at once (their point weights Wn[k], k < nk): the kernel and its derivatives are evaluated
 // once, and each set of sums takes its own weight
 template <class T, class M = KMath<T>>
@@ -87,22 +127,7 @@ __device__ __forceinline__ T adj_point_exact_multi(AdjSums<T>* acc, int nk, cons
     const T i4pi = T(1) / (T(4) * vp_pi<T>());
     const v3<T> w = (sh.L[0] * S.nu[0] + sh.L[1] * S.nu[1] + sh.L[2] * S.nu[2] + sh.Om * S.n) * i4pi;
     gx = g0 + g1 + g2;
-    for (int k = 0; k < nk; ++k) {
-        AdjSums<T>& a = acc[k];
-        const T wn = Wn[k];
-        a.Q += wn * w;
-        a.Xg[0] += (wn * l0) * gx;
-        a.Xg[1] += (wn * l1) * gx;
-        a.Xg[2] += (wn * l2) * gx;
-        a.Gr[0] += wn * g0;
-        a.Gr[1] += wn * g1;
-        a.Gr[2] += wn * g2;
-        for (int e = 0; e < 3; ++e) {
-            a.L[e] += wn * sh.L[e];
-            a.N[e] += wn * sh.dLdlen[e];
-        }
-        a.O += wn * sh.Om;
-    }
+    adj_acc_exact(acc, nk, Wn, l0, l1, l2, w, gx, g0, g1, g2, sh.L, sh.dLdlen, sh.Om);
     return sv;
 }
 
@@ -113,17 +138,7 @@ __device__ __forceinline__ T adj_point_far_multi(AdjSums<T>* acc, int nk, const 
     T ga;
     T sv = sv_far_vjp(S, r, m, gx, gd, ga);
     const v3<T> w = sv_far(S, r);
-    for (int k = 0; k < nk; ++k) {
-        AdjSums<T>& a = acc[k];
-        const T wn = Wn[k];
-        a.Q += wn * w;
-        a.Xg[0] += (wn * l0) * gx;
-        a.Xg[1] += (wn * l1) * gx;
-        a.Xg[2] += (wn * l2) * gx;
-        a.Grf += wn * gx;
-        for (int b = 0; b < 3; ++b) a.Gd[b] += wn * gd[b];
-        a.A += wn * ga;
-    }
+    adj_acc_far(acc, nk, Wn, l0, l1, l2, w, gx, gd, ga);
     return sv;
 }
 

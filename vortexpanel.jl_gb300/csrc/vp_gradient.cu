@@ -633,13 +633,44 @@ __device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjMulti& mx, cons
     }
 }
 
+// the pair's FP64 sums per adjoint vector, in every lane: FP64 lane sums added over the warp (FP64 path), or the
+// warp's totals (mixed path)
+__device__ __forceinline__ void pair_sums(PairCtx& pc, AdjAcc& acc, AdjSums<double>* d, int K) {
+    fold32(acc);
+    for (int j = 0; j < K; ++j) {
+        adj_warp_sum(acc.d[j]);
+        d[j] = acc.d[j];
+    }
+}
+__device__ __forceinline__ void pair_sums(PairCtx& pc, AdjAccW& acc, AdjSums<double>* d, int K) {
+    fold_w(acc, pc.lane);
+    pair_totals(acc, d, K);
+#pragma unroll
+    for (int j = 0; j < ADJ_TSLOT; ++j) acc.tot[j] = 0;
+}
+
+__device__ __forceinline__ void acc_init(AdjAcc&, unsigned char*, int, int) {}
+__device__ __forceinline__ void acc_init(AdjAccW& acc, unsigned char* smem, int w, int lane) {
+    acc.lanes = reinterpret_cast<AdjLane*>(smem) + 32 * w;
+    acc.me = acc.lanes + lane;
+}
+
 // the pairs the lanes kernel left (self, touching, contact), one warp per pair, for up to ADJ_MAX adjoint vectors at
 // once: every point's kernel and derivatives are evaluated once, and each vector keeps its sums. A persistent grid
 // whose warps take the next pair of the list from a counter, so that test triangles with many contact pairs do not
 // leave the end of the launch to a few warps. The test side of a pair goes to TA, the source side to SA (atomics).
+// Acc: AdjAcc (FP64 path: FP64 sums per lane) or AdjAccW (mixed path: FP32 lane partials in dynamic shared memory,
+// NEAR_WARPS x 32 AdjLane, folded into the warp's FP64 totals).
+template <class Acc>
 __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, AdjMulti mx) {
     __shared__ WarpSh shm[NEAR_WARPS];
+    extern __shared__ __align__(16) unsigned char adjw_smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if constexpr (std::is_same<Acc, AdjAccW>::value) {
+        float* mine = reinterpret_cast<float*>(reinterpret_cast<AdjLane*>(adjw_smem) + threadIdx.x);
+        for (int z = 0; z < ADJ_LSTRIDE; ++z) mine[z] = 0.f;
+        __syncwarp();
+    }
     const int n = 2 * a.ntri;
     const long long total = a.rest_off[n];
     const int K = mx.nadj;
@@ -682,7 +713,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, 
         const double sig = wake ? 0.0 : S.sigma;
         pc.m = cross(nT, G) + sig * nT;
         pc.mf = mk3(float(pc.m.x), float(pc.m.y), float(pc.m.z));
-        AdjAcc acc = {};
+        Acc acc = {};
+        acc_init(acc, adjw_smem, w, lane);
         pc.kind = 0;
         pc.npts = 0;
         pc.n64 = 0;
@@ -690,12 +722,12 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, 
         pc.nq64 = 0;
         const int tier = tri_pair(pc, acc, t, s, wake);
         flush_gdir(pc, mx, T, &S, wake);
-        fold32(acc);
+        AdjSums<double> dsum[ADJ_MAX];
+        pair_sums(pc, acc, dsum, K);
         v3<double> xS[3];
         tri_corners(S, xS);
         for (int j = 0; j < K; ++j) {
-            adj_warp_sum(acc.d[j]);
-            const AdjSums<double>& d = acc.d[j];
+            const AdjSums<double>& d = dsum[j];
             // the test side: lane k adds field k of the pair's (Xg, U, fs)
             const v3<double> U = cross(G, d.Q) + sig * d.Q;
             const double v[NTA] = {d.Xg[0].x, d.Xg[0].y, d.Xg[0].z, d.Xg[1].x, d.Xg[1].y, d.Xg[1].z,
@@ -1169,10 +1201,18 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         }
         na.stats = d_stats;
         if ((r = rest_list(ctx, dl, na, nullptr))) return r;
-        const int npb = persistent_blocks(ctx, adj_pairs_kernel, 32 * NEAR_WARPS, 0);
         vp_phase_end(ctx);
         vp_phase_begin(ctx, PH_ADJ_PAIRS);
-        adj_pairs_kernel<<<npb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
+        if (na.mixed) {  // FP32 lane partials in shared memory, FP64 totals per warp
+            const size_t wsm = sizeof(AdjLane) * 32 * NEAR_WARPS;
+            VP_CUDA(ctx, cudaFuncSetAttribute(adj_pairs_kernel<AdjAccW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              int(wsm)));
+            const int npb = persistent_blocks(ctx, adj_pairs_kernel<AdjAccW>, 32 * NEAR_WARPS, wsm);
+            adj_pairs_kernel<AdjAccW><<<npb, 32 * NEAR_WARPS, wsm, ctx->stream>>>(na, mx);
+        } else {
+            const int npb = persistent_blocks(ctx, adj_pairs_kernel<AdjAcc>, 32 * NEAR_WARPS, 0);
+            adj_pairs_kernel<AdjAcc><<<npb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
+        }
         vp_phase_end(ctx);
         vp_phase_begin(ctx, PH_ADJ_NEAR);
         adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);

@@ -618,6 +618,65 @@ __device__ __forceinline__ void fold32(AdjAcc& acc) {
     acc.nf = 0;
 }
 
+// Mixed-precision adjoint sums of a pair, held by the warp. Each lane adds its points into FP32 partial sums in shared
+// memory (AdjLane: both vectors' AdjSums, then the dependent piece's Bb and Fb); every ADJ_FOLD point batches the warp
+// adds the 32 lanes' partials field by field, in lane order, into FP64 totals spread over the lanes (field z in lane
+// z % 32, slot z / 32). The lanes keep no FP64 sums of their own, and the FP64 work per point is a few additions per
+// fold instead of two per field and point.
+constexpr int ADJ_NSUM = 41;                                      // fields of AdjSums
+constexpr int ADJ_NFIELD = ADJ_MAX * ADJ_NSUM + ADJ_MAX * 10;     // sums, then Bb (9) per vector, then Fb per vector
+constexpr int ADJ_BB0 = ADJ_MAX * ADJ_NSUM;                       // field of Bb[0][0]
+constexpr int ADJ_FB0 = ADJ_BB0 + ADJ_MAX * 9;                    // field of Fb[0]
+constexpr int ADJ_TSLOT = (ADJ_NFIELD + 31) / 32;
+constexpr int ADJ_FOLD = 8;
+
+struct AdjLane {
+    AdjSums<float> f[ADJ_MAX];
+    float Bbf[ADJ_MAX][9], Fbf[ADJ_MAX];
+    float pad;  // an odd stride in words: the 32 lanes' copies of a field fall in 32 banks
+};
+static_assert(sizeof(AdjSums<float>) == ADJ_NSUM * sizeof(float), "AdjSums is a plain array of fields");
+static_assert(sizeof(AdjLane) == (ADJ_NFIELD + 1) * sizeof(float), "AdjLane is a plain array of fields");
+static_assert(sizeof(AdjSums<double>) == ADJ_NSUM * sizeof(double), "AdjSums is a plain array of fields");
+constexpr int ADJ_LSTRIDE = ADJ_NFIELD + 1;
+
+struct AdjAccW {
+    AdjLane* lanes;            // the warp's 32 partials (shared memory)
+    AdjLane* me;               // this lane's
+    double tot[ADJ_TSLOT];     // the warp's FP64 totals of fields lane + 32 j
+    int nb;                    // point batches since the last fold (warp-uniform)
+};
+
+// the warp's fold: lane z sums field z over the 32 lanes (two halves of 16, in lane order), adds it to its total and
+// clears the partials it read. Called by the whole warp.
+__device__ __noinline__ void fold_w(AdjAccW& acc, int lane) {
+    __syncwarp();
+    float* base = reinterpret_cast<float*>(acc.lanes);
+#pragma unroll
+    for (int j = 0; j < ADJ_TSLOT; ++j) {
+        const int z = lane + 32 * j;
+        if (z < ADJ_NFIELD) {
+            float s0 = 0.f, s1 = 0.f;
+            for (int l = 0; l < 16; ++l) {
+                float* p0 = base + l * ADJ_LSTRIDE + z;
+                float* p1 = base + (l + 16) * ADJ_LSTRIDE + z;
+                s0 += *p0;
+                s1 += *p1;
+                *p0 = 0.f;
+                *p1 = 0.f;
+            }
+            acc.tot[j] += double(s0) + double(s1);
+        }
+    }
+    __syncwarp();
+    acc.nb = 0;
+}
+
+// the FP64 total of field z (a compile-time index after unrolling), in every lane
+__device__ __forceinline__ double tot_field(const AdjAccW& acc, int z) {
+    return __shfl_sync(0xffffffffu, acc.tot[z >> 5], z & 31);
+}
+
 // the rule-geometry sums of one point of a dependent piece: weight W, barycentrics l, value s = w·m, ds/dx
 template <class T>
 __device__ __forceinline__ void rule_point(const PairCtx& pc, const T* nu, const T* binv, T* Bb, T& Fb, T W, T l0, T l1,
@@ -742,6 +801,88 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
     return true;
 }
 
+__device__ __forceinline__ v3<float> f3(v3<double> v) { return mk3(float(v.x), float(v.y), float(v.z)); }
+
+// the mixed path's FP64 point (a triangle source's point the FP32 guard refused), warp sums: the kernel and its
+// derivatives in FP64 geometry with the FP32-based functions, added to this lane's FP32 partials
+__device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAccW& acc, double l0, double l1, double l2, double W) {
+    const WarpSh& sh = *pc.sh;
+    const v3<double> psi = test_weights(pc.a->test_mode, l0, l1, l2);
+    float Wn[ADJ_MAX];
+    for (int k = 0; k < ADJ_MAX; ++k)
+        Wn[k] = float(W * (pc.nuk[k][0] * psi.x + pc.nuk[k][1] * psi.y + pc.nuk[k][2] * psi.z));
+    const v3<double> ra = l0 * ld3(sh.E + 0) + l1 * ld3(sh.E + 9) + l2 * ld3(sh.E + 18);
+    const v3<double> rb = l0 * ld3(sh.E + 3) + l1 * ld3(sh.E + 12) + l2 * ld3(sh.E + 21);
+    const v3<double> rc = l0 * ld3(sh.E + 6) + l1 * ld3(sh.E + 15) + l2 * ld3(sh.E + 24);
+    const v3<double> r = l0 * ld3(sh.D) + l1 * ld3(sh.D + 3) + l2 * ld3(sh.D + 6);
+    const SrcKern<double> S = src64(sh);
+    const float fl0 = float(l0), fl1 = float(l1), fl2 = float(l2);
+    const double fd = pc.a->kernel_far * S.diam;
+    v3<double> gx;
+    double sv;
+    if (dot(r, r) > fd * fd) {
+        v3<double> gd[3];
+        double ga;
+        sv = sv_far_vjp(S, r, pc.m, gx, gd, ga);
+        const v3<float> gdf[3] = {f3(gd[0]), f3(gd[1]), f3(gd[2])};
+        adj_acc_far(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(sv_far(S, r)), f3(gx), gdf, float(ga));
+    } else {
+        v3<double> g0, g1, g2;
+        ExactShape<double> shp;
+        sv = sv_exact_vjp<double, KMathHyb>(S, ra, rb, rc, r, pc.m, pc.side, 1e-12, g0, g1, g2, shp);
+        const double i4pi = 1.0 / (4.0 * vp_pi<double>());
+        const v3<double> w = (shp.L[0] * S.nu[0] + shp.L[1] * S.nu[1] + shp.L[2] * S.nu[2] + shp.Om * S.n) * i4pi;
+        gx = g0 + g1 + g2;
+        const float Lf[3] = {float(shp.L[0]), float(shp.L[1]), float(shp.L[2])};
+        const float dLf[3] = {float(shp.dLdlen[0]), float(shp.dLdlen[1]), float(shp.dLdlen[2])};
+        adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(w), f3(gx), f3(g0), f3(g1), f3(g2), Lf, dLf,
+                      float(shp.Om));
+    }
+    if (pc.dep)
+        for (int k = 0; k < pc.nadj; ++k)
+            rule_point(pc, pc.nukf[k], pc.binvf, acc.me->Bbf[k], acc.me->Fbf[k], float(W), fl0, fl1, fl2, float(sv),
+                       f3(gx), pc.Xcf);
+}
+
+// one point in FP32 under the guard, warp sums; false when it must be evaluated in FP64
+__device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAccW& acc, float l0, float l1, float l2, float W) {
+    if (pc.a->test_mode == 2) return false;
+    const WarpSh& sh = *pc.sh;
+    SrcKern<float> S = src32(sh);
+    v3<float> r = l0 * mk3(sh.D32[0], sh.D32[1], sh.D32[2]) + l1 * mk3(sh.D32[3], sh.D32[4], sh.D32[5]) +
+                  l2 * mk3(sh.D32[6], sh.D32[7], sh.D32[8]);
+    v3<float> psi = pc.a->test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);
+    float Wn[ADJ_MAX];
+    for (int k = 0; k < ADJ_MAX; ++k)
+        Wn[k] = W * (pc.nukf[k][0] * psi.x + pc.nukf[k][1] * psi.y + pc.nukf[k][2] * psi.z);
+    float fd = pc.a->kernel_far32 * S.diam;
+    v3<float> gx;
+    float sv;
+    if (dot(r, r) > fd * fd) {
+        sv = adj_point_far_multi(acc.me->f, pc.nadj, Wn, S, l0, l1, l2, r, pc.mf, gx);
+    } else {
+        const float* E = sh.E32;
+        v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
+        v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
+        v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
+        if (!fp32_guard_ok(S, ra, rb, rc, pc.side, Fp32Guard{ADJ_GUARD})) return false;
+        sv = adj_point_exact_multi(acc.me->f, pc.nadj, Wn, S, l0, l1, l2, ra, rb, rc, r, pc.mf, pc.side,
+                                   pc.side ? 1e-4f : 1e-12f, gx);
+    }
+    if (pc.dep)
+        for (int k = 0; k < pc.nadj; ++k)
+            rule_point(pc, pc.nukf[k], pc.binvf, acc.me->Bbf[k], acc.me->Fbf[k], W, l0, l1, l2, sv, gx, pc.Xcf);
+    return true;
+}
+
+// the warp's fold after a batch of points (one per lane), every ADJ_FOLD batches; nothing for the other accumulators
+template <class Acc>
+__device__ __forceinline__ void batch_done(PairCtx& pc, Acc& acc) {
+    if constexpr (std::is_same<Acc, AdjAccW>::value) {
+        if (++acc.nb == ADJ_FOLD) fold_w(acc, pc.lane);
+    }
+}
+
 __device__ __forceinline__ double wsum_d(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -787,6 +928,7 @@ __device__ __noinline__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, c
             double l2 = m.l0 * c[2] + m.l1 * c[5] + m.l2 * c[8];
             eval_point64(pc, acc, l0, l1, l2, (m.w * fr) * areaT);
         }
+        batch_done(pc, acc);
         __syncwarp();
         int rest = pc.nq64 - take;
         int mi = 0, ml = 0;
@@ -810,7 +952,7 @@ __device__ __noinline__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, c
 template <class Acc>
 __device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, int rid, int i, int lf, const double* b,
                                            const float* bf, double frac) {
-    if (!pc.fp32) {
+    if (!std::is_same<Acc, AdjAccW>::value && !pc.fp32) {
         if (valid) {
             RulePt m = pc.a->rule[rid][i];
             double l0 = m.l0 * b[0] + m.l1 * b[3] + m.l2 * b[6];
@@ -837,6 +979,7 @@ __device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, in
         }
         pc.nq64 += __popc(msk);
     }
+    batch_done(pc, acc);
 }
 
 // a piece carrying a whole tabulated rule: lanes stride over its points
@@ -897,7 +1040,7 @@ __device__ void emit_leaf(PairCtx& pc, Acc& acc, const double* b, double frac) {
 // one geometry coordinate (lane < 18); the points of a dependent piece sum sum W beta_j dphi/dl and sum W phi
 // (rule_point), and piece_end contracts those with the lanes' tangents.
 template <class Acc>
-constexpr bool kAdj = std::is_same<Acc, AdjAcc>::value;
+constexpr bool kAdj = std::is_same<Acc, AdjAcc>::value || std::is_same<Acc, AdjAccW>::value;
 
 __device__ __forceinline__ void piece_begin(PairCtx&, FwdAcc&, const double*, double, const double*) {}
 __device__ __forceinline__ void piece_end(PairCtx&, FwdAcc&) {}
@@ -943,6 +1086,55 @@ __device__ void piece_end(PairCtx& pc, AdjAcc& acc) {
         if (pc.lane < 18) pc.gdir[j] += v;
     }
     pc.dep = 0;
+}
+
+__device__ void piece_begin(PairCtx& pc, AdjAccW& acc, const double* c, double frac, const double* tan) {
+    if (pc.nleaf) flush_leaves(pc, acc);
+    if (!tan) {
+        pc.dep = 0;
+        return;
+    }
+    pc.dep = 1;
+    pc.pfrac = frac;
+    for (int k = 0; k < 10; ++k) pc.tb[k] = tan[k];
+    const double a = c[0], b = c[3], cc = c[6], d = c[1], e = c[4], f = c[7], g = c[2], h = c[5], i = c[8];
+    const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+    const double id = 1.0 / (a * A + b * B + cc * C);
+    const double bi[9] = {A * id, -(b * i - cc * h) * id, (b * f - cc * e) * id, B * id, (a * i - cc * g) * id,
+                          -(a * f - cc * d) * id, C * id, -(a * h - b * g) * id, (a * e - b * d) * id};
+    for (int k = 0; k < 9; ++k) {
+        pc.binv[k] = bi[k];
+        pc.binvf[k] = float(bi[k]);
+    }
+}
+
+// the piece's rule-geometry totals (folded first) contracted with this lane's tangent; the totals are then cleared
+__device__ void piece_end(PairCtx& pc, AdjAccW& acc) {
+    if (!pc.dep) return;
+    if (pc.nleaf) flush_leaves(pc, acc);
+    fold_w(acc, pc.lane);
+#pragma unroll
+    for (int j = 0; j < ADJ_MAX; ++j) {
+        if (j >= pc.nadj) break;
+        double v = 0;
+#pragma unroll
+        for (int k = 0; k < 9; ++k) v += tot_field(acc, ADJ_BB0 + 9 * j + k) * pc.tb[k];
+        v += tot_field(acc, ADJ_FB0 + j) * pc.tb[9] / pc.pfrac;
+        if (pc.lane < 18) pc.gdir[j] += v;
+    }
+#pragma unroll
+    for (int j = 0; j < ADJ_TSLOT; ++j) {
+        const int z = pc.lane + 32 * j;
+        if (z >= ADJ_BB0 && z < ADJ_NFIELD) acc.tot[j] = 0;
+    }
+    pc.dep = 0;
+}
+
+// the warp's FP64 sums of the pair's d[j], j < nadj, in every lane (after the last fold)
+__device__ void pair_totals(const AdjAccW& acc, AdjSums<double>* d, int nadj) {
+    double* o = reinterpret_cast<double*>(d);
+#pragma unroll
+    for (int z = 0; z < ADJ_BB0; ++z) o[z] = z < nadj * ADJ_NSUM ? tot_field(acc, z) : 0.0;
 }
 
 // this lane's tangent of the point with test barycentrics b (3) whose tangent is bt (3)
