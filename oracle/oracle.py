@@ -31,9 +31,9 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile the C++ restatement (g++, OpenMP) into oracle/_build/libvp_oracle.so"""
     src = os.path.join(HERE, "vp_oracle.cpp")
-    hdr = os.path.join(HERE, "vp_oracle.hpp")
+    hdrs = [os.path.join(HERE, h) for h in ("vp_oracle.hpp", "vp_dual.hpp")]
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(src), os.path.getmtime(hdr)):
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(map(os.path.getmtime, [src] + hdrs)):
         return LIB
     tmp = LIB + f".tmp{os.getpid()}"
     subprocess.check_call(["g++", "-O2", "-std=c++17", "-fopenmp", "-fPIC", "-shared", src, "-o", tmp])

@@ -9,6 +9,7 @@
 //   src/post/Post.jl                  body_velocity
 //   src/freewake/step.jl              blob_velocities
 #include "vp_oracle.hpp"
+#include "vp_dual.hpp"
 
 #include <algorithm>
 #include <cstdint>
@@ -22,60 +23,66 @@
 namespace vpo {
 
 // FlatTriangle (flat_triangle.jl:12-31)
-bool make_flat_tri(const Vec& a, const Vec& b, const Vec& c, FlatTri& t) {
+template <class T>
+bool make_flat_tri(const V3<T>& a, const V3<T>& b, const V3<T>& c, FlatTriT<T>& t) {
     if (!make_source_tri(a, b, c, t.src)) return false;
     t.x[0] = a; t.x[1] = b; t.x[2] = c;
     t.n = t.src.n;
     t.area = t.src.area;
     t.c = t.src.c;
     t.diam = t.src.diam;
-    double A2 = 2 * t.area;
-    Vec e[3] = {c - b, a - c, b - a};
+    T A2 = T(2) * t.area;
+    V3<T> e[3] = {c - b, a - c, b - a};
     for (int k = 0; k < 3; ++k) {
         t.gradl[k] = cross(t.n, e[k]) / A2;
         t.gam[k] = -e[k] / A2;
     }
     return true;
 }
+template bool make_flat_tri<double>(const Vec&, const Vec&, const Vec&, FlatTri&);
 
 // reach (flat_triangle.jl:56)
-double reach(const FlatTri& el) {
+template <class T>
+T reach(const FlatTriT<T>& el) {
     return std::max({norm(el.x[0] - el.c), norm(el.x[1] - el.c), norm(el.x[2] - el.c)});
 }
 
 // distance_to (flat_triangle.jl:59-78), closest point after Ericson 5.1.5
-double distance_to(const FlatTri& el, const Vec& p) {
-    const Vec &a = el.x[0], &b = el.x[1], &c = el.x[2];
-    Vec ab = b - a, ac = c - a, ap = p - a;
-    double d1 = dot(ab, ap), d2 = dot(ac, ap);
+template <class T>
+T distance_to(const FlatTriT<T>& el, const V3<T>& p) {
+    const V3<T> &a = el.x[0], &b = el.x[1], &c = el.x[2];
+    V3<T> ab = b - a, ac = c - a, ap = p - a;
+    T d1 = dot(ab, ap), d2 = dot(ac, ap);
     if (d1 <= 0 && d2 <= 0) return norm(ap);
-    Vec bp = p - b;
-    double d3 = dot(ab, bp), d4 = dot(ac, bp);
+    V3<T> bp = p - b;
+    T d3 = dot(ab, bp), d4 = dot(ac, bp);
     if (d3 >= 0 && d4 <= d3) return norm(bp);
-    double vc = d1 * d4 - d3 * d2;
+    T vc = d1 * d4 - d3 * d2;
     if (vc <= 0 && d1 >= 0 && d3 <= 0) return norm(p - (a + (d1 / (d1 - d3)) * ab));
-    Vec cp = p - c;
-    double d5 = dot(ab, cp), d6 = dot(ac, cp);
+    V3<T> cp = p - c;
+    T d5 = dot(ab, cp), d6 = dot(ac, cp);
     if (d6 >= 0 && d5 <= d6) return norm(cp);
-    double vb = d5 * d2 - d1 * d6;
+    T vb = d5 * d2 - d1 * d6;
     if (vb <= 0 && d2 >= 0 && d6 <= 0) return norm(p - (a + (d2 / (d2 - d6)) * ac));
-    double va = d3 * d6 - d5 * d4;
+    T va = d3 * d6 - d5 * d4;
     if (va <= 0 && d4 - d3 >= 0 && d5 - d6 >= 0) return norm(p - (b + ((d4 - d3) / ((d4 - d3) + (d5 - d6))) * (c - b)));
-    double denom = 1 / (va + vb + vc);
+    T denom = T(1) / (va + vb + vc);
     return norm(p - (a + (vb * denom) * ab + (vc * denom) * ac));
 }
 
 // segment_projection (assemble.jl:145-149)
-static void segment_projection(const Vec& p, const Vec& a, const Vec& c, double& d, double& t) {
-    Vec e = c - a;
+template <class T>
+static void segment_projection(const V3<T>& p, const V3<T>& a, const V3<T>& c, T& d, T& t) {
+    V3<T> e = c - a;
     t = dot(p - a, e) / dot(e, e);
-    t = std::min(std::max(t, 0.0), 1.0);
+    t = std::min(std::max(t, T(0)), T(1));
     d = norm(p - (a + t * e));
 }
 
 // distance_to(::Segment) (assemble.jl:157), distance_to(::Blob) (explicit.jl:20)
-double distance_to(const Segment& s, const Vec& p) {
-    double d, t;
+template <class T>
+T distance_to(const SegmentT<T>& s, const V3<T>& p) {
+    T d, t;
     segment_projection(p, s.a, s.b, d, t);
     return d;
 }
@@ -258,142 +265,177 @@ TierRules tier_rules(const Options& o) {
 }
 
 // ---- tiers (assemble.jl:52-321) ----
+// The pieces, rules and blocks are templates on the scalar type: double for the oracle, a forward-mode dual number
+// for the derivative oracle. Decisions (tiers, splits, wedge counts) compare values; the base rules stay double.
+
+template <class T>
+inline double val(const T& x) { return double(x); }
 
 // test_weights (assemble.jl:52-58)
-static inline Vec test_weights(int test, const Bary& l) {
-    if (test == 0) return Vec(l[0], l[1], l[2]);
-    if (test == 1) return Vec(1, 1, 1);
-    double m = std::max({l[0], l[1], l[2]});
+template <class T>
+static inline V3<T> test_weights(int test, const BaryT<T>& l) {
+    if (test == 0) return V3<T>(l[0], l[1], l[2]);
+    if (test == 1) return V3<T>(T(1), T(1), T(1));
+    double m = std::max({val(l[0]), val(l[1]), val(l[2])});
     double is[3];
     int cnt = 0;
     for (int k = 0; k < 3; ++k) {
-        is[k] = std::fabs(l[k] - m) < 1e-12 ? 1.0 : 0.0;
+        is[k] = std::fabs(val(l[k]) - m) < 1e-12 ? 1.0 : 0.0;
         cnt += int(is[k]);
     }
-    return Vec(is[0] / cnt, is[1] / cnt, is[2] / cnt);
+    return V3<T>(T(is[0] / cnt), T(is[1] / cnt), T(is[2] / cnt));
 }
 
 // test_integrals (assemble.jl:61)
 static inline Vec test_integrals(int test) { return test == 1 ? Vec(1, 1, 1) : Vec(1.0 / 3, 1.0 / 3, 1.0 / 3); }
 
-typedef std::array<Bary, 3> Corners;
-static const Corners CORNERS = {Bary{1, 0, 0}, Bary{0, 1, 0}, Bary{0, 0, 1}};
+template <class T>
+using CornersT = std::array<BaryT<T>, 3>;
+typedef CornersT<double> Corners;
+template <class T>
+static CornersT<T> unit_corners() {
+    return {BaryT<T>{T(1), T(0), T(0)}, BaryT<T>{T(0), T(1), T(0)}, BaryT<T>{T(0), T(0), T(1)}};
+}
 
-static inline Bary bmix(const Bary& a, double sa, const Bary& b, double sb) {
+template <class T>
+static inline BaryT<T> bmix(const BaryT<T>& a, const T& sa, const BaryT<T>& b, const T& sb) {
     return {sa * a[0] + sb * b[0], sa * a[1] + sb * b[1], sa * a[2] + sb * b[2]};
 }
 
 // append_piece! (assemble.jl:85-91)
-static void append_piece(Rule& out, const Rule& r, const Corners& b, double frac) {
+template <class T>
+static void append_piece(RuleT<T>& out, const Rule& r, const CornersT<T>& b, const T& frac) {
     for (size_t i = 0; i < r.size(); ++i) {
         const Bary& m = r.lam[i];
-        Bary l;
-        for (int j = 0; j < 3; ++j) l[j] = m[0] * b[0][j] + m[1] * b[1][j] + m[2] * b[2][j];
+        BaryT<T> l;
+        for (int j = 0; j < 3; ++j) l[j] = T(m[0]) * b[0][j] + T(m[1]) * b[1][j] + T(m[2]) * b[2][j];
         out.lam.push_back(l);
-        out.w.push_back(r.w[i] * frac);
+        out.w.push_back(T(r.w[i]) * frac);
     }
 }
 
+// a stored rule as the pair's rule: itself in double, a constant copy in another scalar type
+static const Rule* as_rule(const Rule& r, Rule&) { return &r; }
+template <class T>
+static const RuleT<T>* as_rule(const Rule& r, RuleT<T>& buf) {
+    buf.clear();
+    append_piece(buf, r, unit_corners<T>(), T(1));
+    return &buf;
+}
+
 // quarters (assemble.jl:79-82)
-static std::array<Corners, 4> quarters(const Corners& b) {
-    Bary m12 = bmix(b[0], 0.5, b[1], 0.5), m23 = bmix(b[1], 0.5, b[2], 0.5), m31 = bmix(b[2], 0.5, b[0], 0.5);
-    return {Corners{b[0], m12, m31}, Corners{m12, b[1], m23}, Corners{m31, m23, b[2]}, Corners{m12, m23, m31}};
+template <class T>
+static std::array<CornersT<T>, 4> quarters(const CornersT<T>& b) {
+    const T h(0.5);
+    BaryT<T> m12 = bmix(b[0], h, b[1], h), m23 = bmix(b[1], h, b[2], h), m31 = bmix(b[2], h, b[0], h);
+    return {CornersT<T>{b[0], m12, m31}, CornersT<T>{m12, b[1], m23}, CornersT<T>{m31, m23, b[2]},
+            CornersT<T>{m12, m23, m31}};
 }
 
 // near_pieces! (assemble.jl:131-142)
-template <class S>
-static void near_pieces(Rule& out, const FlatTri& T, const S& src, const Rule& base, double ratio, int depth,
-                        const Corners& b, double frac, int level) {
-    Vec p1 = point(T, b[0]), p2 = point(T, b[1]), p3 = point(T, b[2]);
-    double size = std::max({norm(p2 - p1), norm(p3 - p2), norm(p1 - p3)});
-    if (level < depth && distance_to(src, (p1 + p2 + p3) / 3.0) < ratio * size) {
-        for (const Corners& sub : quarters(b)) near_pieces(out, T, src, base, ratio, depth, sub, frac / 4, level + 1);
+template <class T, class S>
+static void near_pieces(RuleT<T>& out, const FlatTriT<T>& Tr, const S& src, const Rule& base, double ratio, int depth,
+                        const CornersT<T>& b, const T& frac, int level) {
+    V3<T> p1 = point(Tr, b[0]), p2 = point(Tr, b[1]), p3 = point(Tr, b[2]);
+    T size = std::max({norm(p2 - p1), norm(p3 - p2), norm(p1 - p3)});
+    if (level < depth && distance_to(src, (p1 + p2 + p3) / T(3)) < T(ratio) * size) {
+        for (const CornersT<T>& sub : quarters(b))
+            near_pieces(out, Tr, src, base, ratio, depth, sub, frac / T(4), level + 1);
     } else {
         append_piece(out, base, b, frac);
     }
 }
 
 // vertex_pieces! (assemble.jl:102-116); k 0-based
-static void vertex_pieces(Rule& out, const Vec p[3], int k, const Rule& base, const Corners& b, double frac,
-                          double corner_angle) {
+template <class T>
+static void vertex_pieces(RuleT<T>& out, const V3<T> p[3], int k, const Rule& base, const CornersT<T>& b,
+                          const T& frac, double corner_angle) {
+    using std::acos;
+    using std::sin;
     int i = (k + 1) % 3, j = (k + 2) % 3;
-    Vec u = p[i] - p[k], v = p[j] - p[k];
-    double cs = dot(u, v) / (norm(u) * norm(v));
-    double th = std::acos(std::min(std::max(cs, -1.0), 1.0));
-    if (th <= M_PI / 2) {
-        append_piece(out, base, Corners{b[k], b[i], b[j]}, frac);
+    V3<T> u = p[i] - p[k], v = p[j] - p[k];
+    T cs = dot(u, v) / (norm(u) * norm(v));
+    T th = acos(std::min(std::max(cs, T(-1.0)), T(1.0)));
+    if (th <= T(M_PI / 2)) {
+        append_piece(out, base, CornersT<T>{b[k], b[i], b[j]}, frac);
         return;
     }
-    int m = int(std::ceil(th * (180.0 / M_PI) / corner_angle));  // rad2deg(θ) = θ * (180 / π), as Julia rounds it
-    std::vector<double> ts(m + 1);
-    ts[0] = 0;
-    ts[m] = 1;
-    double nu = norm(u), nv = norm(v);
+    int m = int(std::ceil(val(th) * (180.0 / M_PI) / corner_angle));  // rad2deg(θ) = θ * (180 / π), as Julia
+    std::vector<T> ts(m + 1);
+    ts[0] = T(0);
+    ts[m] = T(1);
+    T nu = norm(u), nv = norm(v);
     for (int q = 1; q < m; ++q) {
-        double phi = th * q / m;
-        ts[q] = nu * std::sin(phi) / (nu * std::sin(phi) + nv * std::sin(th - phi));
+        T phi = th * T(q) / T(m);
+        ts[q] = nu * sin(phi) / (nu * sin(phi) + nv * sin(th - phi));
     }
     for (int q = 0; q < m; ++q) {
-        Bary b1 = bmix(b[i], 1 - ts[q], b[j], ts[q]), b2 = bmix(b[i], 1 - ts[q + 1], b[j], ts[q + 1]);
-        append_piece(out, base, Corners{b[k], b1, b2}, frac * (ts[q + 1] - ts[q]));
+        BaryT<T> b1 = bmix(b[i], T(1) - ts[q], b[j], ts[q]), b2 = bmix(b[i], T(1) - ts[q + 1], b[j], ts[q + 1]);
+        append_piece(out, base, CornersT<T>{b[k], b1, b2}, frac * (ts[q + 1] - ts[q]));
     }
 }
 
 // vertex_rule (assemble.jl:119-125); returns a pointer to the stored rule or fills `buf`
-static const Rule* vertex_rule(const FlatTri& T, int k, const TierRules& rules, const Options& o, Rule& buf) {
-    Vec u = T.x[(k + 1) % 3] - T.x[k], v = T.x[(k + 2) % 3] - T.x[k];
-    if (dot(u, v) >= 0) return &rules.vertex[k];
+template <class T>
+static const RuleT<T>* vertex_rule(const FlatTriT<T>& Tr, int k, const TierRules& rules, const Options& o,
+                                   RuleT<T>& buf) {
+    V3<T> u = Tr.x[(k + 1) % 3] - Tr.x[k], v = Tr.x[(k + 2) % 3] - Tr.x[k];
+    if (dot(u, v) >= 0) return as_rule(rules.vertex[k], buf);
     buf.clear();
-    vertex_pieces(buf, T.x, k, rules.vertex[0], CORNERS, 1.0, o.corner_angle);
+    vertex_pieces(buf, Tr.x, k, rules.vertex[0], unit_corners<T>(), T(1), o.corner_angle);
     return &buf;
 }
 
 // edge_splits / splits_an_edge (assemble.jl:160-184); S is a flat triangle
-static void edge_splits(const Vec p[3], const FlatTri& S, double tol, std::vector<double> ts[3]) {
+template <class T>
+static void edge_splits(const V3<T> p[3], const FlatTriT<T>& S, const T& tol, std::vector<T> ts[3]) {
     for (int k = 0; k < 3; ++k) {
         ts[k].clear();
-        const Vec &a = p[k], &c = p[(k + 1) % 3];
-        double L = norm(c - a);
+        const V3<T> &a = p[k], &c = p[(k + 1) % 3];
+        T L = norm(c - a);
         for (int q = 0; q < 3; ++q) {
-            double d, t;
+            T d, t;
             segment_projection(S.x[q], a, c, d, t);
-            if (d <= tol && t * L > tol && (1 - t) * L > tol) ts[k].push_back(t);
+            if (d <= tol && t * L > tol && (T(1) - t) * L > tol) ts[k].push_back(t);
         }
         std::sort(ts[k].begin(), ts[k].end());
     }
 }
-static bool splits_an_edge(const Vec p[3], const FlatTri& S, double tol) {
+template <class T>
+static bool splits_an_edge(const V3<T> p[3], const FlatTriT<T>& S, const T& tol) {
     for (int k = 0; k < 3; ++k) {
-        const Vec &a = p[k], &c = p[(k + 1) % 3];
-        double L = norm(c - a);
+        const V3<T> &a = p[k], &c = p[(k + 1) % 3];
+        T L = norm(c - a);
         for (int q = 0; q < 3; ++q) {
-            double d, t;
+            T d, t;
             segment_projection(S.x[q], a, c, d, t);
-            if (d <= tol && t * L > tol && (1 - t) * L > tol) return true;
+            if (d <= tol && t * L > tol && (T(1) - t) * L > tol) return true;
         }
     }
     return false;
 }
 
 // contact_pieces! (assemble.jl:209-238)
-static void contact_pieces(Rule& out, const FlatTri& T, const FlatTri& S, const TierRules& rules, const Options& o,
-                           double tol, const Corners& b, double frac, int level) {
-    Vec p[3] = {point(T, b[0]), point(T, b[1]), point(T, b[2])};
+template <class T>
+static void contact_pieces(RuleT<T>& out, const FlatTriT<T>& Tr, const FlatTriT<T>& S, const TierRules& rules,
+                           const Options& o, const T& tol, const CornersT<T>& b, const T& frac, int level) {
+    V3<T> p[3] = {point(Tr, b[0]), point(Tr, b[1]), point(Tr, b[2])};
     if (level < 4) {
-        std::vector<double> splits[3];
+        std::vector<T> splits[3];
         edge_splits(p, S, tol, splits);
         int k = -1;
         for (int q = 0; q < 3; ++q)
             if (!splits[q].empty()) { k = q; break; }
         if (k >= 0) {
-            std::vector<double> ts;
-            ts.push_back(0.0);
+            std::vector<T> ts;
+            ts.push_back(T(0));
             ts.insert(ts.end(), splits[k].begin(), splits[k].end());
-            ts.push_back(1.0);
-            const Bary &bk = b[k], &bk1 = b[(k + 1) % 3], &opp = b[(k + 2) % 3];
+            ts.push_back(T(1));
+            const BaryT<T> &bk = b[k], &bk1 = b[(k + 1) % 3], &opp = b[(k + 2) % 3];
             for (size_t i = 0; i + 1 < ts.size(); ++i) {
-                Corners piece = {bmix(bk, 1 - ts[i], bk1, ts[i]), bmix(bk, 1 - ts[i + 1], bk1, ts[i + 1]), opp};
-                contact_pieces(out, T, S, rules, o, tol, piece, frac * (ts[i + 1] - ts[i]), level + 1);
+                CornersT<T> piece = {bmix(bk, T(1) - ts[i], bk1, ts[i]), bmix(bk, T(1) - ts[i + 1], bk1, ts[i + 1]),
+                                     opp};
+                contact_pieces(out, Tr, S, rules, o, tol, piece, frac * (ts[i + 1] - ts[i]), level + 1);
             }
             return;
         }
@@ -406,7 +448,7 @@ static void contact_pieces(Rule& out, const FlatTri& T, const FlatTri& S, const 
     }
     if (nc == 2) {
         int k = !on[2] ? 0 : (!on[0] ? 1 : 2);
-        if (distance_to(S, (p[k] + p[(k + 1) % 3]) / 2.0) <= tol) {
+        if (distance_to(S, (p[k] + p[(k + 1) % 3]) / T(2)) <= tol) {
             append_piece(out, rules.edge[k], b, frac);
             return;
         }
@@ -415,40 +457,43 @@ static void contact_pieces(Rule& out, const FlatTri& T, const FlatTri& S, const 
         int k = on[0] ? 0 : (on[1] ? 1 : 2);
         vertex_pieces(out, p, k, rules.vertex[0], b, frac, o.corner_angle);
     } else if (nc == 0) {
-        near_pieces(out, T, S, rules.near_, o.near_ratio, o.near_depth, b, frac, 0);
+        near_pieces(out, Tr, S, rules.near_, o.near_ratio, o.near_depth, b, frac, 0);
     } else {
         append_piece(out, rules.self, b, frac);
     }
 }
 
 // contact_rule (assemble.jl:199-207); returns false when S touches T at shared corners only
-static bool contact_rule(const FlatTri& T, const FlatTri& S, const bool shared[3], const TierRules& rules,
-                         const Options& o, Rule& out) {
-    double tol = o.contact_rel * std::min(T.diam, S.diam);
-    if (norm(S.c - T.c) > reach(T) + reach(S) + tol) return false;
+template <class T>
+static bool contact_rule(const FlatTriT<T>& Tr, const FlatTriT<T>& S, const bool shared[3], const TierRules& rules,
+                         const Options& o, RuleT<T>& out) {
+    T tol = T(o.contact_rel) * std::min(Tr.diam, S.diam);
+    if (norm(S.c - Tr.c) > reach(Tr) + reach(S) + tol) return false;
     bool extra = false;
     for (int k = 0; k < 3; ++k)
-        if (!shared[k] && distance_to(S, T.x[k]) <= tol) extra = true;
-    if (!extra) extra = splits_an_edge(T.x, S, tol);
+        if (!shared[k] && distance_to(S, Tr.x[k]) <= tol) extra = true;
+    if (!extra) extra = splits_an_edge(Tr.x, S, tol);
     if (!extra) return false;
     out.clear();
-    contact_pieces(out, T, S, rules, o, tol, CORNERS, 1.0, 0);
+    contact_pieces(out, Tr, S, rules, o, tol, unit_corners<T>(), T(1), 0);
     return true;
 }
 
 // near_rule (assemble.jl:69-73)
-template <class S>
-static void near_rule(Rule& out, const FlatTri& T, const S& src, const Rule& base, double ratio, int depth) {
+template <class T, class S>
+static void near_rule(RuleT<T>& out, const FlatTriT<T>& Tr, const S& src, const Rule& base, double ratio, int depth) {
     out.clear();
-    near_pieces(out, T, src, base, ratio, depth, CORNERS, 1.0, 0);
+    near_pieces(out, Tr, src, base, ratio, depth, unit_corners<T>(), T(1), 0);
 }
 
 // pair_rule (assemble.jl:266-282)
-static const Rule* pair_rule(const FlatTri* els, const int* tris, int t, int s, const TierRules& rules,
-                             const Options& o, const std::set<std::pair<int, int>>& touch, Rule& buf, int& tier) {
-    const FlatTri &T = els[t], &S = els[s];
-    if (s == t) { tier = SELF; return &rules.self; }
-    if (norm(S.c - T.c) > o.far_ratio * std::max(T.diam, S.diam)) { tier = FAR; return &rules.far; }
+template <class T>
+static const RuleT<T>* pair_rule(const FlatTriT<T>* els, const int* tris, int t, int s, const TierRules& rules,
+                                 const Options& o, const std::set<std::pair<int, int>>& touch, RuleT<T>& buf,
+                                 int& tier) {
+    const FlatTriT<T> &Tr = els[t], &S = els[s];
+    if (s == t) { tier = SELF; return as_rule(rules.self, buf); }
+    if (norm(S.c - Tr.c) > T(o.far_ratio) * std::max(Tr.diam, S.diam)) { tier = FAR; return as_rule(rules.far, buf); }
     const int* tri = tris + 3 * t;
     const int* gs = tris + 3 * s;
     bool shared[3];
@@ -457,63 +502,69 @@ static const Rule* pair_rule(const FlatTri* els, const int* tris, int t, int s, 
         shared[k] = tri[k] == gs[0] || tri[k] == gs[1] || tri[k] == gs[2];
         ns += shared[k];
     }
-    if (contact_rule(T, S, shared, rules, o, buf)) { tier = CONTACT; return &buf; }
+    if (contact_rule(Tr, S, shared, rules, o, buf)) { tier = CONTACT; return &buf; }
     if (ns == 2) {
         tier = EDGE;
-        return &rules.edge[(shared[0] && shared[1]) ? 0 : ((shared[1] && shared[2]) ? 1 : 2)];
+        return as_rule(rules.edge[(shared[0] && shared[1]) ? 0 : ((shared[1] && shared[2]) ? 1 : 2)], buf);
     }
     if (ns == 1) {
         tier = VERTEX;
         int k = shared[0] ? 0 : (shared[1] ? 1 : 2);
-        return vertex_rule(T, k, rules, o, buf);
+        return vertex_rule(Tr, k, rules, o, buf);
     }
     int depth = touch.count(std::make_pair(t, s)) ? o.near_depth + 4 : o.near_depth;
     tier = NEAR;
-    near_rule(buf, T, S, rules.near_, o.near_ratio, depth);
+    near_rule(buf, Tr, S, rules.near_, o.near_ratio, depth);
     return &buf;
 }
 
 // wake_pair_rule (assemble.jl:288-293)
-static const Rule* wake_pair_rule(const FlatTri& T, const FlatTri& S, const TierRules& rules, const Options& o,
-                                  Rule& buf, int& tier) {
-    if (norm(S.c - T.c) > o.far_ratio * std::max(T.diam, S.diam)) { tier = FAR; return &rules.far; }
+template <class T>
+static const RuleT<T>* wake_pair_rule(const FlatTriT<T>& Tr, const FlatTriT<T>& S, const TierRules& rules,
+                                      const Options& o, RuleT<T>& buf, int& tier) {
+    if (norm(S.c - Tr.c) > T(o.far_ratio) * std::max(Tr.diam, S.diam)) { tier = FAR; return as_rule(rules.far, buf); }
     bool none[3] = {false, false, false};
-    if (contact_rule(T, S, none, rules, o, buf)) { tier = CONTACT; return &buf; }
+    if (contact_rule(Tr, S, none, rules, o, buf)) { tier = CONTACT; return &buf; }
     tier = NEAR;
-    near_rule(buf, T, S, rules.near_, o.near_ratio, o.near_depth);
+    near_rule(buf, Tr, S, rules.near_, o.near_ratio, o.near_depth);
     return &buf;
 }
 
 // segment_rule (assemble.jl:299-306)
-static const Rule* segment_rule(const FlatTri& T, const Segment& f, const TierRules& rules, const Options& o,
-                                Rule& buf, int& tier) {
-    double L = norm(f.b - f.a);
-    if (norm((f.a + f.b) / 2.0 - T.c) > o.far_ratio * std::max(T.diam, L)) { tier = FAR; return &rules.far; }
+template <class T>
+static const RuleT<T>* segment_rule(const FlatTriT<T>& Tr, const SegmentT<T>& f, const TierRules& rules,
+                                    const Options& o, RuleT<T>& buf, int& tier) {
+    T L = norm(f.b - f.a);
+    if (norm((f.a + f.b) / T(2) - Tr.c) > T(o.far_ratio) * std::max(Tr.diam, L)) {
+        tier = FAR;
+        return as_rule(rules.far, buf);
+    }
     for (int k = 0; k < 3; ++k)
-        if (std::min(norm(T.x[k] - f.a), norm(T.x[k] - f.b)) <= 1e-12 * T.diam) {
+        if (std::min(norm(Tr.x[k] - f.a), norm(Tr.x[k] - f.b)) <= T(1e-12) * Tr.diam) {
             tier = VERTEX;
-            return vertex_rule(T, k, rules, o, buf);
+            return vertex_rule(Tr, k, rules, o, buf);
         }
     tier = NEAR;
-    near_rule(buf, T, f, rules.near_, o.near_ratio, o.near_depth);
+    near_rule(buf, Tr, f, rules.near_, o.near_ratio, o.near_depth);
     return &buf;
 }
 
 // pair_block (assemble.jl:245-258)
-static void pair_block(const FlatTri& T, const FlatTri& S, const Rule& rule, double sigS, int test, int side,
-                       double kernel_far, double blk[3][3], double rb[3]) {
+template <class T>
+static void pair_block(const FlatTriT<T>& Tr, const FlatTriT<T>& S, const RuleT<T>& rule, const T& sigS, int test,
+                       int side, double kernel_far, T blk[3][3], T rb[3]) {
     for (int a = 0; a < 3; ++a) {
-        rb[a] = 0;
-        for (int b = 0; b < 3; ++b) blk[a][b] = 0;
+        rb[a] = T(0);
+        for (int b = 0; b < 3; ++b) blk[a][b] = T(0);
     }
     for (size_t q = 0; q < rule.size(); ++q) {
-        const Bary& l = rule.lam[q];
-        Vec w = source_velocity(S.src, point(T, l), side, kernel_far);
-        double W = rule.w[q] * T.area;
-        Vec v = cross(w, T.n);
-        double c[3] = {dot(v, S.gam[0]), dot(v, S.gam[1]), dot(v, S.gam[2])};
-        Vec psi = W * test_weights(test, l);
-        double wn = sigS * dot(w, T.n);
+        const BaryT<T>& l = rule.lam[q];
+        V3<T> w = source_velocity(S.src, point(Tr, l), side, kernel_far);
+        T W = rule.w[q] * Tr.area;
+        V3<T> v = cross(w, Tr.n);
+        T c[3] = {dot(v, S.gam[0]), dot(v, S.gam[1]), dot(v, S.gam[2])};
+        V3<T> psi = W * test_weights(test, l);
+        T wn = sigS * dot(w, Tr.n);
         for (int a = 0; a < 3; ++a) {
             for (int b = 0; b < 3; ++b) blk[a][b] += psi[a] * c[b];
             rb[a] -= wn * psi[a];
@@ -522,13 +573,15 @@ static void pair_block(const FlatTri& T, const FlatTri& S, const Rule& rule, dou
 }
 
 // segment_block (assemble.jl:312-321)
-static void segment_block(const FlatTri& T, const Segment& f, const Rule& rule, int test, double ca[3], double cb[3]) {
-    for (int a = 0; a < 3; ++a) ca[a] = cb[a] = 0;
+template <class T>
+static void segment_block(const FlatTriT<T>& Tr, const SegmentT<T>& f, const RuleT<T>& rule, int test, T ca[3],
+                          T cb[3]) {
+    for (int a = 0; a < 3; ++a) ca[a] = cb[a] = T(0);
     for (size_t q = 0; q < rule.size(); ++q) {
-        Vec va, vb;
-        segment_velocity(f.a, f.b, point(T, rule.lam[q]), va, vb);
-        Vec psi = (rule.w[q] * T.area) * test_weights(test, rule.lam[q]);
-        double da = dot(va, T.n), db = dot(vb, T.n);
+        V3<T> va, vb;
+        segment_velocity(f.a, f.b, point(Tr, rule.lam[q]), va, vb);
+        V3<T> psi = (rule.w[q] * Tr.area) * test_weights(test, rule.lam[q]);
+        T da = dot(va, Tr.n), db = dot(vb, Tr.n);
         for (int a = 0; a < 3; ++a) {
             ca[a] += da * psi[a];
             cb[a] += db * psi[a];
@@ -537,6 +590,14 @@ static void segment_block(const FlatTri& T, const Segment& f, const Rule& rule, 
 }
 
 static inline Vec vec_at(const double* x, int i) { return Vec(x[3 * i], x[3 * i + 1], x[3 * i + 2]); }
+
+template <class T>
+static bool build_elements(int ntri, const V3<T>* X, const int* tris, std::vector<FlatTriT<T>>& els) {
+    els.resize(ntri);
+    for (int t = 0; t < ntri; ++t)
+        if (!make_flat_tri(X[tris[3 * t]], X[tris[3 * t + 1]], X[tris[3 * t + 2]], els[t])) return false;
+    return true;
+}
 
 static bool build_elements(int ntri, const double* x, const int* tris, std::vector<FlatTri>& els) {
     els.resize(ntri);
@@ -759,6 +820,110 @@ int vpo_assemble_list(const vpo_options* po, int nnode, const double* x, int ntr
                           wtris, nfil, fil, 0, ntest, tlist, A, b, pairs, points, nthreads);
 }
 
+}  // extern "C"
+
+namespace vpo {
+
+// the rows of test triangles t0..t1-1 (or tlist[t0..t1)) of assemble (assemble.jl:377-447) over built elements:
+// body pairs, wake sheets (add_wake!, :333-356), filaments and the exact freestream term (:422). A (nslot x ncols)
+// and b are accumulated; per-tier pair and point counts go to P, Q.
+template <class T>
+static void assemble_core(const Options& o, const TierRules& rules, const std::vector<FlatTriT<T>>& els,
+                          const int* tris, const int* corner_slot, int nslot, const std::set<std::pair<int, int>>& touch,
+                          const T* sigma, const V3<T>& Vinf, int nwnode, const std::vector<FlatTriT<T>>& wels,
+                          const int* wtris, const std::vector<SegmentT<T>>& segs, const int* fil, int t0, int t1,
+                          const int* tlist, T* A, T* b, long long* P, long long* Q, int nthreads) {
+    const int ntri = int(els.size()), nwtri = int(wels.size()), nfil = int(segs.size());
+    const int ncols = nslot + nwnode;
+    const Vec ti = test_integrals(o.test);
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+    (void)nthreads;
+#endif
+#pragma omp parallel
+    {
+        std::vector<T> buf(size_t(3) * ncols);
+        RuleT<T> rbuf;
+        long long myP[6] = {0}, myQ[6] = {0};
+#pragma omp for schedule(dynamic, 4)
+        for (int it = t0; it < t1; ++it) {
+            const int t = tlist ? tlist[it] : it;
+            const FlatTriT<T>& Tr = els[t];
+            std::fill(buf.begin(), buf.end(), T(0));
+            T rows[3] = {T(0), T(0), T(0)};
+            for (int s = 0; s < ntri; ++s) {
+                int tier;
+                const RuleT<T>* rule = pair_rule(els.data(), tris, t, s, rules, o, touch, rbuf, tier);
+                T blk[3][3], rb[3];
+                pair_block(Tr, els[s], *rule, sigma[s], o.test, s == t ? 1 : 0, o.kernel_far, blk, rb);
+                const int* cs = corner_slot + 3 * s;
+                for (int bb = 0; bb < 3; ++bb)
+                    for (int a = 0; a < 3; ++a) buf[size_t(a) * ncols + cs[bb]] += blk[a][bb];
+                for (int a = 0; a < 3; ++a) rows[a] += rb[a];
+                myP[tier] += 1;
+                myQ[tier] += (long long)rule->size();
+            }
+            // add_wake! (assemble.jl:333-356)
+            for (int s = 0; s < nwtri; ++s) {
+                int tier;
+                const RuleT<T>* rule = wake_pair_rule(Tr, wels[s], rules, o, rbuf, tier);
+                T blk[3][3], rb[3];
+                pair_block(Tr, wels[s], *rule, T(0), o.test, 0, o.kernel_far, blk, rb);
+                const int* c = wtris + 3 * s;
+                for (int bb = 0; bb < 3; ++bb)
+                    for (int a = 0; a < 3; ++a) buf[size_t(a) * ncols + nslot + c[bb]] += blk[a][bb];
+                myP[tier] += 1;
+                myQ[tier] += (long long)rule->size();
+            }
+            for (int f = 0; f < nfil; ++f) {
+                int tier;
+                const RuleT<T>* rule = segment_rule(Tr, segs[f], rules, o, rbuf, tier);
+                T ca[3], cb[3];
+                segment_block(Tr, segs[f], *rule, o.test, ca, cb);
+                int ia = fil[2 * f], ib = fil[2 * f + 1];
+                for (int a = 0; a < 3; ++a) {
+                    buf[size_t(a) * ncols + nslot + ia] += ca[a];
+                    buf[size_t(a) * ncols + nslot + ib] += cb[a];
+                }
+                myP[tier] += 1;
+                myQ[tier] += (long long)rule->size();
+            }
+            // freestream (exact), assemble.jl:422
+            T vn = dot(Vinf, Tr.n) * Tr.area;
+            for (int a = 0; a < 3; ++a) rows[a] -= vn * T(ti[a]);
+            const int* ct = corner_slot + 3 * t;
+#pragma omp critical(vpo_scatter)
+            {
+                for (int a = 0; a < 3; ++a) {
+                    T* Arow = A + size_t(ct[a]) * ncols;
+                    const T* src = buf.data() + size_t(a) * ncols;
+                    for (int j = 0; j < ncols; ++j) Arow[j] += src[j];
+                    b[ct[a]] += rows[a];
+                }
+            }
+        }
+#pragma omp critical(vpo_stats)
+        for (int k = 0; k < 6; ++k) {
+            P[k] += myP[k];
+            Q[k] += myQ[k];
+        }
+    }
+}
+
+static std::set<std::pair<int, int>> touch_set(int ntouch, const int* touch_pairs) {
+    std::set<std::pair<int, int>> touch;
+    for (int i = 0; i < ntouch; ++i) {
+        touch.insert({touch_pairs[2 * i], touch_pairs[2 * i + 1]});
+        touch.insert({touch_pairs[2 * i + 1], touch_pairs[2 * i]});
+    }
+    return touch;
+}
+
+}  // namespace vpo
+
+extern "C" {
+
 static int assemble_tests(const vpo_options* po, int ntri, const double* x, const int* tris, const int* corner_slot,
                           int nslot, int ntouch, const int* touch_pairs, const double* sigma, const double* V,
                           int nwnode, const double* wx, int nwtri, const int* wtris, int nfil, const int* fil, int t0,
@@ -771,93 +936,97 @@ static int assemble_tests(const vpo_options* po, int ntri, const double* x, cons
     if (nwtri > 0 && !build_elements(nwtri, wx, wtris, wels)) return -1;
     std::vector<Segment> segs(nfil);
     for (int f = 0; f < nfil; ++f) segs[f] = Segment{vec_at(wx, fil[2 * f]), vec_at(wx, fil[2 * f + 1])};
-    std::set<std::pair<int, int>> touch;
-    for (int i = 0; i < ntouch; ++i) {
-        touch.insert({touch_pairs[2 * i], touch_pairs[2 * i + 1]});
-        touch.insert({touch_pairs[2 * i + 1], touch_pairs[2 * i]});
-    }
-    const Vec Vinf = vec_at(V, 0);
-    const int ncols = nslot + nwnode;
-    const Vec ti = test_integrals(o.test);
-    long long P[6] = {0}, Q[6] = {0};
     if (t0 < 0) t0 = 0;
     if (!tlist && t1 > ntri) t1 = ntri;
-#ifdef _OPENMP
-    if (nthreads > 0) omp_set_num_threads(nthreads);
-#else
-    (void)nthreads;
-#endif
-#pragma omp parallel
-    {
-        std::vector<double> buf(size_t(3) * ncols);
-        Rule rbuf;
-        long long myP[6] = {0}, myQ[6] = {0};
-#pragma omp for schedule(dynamic, 4)
-        for (int it = t0; it < t1; ++it) {
-            const int t = tlist ? tlist[it] : it;
-            const FlatTri& T = els[t];
-            std::fill(buf.begin(), buf.end(), 0.0);
-            double rows[3] = {0, 0, 0};
-            for (int s = 0; s < ntri; ++s) {
-                int tier;
-                const Rule* rule = pair_rule(els.data(), tris, t, s, rules, o, touch, rbuf, tier);
-                double blk[3][3], rb[3];
-                pair_block(T, els[s], *rule, sigma[s], o.test, s == t ? 1 : 0, o.kernel_far, blk, rb);
-                const int* cs = corner_slot + 3 * s;
-                for (int bb = 0; bb < 3; ++bb)
-                    for (int a = 0; a < 3; ++a) buf[size_t(a) * ncols + cs[bb]] += blk[a][bb];
-                for (int a = 0; a < 3; ++a) rows[a] += rb[a];
-                myP[tier] += 1;
-                myQ[tier] += (long long)rule->size();
+    long long P[6] = {0}, Q[6] = {0};
+    assemble_core(o, rules, els, tris, corner_slot, nslot, touch_set(ntouch, touch_pairs), sigma, vec_at(V, 0), nwnode,
+                  wels, wtris, segs, fil, t0, t1, tlist, A, b, P, Q, nthreads);
+    for (int k = 0; k < 6; ++k) {
+        pairs[k] += P[k];
+        points[k] += Q[k];
+    }
+    return 0;
+}
+
+// ---- the derivative oracle: the assembly in forward-mode dual numbers ----
+
+// directions one dual pass carries
+int vpo_dual_nd(void) { return VPO_ND; }
+
+// A and b of assemble (assemble.jl:377-447) with their derivatives along nd <= VPO_ND directions. Node positions x
+// (nnode x 3) with tangents dx (nd x nnode x 3); the wake's nodes wx (nwnode x 3) with dwx (nd x nwnode x 3); the
+// freestream V with dV (nd x 3). sigma = -n.V (assemble.jl:364) is formed from the dual normals and V. Out, each
+// with (1 + nd) layers (value, then the nd derivatives): A (nslot x (nslot + nwnode)), b (nslot), and per body
+// triangle its area, normal (3) and barycentric gradients gradl (9) (flat_triangle.jl:12-31), 13 values.
+int vpo_dual_assemble(const vpo_options* po, int nnode, const double* x, const double* dx, int ntri, const int* tris,
+                      const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* V,
+                      const double* dV, int nwnode, const double* wx, const double* dwx, int nwtri, const int* wtris,
+                      int nfil, const int* fil, int nd, double* A, double* b, double* elem, long long* pairs,
+                      long long* points, int nthreads) {
+    typedef Dual<VPO_ND> D;
+    if (nd < 0 || nd > VPO_ND) return -2;
+    auto dual_points = [nd](int n, const double* p, const double* dp) {
+        std::vector<V3<D>> X(n);
+        for (int i = 0; i < n; ++i)
+            for (int c = 0; c < 3; ++c) {
+                D v(p[3 * i + c]);
+                for (int k = 0; k < nd; ++k) v.d[k] = dp[(size_t(k) * n + i) * 3 + c];
+                X[i][c] = v;
             }
-            // add_wake! (assemble.jl:333-356)
-            for (int s = 0; s < nwtri; ++s) {
-                int tier;
-                const Rule* rule = wake_pair_rule(T, wels[s], rules, o, rbuf, tier);
-                double blk[3][3], rb[3];
-                pair_block(T, wels[s], *rule, 0.0, o.test, 0, o.kernel_far, blk, rb);
-                const int* c = wtris + 3 * s;
-                for (int bb = 0; bb < 3; ++bb)
-                    for (int a = 0; a < 3; ++a) buf[size_t(a) * ncols + nslot + c[bb]] += blk[a][bb];
-                myP[tier] += 1;
-                myQ[tier] += (long long)rule->size();
-            }
-            for (int f = 0; f < nfil; ++f) {
-                int tier;
-                const Rule* rule = segment_rule(T, segs[f], rules, o, rbuf, tier);
-                double ca[3], cb[3];
-                segment_block(T, segs[f], *rule, o.test, ca, cb);
-                int ia = fil[2 * f], ib = fil[2 * f + 1];
-                for (int a = 0; a < 3; ++a) {
-                    buf[size_t(a) * ncols + nslot + ia] += ca[a];
-                    buf[size_t(a) * ncols + nslot + ib] += cb[a];
-                }
-                myP[tier] += 1;
-                myQ[tier] += (long long)rule->size();
-            }
-            // freestream (exact), assemble.jl:422
-            double vn = dot(Vinf, T.n) * T.area;
-            for (int a = 0; a < 3; ++a) rows[a] -= vn * ti[a];
-            const int* ct = corner_slot + 3 * t;
-#pragma omp critical(vpo_scatter)
-            {
-                for (int a = 0; a < 3; ++a) {
-                    double* Arow = A + size_t(ct[a]) * ncols;
-                    const double* src = buf.data() + size_t(a) * ncols;
-                    for (int j = 0; j < ncols; ++j) Arow[j] += src[j];
-                    b[ct[a]] += rows[a];
-                }
-            }
-        }
-#pragma omp critical(vpo_stats)
-        for (int k = 0; k < 6; ++k) {
-            P[k] += myP[k];
-            Q[k] += myQ[k];
+        return X;
+    };
+    const std::vector<V3<D>> X = dual_points(nnode, x, dx), WX = dual_points(nwnode, wx, dwx);
+    const V3<D> Vd = dual_points(1, V, dV)[0];
+    Options o = to_opts(po);
+    TierRules rules = tier_rules(o);
+    std::vector<FlatTriT<D>> els, wels;
+    if (!build_elements(ntri, X.data(), tris, els)) return -1;
+    if (nwtri > 0 && !build_elements(nwtri, WX.data(), wtris, wels)) return -1;
+    std::vector<SegmentT<D>> segs(nfil);
+    for (int f = 0; f < nfil; ++f) segs[f] = SegmentT<D>{WX[fil[2 * f]], WX[fil[2 * f + 1]]};
+    std::vector<D> sigma(ntri);
+    for (int t = 0; t < ntri; ++t) sigma[t] = -dot(els[t].n, Vd);
+    const int ncols = nslot + nwnode;
+    std::vector<D> Ad(size_t(nslot) * ncols), bd(nslot);
+    long long P[6] = {0}, Q[6] = {0};
+    assemble_core(o, rules, els, tris, corner_slot, nslot, touch_set(ntouch, touch_pairs), sigma.data(), Vd, nwnode,
+                  wels, wtris, segs, fil, 0, ntri, nullptr, Ad.data(), bd.data(), P, Q, nthreads);
+    const size_t na = Ad.size();
+    for (int k = 0; k <= nd; ++k) {
+        auto pick = [k](const D& v) { return k == 0 ? v.v : v.d[k - 1]; };
+        for (size_t i = 0; i < na; ++i) A[k * na + i] = pick(Ad[i]);
+        for (int i = 0; i < nslot; ++i) b[size_t(k) * nslot + i] = pick(bd[i]);
+        for (int t = 0; t < ntri; ++t) {
+            double* e = elem + (size_t(k) * ntri + t) * 13;
+            const FlatTriT<D>& el = els[t];
+            e[0] = pick(el.area);
+            for (int c = 0; c < 3; ++c) e[1 + c] = pick(el.n[c]);
+            for (int j = 0; j < 3; ++j)
+                for (int c = 0; c < 3; ++c) e[4 + 3 * j + c] = pick(el.gradl[j][c]);
         }
     }
     for (int k = 0; k < 6; ++k) {
         pairs[k] += P[k];
         points[k] += Q[k];
+    }
+    return 0;
+}
+
+// source_velocity (source_triangle.jl:134-138) of triangle abc at x with its Jacobian J (3 x 3, row = component of
+// w, column = direction): wrt = 0 the point x, wrt = 1 the vertex a
+int vpo_dual_source_velocity(const double* abc, const double* x, int wrt, double far, double* w, double* J) {
+    typedef Dual<VPO_ND> D;
+    V3<D> v[3], xd;
+    for (int i = 0; i < 3; ++i)
+        for (int c = 0; c < 3; ++c) v[i][c] = D(abc[3 * i + c]);
+    for (int c = 0; c < 3; ++c) xd[c] = D(x[c]);
+    for (int c = 0; c < 3; ++c) (wrt == 0 ? xd : v[0])[c].d[c] = 1.0;
+    SourceTri<D> s;
+    if (!make_source_tri(v[0], v[1], v[2], s)) return -1;
+    const V3<D> r = source_velocity(s, xd, 0, far);
+    for (int i = 0; i < 3; ++i) {
+        w[i] = r[i].v;
+        for (int c = 0; c < 3; ++c) J[3 * i + c] = r[i].d[c];
     }
     return 0;
 }

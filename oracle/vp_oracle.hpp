@@ -179,34 +179,43 @@ V3<T> blob_velocity(const V3<T>& x, const V3<T>& xp, const V3<T>& al, T delta) {
 }
 
 // ---- elements (src/elements/flat_triangle.jl:12-31, 59-78) ----
-struct FlatTri {
-    Vec x[3], n, c;
-    double area, diam;
-    Vec gradl[3], gam[3];
-    SourceTri<double> src;
+template <class T>
+struct FlatTriT {
+    V3<T> x[3], n, c;
+    T area, diam;
+    V3<T> gradl[3], gam[3];
+    SourceTri<T> src;
 };
-bool make_flat_tri(const Vec& a, const Vec& b, const Vec& c, FlatTri& t);
-inline Vec point(const FlatTri& T, const Bary& l) { return l[0] * T.x[0] + l[1] * T.x[1] + l[2] * T.x[2]; }
-double distance_to(const FlatTri& el, const Vec& p);
-double reach(const FlatTri& el);
+typedef FlatTriT<double> FlatTri;
+template <class T>
+bool make_flat_tri(const V3<T>& a, const V3<T>& b, const V3<T>& c, FlatTriT<T>& t);
+template <class T, class B>
+inline V3<T> point(const FlatTriT<T>& Tr, const B& l) {
+    return T(l[0]) * Tr.x[0] + T(l[1]) * Tr.x[1] + T(l[2]) * Tr.x[2];
+}
 
-struct Segment {
-    Vec a, b;
+template <class T>
+struct SegmentT {
+    V3<T> a, b;
 };
+typedef SegmentT<double> Segment;
 struct Blob {
     Vec x, al;
     double delta;
 };
-double distance_to(const Segment& s, const Vec& p);
 double distance_to(const Blob& b, const Vec& p);
 
 // ---- rules (src/elements/rules.jl) ----
-struct Rule {
-    std::vector<Bary> lam;
-    std::vector<double> w;
+template <class T>
+using BaryT = std::array<T, 3>;
+template <class T>
+struct RuleT {
+    std::vector<BaryT<T>> lam;
+    std::vector<T> w;
     size_t size() const { return w.size(); }
     void clear() { lam.clear(); w.clear(); }
 };
+typedef RuleT<double> Rule;
 void gauss_legendre(int n, std::vector<double>& x, std::vector<double>& w);
 void graded_gauss(int levels, double ratio, int order, std::vector<double>& x, std::vector<double>& w);
 void graded_gauss_both(int levels, double ratio, int order, std::vector<double>& x, std::vector<double>& w);

@@ -672,6 +672,29 @@ __device__ __noinline__ void fold_w(AdjAccW& acc, int lane) {
     acc.nb = 0;
 }
 
+// the fold of the dependent piece's fields only (Bb, Fb), at the end of a piece: the pair's sums stay in the partials
+__device__ __noinline__ void fold_piece(AdjAccW& acc, int lane) {
+    __syncwarp();
+    float* base = reinterpret_cast<float*>(acc.lanes);
+#pragma unroll
+    for (int j = ADJ_BB0 / 32; j < ADJ_TSLOT; ++j) {
+        const int z = lane + 32 * j;
+        if (z >= ADJ_BB0 && z < ADJ_NFIELD) {
+            float s0 = 0.f, s1 = 0.f;
+            for (int l = 0; l < 16; ++l) {
+                float* p0 = base + l * ADJ_LSTRIDE + z;
+                float* p1 = base + (l + 16) * ADJ_LSTRIDE + z;
+                s0 += *p0;
+                s1 += *p1;
+                *p0 = 0.f;
+                *p1 = 0.f;
+            }
+            acc.tot[j] += double(s0) + double(s1);
+        }
+    }
+    __syncwarp();
+}
+
 // the FP64 total of field z (a compile-time index after unrolling), in every lane
 __device__ __forceinline__ double tot_field(const AdjAccW& acc, int z) {
     return __shfl_sync(0xffffffffu, acc.tot[z >> 5], z & 31);
@@ -1112,7 +1135,7 @@ __device__ void piece_begin(PairCtx& pc, AdjAccW& acc, const double* c, double f
 __device__ void piece_end(PairCtx& pc, AdjAccW& acc) {
     if (!pc.dep) return;
     if (pc.nleaf) flush_leaves(pc, acc);
-    fold_w(acc, pc.lane);
+    fold_piece(acc, pc.lane);
 #pragma unroll
     for (int j = 0; j < ADJ_MAX; ++j) {
         if (j >= pc.nadj) break;
