@@ -7,6 +7,8 @@
 #pragma once
 #include <cmath>
 
+#include "vp_oracle.hpp"
+
 namespace vpo {
 
 constexpr int VPO_ND = 8;  // directions of one dual pass of the oracle
@@ -100,5 +102,17 @@ template <int N> inline Dual<N> atan2(const Dual<N>& y, const Dual<N>& x) {
     return r;
 }
 template <int N> inline Dual<N> fabs(const Dual<N>& a) { return a.v < 0 ? -a : a; }
+
+// the in-plane branch of the solid angle: its value, with the off-plane formula's derivatives
+template <int N>
+struct carries_derivatives<Dual<N>> {
+    static const bool value = true;
+};
+template <int N>
+inline Dual<N> plane_limit(const Dual<N>& in_plane, const Dual<N>& off_plane) {
+    Dual<N> r = off_plane;
+    r.v = in_plane.v;
+    return r;
+}
 
 }  // namespace vpo

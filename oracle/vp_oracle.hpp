@@ -103,10 +103,29 @@ T inplane_fraction(const SourceTri<T>& tri, const V3<T>& x, double tol) {
     return acos(cs) / (T(2) * T(M_PI));
 }
 
+// numbers that carry derivatives (the derivative oracle's duals) take the in-plane branch's value with the
+// derivatives of the off-plane solid angle: the in-plane set has measure zero, so under any move of the geometry the
+// solid angle of such a point follows the off-plane formula
+template <class T>
+struct carries_derivatives {
+    static const bool value = false;
+};
+template <class T>
+inline T plane_limit(const T& in_plane, const T&) { return in_plane; }
+
+// the solid angle of the triangle seen from offsets ra, rb, rc (Van Oosterom-Strackee), source_triangle.jl:85-87
+template <class T>
+inline T solid_angle(const V3<T>& ra, const V3<T>& rb, const V3<T>& rc) {
+    using std::atan2;
+    T la = norm(ra), lb = norm(rb), lc = norm(rc);
+    T N = dot(ra, cross(rb, rc));
+    T D = la * lb * lc + dot(ra, rb) * lc + dot(ra, rc) * lb + dot(rb, rc) * la;
+    return T(2) * atan2(N, D);
+}
+
 // source_velocity_exact (source_triangle.jl:75-89)
 template <class T>
 V3<T> source_velocity_exact(const SourceTri<T>& tri, const V3<T>& x, int side, double plane_tol) {
-    using std::atan2;
     V3<T> ra = x - tri.v[0], rb = x - tri.v[1], rc = x - tri.v[2];
     V3<T> wt = edge_log(ra, rb, tri.len[0]) * tri.nu[0] + edge_log(rb, rc, tri.len[1]) * tri.nu[1] +
                edge_log(rc, ra, tri.len[2]) * tri.nu[2];
@@ -114,11 +133,9 @@ V3<T> source_velocity_exact(const SourceTri<T>& tri, const V3<T>& x, int side, d
     T Om;
     if (std::fabs(double(z)) <= plane_tol * double(tri.diam)) {
         Om = T(side) * T(2) * T(M_PI) * inplane_fraction(tri, x, plane_tol);
+        if (carries_derivatives<T>::value) Om = plane_limit(Om, solid_angle(ra, rb, rc));
     } else {
-        T la = norm(ra), lb = norm(rb), lc = norm(rc);
-        T N = dot(ra, cross(rb, rc));
-        T D = la * lb * lc + dot(ra, rb) * lc + dot(ra, rc) * lb + dot(rb, rc) * la;
-        Om = T(2) * atan2(N, D);
+        Om = solid_angle(ra, rb, rc);
     }
     return (wt + Om * tri.n) / (T(4) * T(M_PI));
 }

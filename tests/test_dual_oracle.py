@@ -78,12 +78,16 @@ def test_wing_tangents_against_oracle_differences():
     W = meshes.wake_rows(w.dm, wake.te)
     a = math.radians(5.0)
     rng = np.random.default_rng(1)
-    nodes = list(rng.choice(wingcase.clear_nodes(w.g), 3, replace=False))
-    nodes.append(int(w.dm.wake_te.node[len(w.dm.wake_te.node) // 2]))
+    nodes = [(int(n), int(rng.integers(3))) for n in rng.choice(wingcase.clear_nodes(w.g), 3, replace=False)]
+    nodes.append((int(w.dm.wake_te.node[len(w.dm.wake_te.node) // 2]), 0))
+    # the trailing edge node at the tip, across the wake's plane: points of the tip cap lie in the first wake sheet's
+    # plane, where the solid angle's value takes the in-plane branch and its derivative the off-plane formula's
+    te = w.dm.wake_te.node
+    nodes.append((int(te[np.argmin(w.g.x[te, 1])]), 2))
     dirs = []
-    for n in nodes:
+    for n, c in nodes:
         dx = np.zeros((w.g.nnode, 3))
-        dx[n, int(rng.integers(3))] = 1.0
+        dx[n, c] = 1.0
         dirs.append((dx, 0.0))
     dirs.append((np.zeros((w.g.nnode, 3)), 1.0))
     CL, CDi, dCL, dCDi = dual_oracle.wing_loads_tangent(w, wake, W, a, dirs)

@@ -332,18 +332,24 @@ __device__ __forceinline__ AdjSums<double> sums_unflat(const double* f) {
     return a;
 }
 
-struct AdjChunkSh {
-    NearPlanSh pl;
-    double acc[32][NSUM];  // per pair: the sums of its FP64 points
-    float accf[32][NSUM];  // and of its FP32 points
-    double m64[32][3];     // the pair's direction m
-    int off[33];           // points before each pair
-    int qp[64], qk[64];    // queued FP64 points: pair, point within the pair
+// the adjoint vectors of one pass of the warp-cooperative kernels, each with its outputs
+struct AdjMulti {
+    AdjExtra x[ADJ_MAX];
+    int nadj;
 };
 
-// the FP64 adjoint evaluation of point k of pair p (queued by the FP32 guard)
-__device__ void adj_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S, const AdjChunkSh& ns, const double* nu,
-                            int p, int k, double* v) {
+struct AdjChunkSh {
+    NearPlanSh pl;
+    float accf[ADJ_MAX][32][NSUM];  // per adjoint vector and pair: the sums of the pair's points
+    double m64[32][3];              // the pair's direction m
+    int off[33];                    // points before each pair
+    int qp[64], qk[64];             // queued FP64 points: pair, point within the pair
+};
+
+// the FP64 adjoint evaluation of point k of pair p (queued by the FP32 guard) for the K vectors with test-corner
+// values nu[j]: the kernel and its derivatives once, each vector's sums in v[j] (in the AdjSums field order)
+__device__ void adj_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S, const AdjChunkSh& ns,
+                            const double (*nu)[3], int K, int p, int k, float (*v)[NSUM]) {
     const int nr = a.nrule[R_NEAR];
     int leaf = k / nr, q = k - leaf * nr;
     float bf[9];
@@ -357,7 +363,8 @@ __device__ void adj_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S,
     int level = ns.pl.leaf[p][leaf] >> 6;
     double W = (m.w * ldexp(1.0, -2 * level)) * T.area;
     v3<double> psi = test_weights(a.test_mode, l0, l1, l2);
-    double Wn = W * (nu[0] * psi.x + nu[1] * psi.y + nu[2] * psi.z);
+    double Wn[ADJ_MAX];
+    for (int j = 0; j < ADJ_MAX; ++j) Wn[j] = W * (nu[j][0] * psi.x + nu[j][1] * psi.y + nu[j][2] * psi.z);
     v3<double> R[3];
     for (int c = 0; c < 3; ++c)
         R[c] = mk3(l0 * (T.x[0] - S.x[3 * c]) + l1 * (T.x[3] - S.x[3 * c]) + l2 * (T.x[6] - S.x[3 * c]),
@@ -366,33 +373,40 @@ __device__ void adj_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S,
     v3<double> x = mk3(l0 * T.x[0] + l1 * T.x[3] + l2 * T.x[6], l0 * T.x[1] + l1 * T.x[4] + l2 * T.x[7],
                        l0 * T.x[2] + l1 * T.x[5] + l2 * T.x[8]);
     v3<double> r = x - ld3(S.c);
-    SrcKern<double> K;
+    SrcKern<double> Kd;
     for (int z = 0; z < 3; ++z) {
-        K.d[z] = mk3(S.x[3 * z] - S.c[0], S.x[3 * z + 1] - S.c[1], S.x[3 * z + 2] - S.c[2]);
-        K.nu[z] = ld3(S.nu + 3 * z);
-        K.len[z] = S.len[z];
+        Kd.d[z] = mk3(S.x[3 * z] - S.c[0], S.x[3 * z + 1] - S.c[1], S.x[3 * z + 2] - S.c[2]);
+        Kd.nu[z] = ld3(S.nu + 3 * z);
+        Kd.len[z] = S.len[z];
     }
-    K.n = ld3(S.n);
-    K.area = S.area;
-    K.diam = S.diam;
+    Kd.n = ld3(S.n);
+    Kd.area = S.area;
+    Kd.diam = S.diam;
     const v3<double> mm = mk3(ns.m64[p][0], ns.m64[p][1], ns.m64[p][2]);
-    AdjSums<double> as;
-    adj_zero(as);
-    double fd = a.kernel_far * K.diam;
+    AdjSums<double> as[ADJ_MAX];
+    for (int j = 0; j < ADJ_MAX; ++j) adj_zero(as[j]);
+    v3<double> gx;
+    double fd = a.kernel_far * Kd.diam;
     if (dot(r, r) > fd * fd)
-        adj_point_far(as, K, Wn, l0, l1, l2, r, mm);
+        adj_point_far_multi(as, K, Wn, Kd, l0, l1, l2, r, mm, gx);
     else
-        adj_point_exact(as, K, Wn, l0, l1, l2, R[0], R[1], R[2], r, mm, 0, 1e-12);
-    sums_flat(as, v);
+        adj_point_exact_multi(as, K, Wn, Kd, l0, l1, l2, R[0], R[1], R[2], r, mm, 0, 1e-12, gx);
+    for (int j = 0; j < K; ++j) {
+        double f[NSUM];
+        sums_flat(as[j], f);
+        for (int z = 0; z < NSUM; ++z) v[j][z] = float(f[z]);
+    }
 }
 
-// one chunk of up to 32 sources of test t; returns the lanes whose pairs are not in the near tier
-__device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, int t, const int* list, int cnt,
-                              bool wake, v3<double>* Xg, v3<double>& U, double& fs, unsigned long long* P,
+// one chunk of up to 32 sources of test t, for every adjoint vector of mx at once (the plan and each point's kernel
+// once); returns the lanes whose pairs are not in the near tier. Xg, U, fs: this lane's test-side sums per vector.
+__device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjMulti& mx, int t, const int* list, int cnt,
+                              bool wake, v3<double> (*Xg)[3], v3<double>* U, double* fs, unsigned long long* P,
                               unsigned long long* Q, unsigned long long& Q64) {
     const NearArgs& a = *pc.a;
     const TriGeo& T = *pc.T;
     const int lane = pc.lane;
+    const int K = mx.nadj;
     const unsigned FULL = 0xffffffffu;
     const bool valid = lane < cnt;
     const int s = valid ? list[lane] : 0;
@@ -403,7 +417,7 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
     v3<double> G = mk3(0.0, 0.0, 0.0);
     double sig = 0;
     if (near) {
-        const double* gp = (wake ? x.gam_w : x.gam_b) + 3 * size_t(s);
+        const double* gp = (wake ? mx.x[0].gam_w : mx.x[0].gam_b) + 3 * size_t(s);
         G = mk3(gp[0], gp[1], gp[2]);
         sig = wake ? 0.0 : S.sigma;
         v3<double> m = cross(nT, G) + sig * nT;
@@ -411,10 +425,8 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
         ns.m64[lane][1] = m.y;
         ns.m64[lane][2] = m.z;
     }
-    for (int k = 0; k < NSUM; ++k) {
-        ns.acc[lane][k] = 0.0;
-        ns.accf[lane][k] = 0.f;
-    }
+    for (int j = 0; j < ADJ_MAX; ++j)
+        for (int k = 0; k < NSUM; ++k) ns.accf[j][lane][k] = 0.f;
     const int nr = a.nrule[R_NEAR];
     int incl = near ? nleaf * nr : 0;
 #pragma unroll
@@ -428,16 +440,17 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
     const unsigned nearmask = __ballot_sync(FULL, near);
     __syncwarp();
     const float kf = float(a.kernel_far), areaT = float(T.area);
-    const float nu0 = float(pc.nu[0]), nu1 = float(pc.nu[1]), nu2 = float(pc.nu[2]);
+    float nuf[ADJ_MAX][3];
+    for (int j = 0; j < ADJ_MAX; ++j)
+        for (int c = 0; c < 3; ++c) nuf[j][c] = float(pc.nuk[j][c]);
     int nq = 0;
     unsigned long long n64 = 0;
     for (int i0 = 0; i0 < total; i0 += 32) {
         const int i = i0 + lane;
         const bool v = i < total;
         int p = 32 + lane, k = 0;
-        float vals[NSUM];
-#pragma unroll
-        for (int z = 0; z < NSUM; ++z) vals[z] = 0.f;
+        AdjSums<float> as[ADJ_MAX];
+        for (int j = 0; j < ADJ_MAX; ++j) adj_zero(as[j]);
         bool need = false;
         if (v) {
             int lo = 0, hi = 31;
@@ -460,38 +473,43 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
             float l1 = m.x * b[1] + m.y * b[4] + m.z * b[7];
             float l2 = m.x * b[2] + m.y * b[5] + m.z * b[8];
             float W = m.w * ldexpf(1.f, -2 * (code >> 6)) * areaT;
-            float Wn = W * (a.test_mode == 0 ? nu0 * l0 + nu1 * l1 + nu2 * l2 : nu0 + nu1 + nu2);
+            float Wn[ADJ_MAX];
+            for (int j = 0; j < ADJ_MAX; ++j)
+                Wn[j] = W * (a.test_mode == 0 ? nuf[j][0] * l0 + nuf[j][1] * l1 + nuf[j][2] * l2
+                                              : nuf[j][0] + nuf[j][1] + nuf[j][2]);
             const float* E = ns.pl.E32[p];
             const float* Dp = ns.pl.D32[p];
             const float* Sf = ns.pl.S32[p];
-            SrcKern<float> K;
+            SrcKern<float> Kf;
             for (int z = 0; z < 3; ++z) {
-                K.d[z] = mk3(Sf[3 * z], Sf[3 * z + 1], Sf[3 * z + 2]);
-                K.nu[z] = mk3(Sf[9 + 3 * z], Sf[10 + 3 * z], Sf[11 + 3 * z]);
-                K.len[z] = Sf[18 + z];
+                Kf.d[z] = mk3(Sf[3 * z], Sf[3 * z + 1], Sf[3 * z + 2]);
+                Kf.nu[z] = mk3(Sf[9 + 3 * z], Sf[10 + 3 * z], Sf[11 + 3 * z]);
+                Kf.len[z] = Sf[18 + z];
             }
-            K.n = mk3(Sf[21], Sf[22], Sf[23]);
-            K.area = Sf[24];
-            K.diam = Sf[25];
+            Kf.n = mk3(Sf[21], Sf[22], Sf[23]);
+            Kf.area = Sf[24];
+            Kf.diam = Sf[25];
             const v3<float> mf = mk3(float(ns.m64[p][0]), float(ns.m64[p][1]), float(ns.m64[p][2]));
             v3<float> r = l0 * mk3(Dp[0], Dp[1], Dp[2]) + l1 * mk3(Dp[3], Dp[4], Dp[5]) + l2 * mk3(Dp[6], Dp[7], Dp[8]);
-            AdjSums<float> as;
-            adj_zero(as);
-            float fd = kf * K.diam;
+            v3<float> gx;
+            float fd = kf * Kf.diam;
             if (dot(r, r) > fd * fd) {
-                adj_point_far(as, K, Wn, l0, l1, l2, r, mf);
+                adj_point_far_multi(as, K, Wn, Kf, l0, l1, l2, r, mf, gx);
             } else {
                 v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
                 v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
                 v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
-                if (fp32_guard_ok(K, ra, rb, rc, 0, Fp32Guard{ADJ_GUARD}))
-                    adj_point_exact(as, K, Wn, l0, l1, l2, ra, rb, rc, r, mf, 0, 1e-12f);
+                if (fp32_guard_ok(Kf, ra, rb, rc, 0, Fp32Guard{ADJ_GUARD}))
+                    adj_point_exact_multi(as, K, Wn, Kf, l0, l1, l2, ra, rb, rc, r, mf, 0, 1e-12f, gx);
                 else
                     need = true;
             }
-            if (!need) sums_flat(as, vals);
+            if (need)
+                for (int j = 0; j < ADJ_MAX; ++j) adj_zero(as[j]);
         }
-        if (a.mixed) seg_accumulate<NSUM>(ns.accf, ns.acc, lane, p, vals);
+        if (a.mixed)
+            for (int j = 0; j < K; ++j)
+                seg_accumulate<NSUM>(ns.accf[j], (double (*)[NSUM])nullptr, lane, p, reinterpret_cast<float*>(&as[j]));
         unsigned mq = __ballot_sync(FULL, need);
         if (mq) {
             int pos = nq + __popc(mq & ((1u << lane) - 1u));
@@ -505,15 +523,16 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
         while (nq >= 32 || (nq > 0 && i0 + 32 >= total)) {
             const int take = nq < 32 ? nq : 32;
             int qpair = 32 + lane;
-            double qv[NSUM];
-#pragma unroll
-            for (int z = 0; z < NSUM; ++z) qv[z] = 0.0;
+            float qv[ADJ_MAX][NSUM];
+            for (int j = 0; j < ADJ_MAX; ++j)
+                for (int z = 0; z < NSUM; ++z) qv[j][z] = 0.f;
             if (lane < take) {
                 qpair = ns.qp[lane];
                 const TriGeo& Sq = wake ? a.wtri[list[qpair]] : a.tri[list[qpair]];
-                adj_point64(a, T, Sq, ns, pc.nu, qpair, ns.qk[lane], qv);
+                adj_point64(a, T, Sq, ns, pc.nuk, K, qpair, ns.qk[lane], qv);
             }
-            seg_accumulate<NSUM>(ns.accf, ns.acc, lane, qpair, qv);
+            for (int j = 0; j < K; ++j)
+                seg_accumulate<NSUM>(ns.accf[j], (double (*)[NSUM])nullptr, lane, qpair, qv[j]);
             const int rest = nq - take;
             int mp = 0, mk = 0;
             if (lane < rest) {
@@ -531,23 +550,25 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
         }
     }
     __syncwarp();
-    // each lane finishes its own pair
+    // each lane finishes its own pair, for every vector
     if (near) {
-        double f[NSUM];
-        for (int z = 0; z < NSUM; ++z) f[z] = ns.acc[lane][z] + double(ns.accf[lane][z]);
-        const AdjSums<double> d = sums_unflat(f);
         const v3<double> m = mk3(ns.m64[lane][0], ns.m64[lane][1], ns.m64[lane][2]);
-        for (int k = 0; k < 3; ++k) Xg[k] += d.Xg[k];
-        U += cross(G, d.Q) + sig * d.Q;
-        fs += dot(d.Q, m);
         v3<double> xS[3];
         tri_corners(S, xS);
-        const SrcAdj<double> sa = src_of_pair(xS, d, m, nT);
-        double g[NSA];
-        sa_flat(sa, g);
-        double* dst = x.SA[wake ? 1 : 0] + size_t(s) * NSA;
-        for (int z = 0; z < NSA; ++z)
-            if (g[z] != 0.0) atomicAdd(dst + z, g[z]);
+        for (int j = 0; j < K; ++j) {
+            double f[NSUM];
+            for (int z = 0; z < NSUM; ++z) f[z] = double(ns.accf[j][lane][z]);
+            const AdjSums<double> d = sums_unflat(f);
+            for (int k = 0; k < 3; ++k) Xg[j][k] += d.Xg[k];
+            U[j] += cross(G, d.Q) + sig * d.Q;
+            fs[j] += dot(d.Q, m);
+            const SrcAdj<double> sa = src_of_pair(xS, d, m, nT);
+            double g[NSA];
+            sa_flat(sa, g);
+            double* dst = mx.x[j].SA[wake ? 1 : 0] + size_t(s) * NSA;
+            for (int z = 0; z < NSA; ++z)
+                if (g[z] != 0.0) atomicAdd(dst + z, g[z]);
+        }
     }
     __syncwarp();
     P[TIER_NEAR] += __popc(nearmask);
@@ -556,7 +577,7 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjExtra& x, in
     return __ballot_sync(FULL, valid && !near);
 }
 
-__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, AdjExtra x) {
+__global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, AdjMulti mx) {
     extern __shared__ __align__(16) unsigned char adj_smem[];
     AdjChunkSh& ns = reinterpret_cast<AdjChunkSh*>(adj_smem)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -564,15 +585,23 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, 
     if (idx >= a.ntests) return;
     const int t = a.tests[idx];
     const TriGeo& T = a.tri[t];
+    const int K = mx.nadj;
     PairCtx pc;
     pc.a = &a;
     pc.T = &T;
     pc.sh = nullptr;
     pc.lane = lane;
-    for (int k = 0; k < 3; ++k) pc.nu[k] = x.nu[T.slot[k]];
-    v3<double> Xg[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
-    v3<double> U = mk3(0.0, 0.0, 0.0);
-    double fs = 0;
+    for (int k = 0; k < 3; ++k) {
+        for (int j = 0; j < ADJ_MAX; ++j) pc.nuk[j][k] = j < K ? mx.x[j].nu[T.slot[k]] : 0.0;
+        pc.nu[k] = pc.nuk[0][k];
+    }
+    v3<double> Xg[ADJ_MAX][3], U[ADJ_MAX];
+    double fs[ADJ_MAX];
+    for (int j = 0; j < ADJ_MAX; ++j) {
+        for (int k = 0; k < 3; ++k) Xg[j][k] = mk3(0.0, 0.0, 0.0);
+        U[j] = mk3(0.0, 0.0, 0.0);
+        fs[j] = 0;
+    }
     unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
     for (int set = 0; set < 2; ++set) {
         const bool wake = set == 1;
@@ -583,21 +612,24 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, 
         int nrest = 0;
         for (long long c0 = e0; c0 < e1; c0 += 32) {
             const int cnt = int(e1 - c0 < 32 ? e1 - c0 : 32);
-            unsigned m = adj_chunk(pc, ns, x, t, src + c0, cnt, wake, Xg, U, fs, P, Q, Q64);
+            unsigned m = adj_chunk(pc, ns, mx, t, src + c0, cnt, wake, Xg, U, fs, P, Q, Q64);
             if ((m >> lane) & 1u) rest[e0 + nrest + __popc(m & ((1u << lane) - 1u))] = src[c0 + lane];
             nrest += __popc(m);
         }
         if (lane == 0) a.rest_cnt[2 * t + set] = nrest;
     }
-    // the test side, summed over the warp's pairs
-    double v[NTA] = {Xg[0].x, Xg[0].y, Xg[0].z, Xg[1].x, Xg[1].y, Xg[1].z, Xg[2].x, Xg[2].y, Xg[2].z, U.x, U.y, U.z, fs};
+    // the test side, summed over the warp's pairs, per vector
+    for (int j = 0; j < K; ++j) {
+        double v[NTA] = {Xg[j][0].x, Xg[j][0].y, Xg[j][0].z, Xg[j][1].x, Xg[j][1].y, Xg[j][1].z,
+                         Xg[j][2].x, Xg[j][2].y, Xg[j][2].z, U[j].x,     U[j].y,     U[j].z,     fs[j]};
 #pragma unroll
-    for (int k = 0; k < NTA; ++k) v[k] = warp_sum(v[k]);
-    double mine = 0;
+        for (int k = 0; k < NTA; ++k) v[k] = warp_sum(v[k]);
+        double mine = 0;
 #pragma unroll
-    for (int k = 0; k < NTA; ++k)
-        if (k == lane) mine = v[k];
-    if (lane < NTA && mine != 0.0) atomicAdd(x.TA + size_t(t) * NTA + lane, mine);
+        for (int k = 0; k < NTA; ++k)
+            if (k == lane) mine = v[k];
+        if (lane < NTA && mine != 0.0) atomicAdd(mx.x[j].TA + size_t(t) * NTA + lane, mine);
+    }
     for (int k = 0; k < 6; ++k) {
         unsigned long long pk = P[k], qk = Q[k];
         if (lane == 0 && pk) atomicAdd(a.stats + k, pk);
@@ -609,12 +641,6 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, 
 // ------------------------------------------------------------------------------------------------------------------
 // non-far pairs, tip filaments and freestream: one warp per test triangle
 
-
-// the adjoint vectors of one pass of the warp-cooperative kernel, each with its outputs
-struct AdjMulti {
-    AdjExtra x[ADJ_MAX];
-    int nadj;
-};
 
 // this lane's rule-geometry derivative (direction lane < 18) to the test triangle's nodes and the source's
 __device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjMulti& mx, const TriGeo& T, const TriGeo* S,
@@ -1109,7 +1135,7 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     const int ncols = ps.ncols;
     vp_phase_begin(ctx, PH_ADJOINT);
     double *d_mu, *d_gamb, *d_gamw;
-    unsigned long long *d_stats, *d_stats_x;
+    unsigned long long* d_stats;
     std::vector<double> hmu(mu, mu + ncols);
     std::vector<double> gamb(size_t(3) * ntri), gamw(size_t(3) * std::max(nwtri, 1), 0.0);
     for (int s = 0; s < ntri; ++s)
@@ -1125,10 +1151,9 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
             gamw[3 * size_t(s) + k] = v;
         }
     if ((r = dl.up(ctx, &d_mu, hmu)) || (r = dl.up(ctx, &d_gamb, gamb)) || (r = dl.up(ctx, &d_gamw, gamw)) ||
-        (r = dl.alloc(ctx, &d_stats, 13)) || (r = dl.alloc(ctx, &d_stats_x, 13)))
+        (r = dl.alloc(ctx, &d_stats, 13)))
         return r;
     VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(d_stats_x, 0, sizeof(unsigned long long) * 13, ctx->stream));
     // per adjoint vector: its values and outputs
     AdjMulti mx{};
     mx.nadj = nadj;
@@ -1195,11 +1220,8 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         VP_CUDA(ctx, cudaFuncSetAttribute(adj_lanes_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem)));
         const int nb = (ntri + NEAR_WARPS - 1) / NEAR_WARPS;
         vp_phase_begin(ctx, PH_ADJ_NEAR);
-        for (int k = 0; k < nadj; ++k) {
-            na.stats = k == 0 ? d_stats : d_stats_x;  // the pair counts once
-            adj_lanes_kernel<<<nb, 32 * NEAR_WARPS, smem, ctx->stream>>>(na, mx.x[k]);
-        }
         na.stats = d_stats;
+        adj_lanes_kernel<<<nb, 32 * NEAR_WARPS, smem, ctx->stream>>>(na, mx);  // every vector in one pass
         if ((r = rest_list(ctx, dl, na, nullptr))) return r;
         vp_phase_end(ctx);
         vp_phase_begin(ctx, PH_ADJ_PAIRS);
@@ -1217,7 +1239,7 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
         vp_phase_begin(ctx, PH_ADJ_NEAR);
         adj_near_kernel<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na, mx);
         vp_phase_end(ctx);
-        ctx->launches += nadj + 2;
+        ctx->launches += 3;
         VP_CUDA(ctx, cudaGetLastError());
     }
     vp_phase_begin(ctx, PH_ADJOINT);
