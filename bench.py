@@ -226,6 +226,58 @@ def freewake_bench(vp, ctx, steps=500):
                                     "source": "VortexPanel.jl README, free wake L2, 16 threads, author's CPU"}}
 
 
+BATCH_WINGS = ((28, 18, 4.0), (36, 22, 5.0), (44, 28, 6.0), (56, 32, 7.0), (64, 40, 8.0), (80, 44, 9.0),
+               (96, 50, 10.0), (112, 56, 12.0))
+
+
+def batch_bench(vp, ctx, reps=2):
+    """The uneven batch: 8 wings of 2,124 to 25,532 triangles, aspect ratios 4 to 12, each with its rigid wake, alpha
+    5 deg, mixed precision. One vp_assemble_batch call (far tier per colour over all wings, the touching and contact
+    pairs of all wings in one persistent launch) against the 8 wings assembled one after another; wall time of the
+    call (host classification included) and device time (CUDA events of the library's phases), the best of reps
+    after one warm-up. Throughput: pair integrals (test x source triangle pairs, wakes included) per second."""
+    a = math.radians(ALPHA)
+    V = np.array([math.cos(a), 0.0, math.sin(a)])
+    cases = []
+    for nc, ns, ar in BATCH_WINGS:
+        w = vp.meshes.wing(nc, ns, aspect=ar)
+        wake = vp.meshes.build_wake(w.g, w.dm, (1.0, 0.0, 0.0), length=2.5)
+        els = vp.build_elements(w.g)
+        cases.append((w.g, w.dm, vp.source_strengths(els, V), V, wake))
+    opts = vp.AssemblyOptions(precision="mixed")
+    pairs = sum(g.ntri * (g.ntri + len(wk.tris) + len(wk.filaments)) for g, _, _, _, wk in cases)
+
+    def run_batch():
+        out = vp.assemble_batch(cases, opts=opts, ctx=ctx)
+        del out
+
+    def run_single():
+        for g, dm, sig, VV, wk in cases:
+            A, b, _ = vp.assemble(g, dm, vp.build_elements(g), sig, VV, opts=opts, wake=wk, ctx=ctx)
+            del A
+
+    res = {}
+    for name, fn in (("batch", run_batch), ("one_by_one", run_single)):
+        fn()
+        best = None
+        for _ in range(reps):
+            ctx.phase_times(reset=True)
+            t0 = time.perf_counter()
+            fn()
+            wall = time.perf_counter() - t0
+            ph, launches = ctx.phase_times(reset=True)
+            dev = sum(ph.values()) / 1e3
+            if best is None or wall < best[0]:
+                best = (wall, dev, launches)
+        res[name] = {"wall_s": best[0], "device_s": best[1], "launches": best[2],
+                     "pairs_per_s_wall": pairs / best[0], "pairs_per_s_device": pairs / best[1]}
+    return {"workload": "8 wings AR 4-12, " + ", ".join(str(c[0].ntri) for c in cases) + " tris, rigid wakes, "
+                        "alpha 5 deg, mixed", "wings": len(cases), "tris": int(sum(c[0].ntri for c in cases)),
+            "pair_integrals": int(pairs), **res,
+            "speedup_wall": res["one_by_one"]["wall_s"] / res["batch"]["wall_s"],
+            "speedup_device": res["one_by_one"]["device_s"] / res["batch"]["device_s"]}
+
+
 def dist_setup(n_gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -297,6 +349,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--freewake-steps", type=int, default=500)
+    ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--workload", default="wing25k", choices=list(SIZES),
                     help="wing25k (the measured configuration); medium (56x28 per side) and small (28x14) for profiler captures")
     args = ap.parse_args()
@@ -396,6 +449,8 @@ def main():
     line["nbody"] = nbody(vp, ctx)
     if args.freewake_steps > 0:
         line["freewake"] = freewake_bench(vp, ctx, args.freewake_steps)
+    if not args.no_batch:
+        line["batch"] = batch_bench(vp, ctx)
     if not args.no_cpu_baseline:
         cb = cpu_step(w, wake, W, V)
         line["cpu_baseline"] = {"value": cb["value"], "unit": "s", "cores": cb["cores"], "kind": "port",

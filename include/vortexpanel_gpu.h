@@ -82,6 +82,42 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
                 const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
                 const int* fil, vp_system** out, vp_assembly_stats* stats);
 
+/* Test triangles per tile of the far tier's kernel (the tile each CTA holds in shared memory against a 128-source
+ * tile), per precision: 2 or 4 in VP_FP64 (default 4), 4 or 8 in VP_MIXED (default 8). The autotuner
+ * (vortexpanel_gpu/autotune.py) picks it per mesh size from a measured sweep. No counterpart in the reference. */
+int vp_set_far_tile(vp_ctx* ctx, int precision, int tile);
+/* The current far tile of a precision (0 for a bad argument). */
+int vp_get_far_tile(const vp_ctx* ctx, int precision);
+
+/* One system of a batch: the arguments of vp_assemble for one body with its wake. */
+typedef struct {
+    int nnode;
+    const double* x;
+    int ntri;
+    const int* tris;
+    const int* corner_slot;
+    int nslot;
+    int ntouch;
+    const int* touch_pairs;
+    const double* sigma;
+    const double* vinf;
+    int nwnode;
+    const double* wx;
+    int nwtri;
+    const int* wtris;
+    int nfil;
+    const int* fil;
+} vp_assembly_input;
+
+/* assemble (src/assembly/assemble.jl:377-447) of nsys independent systems of uneven sizes in shared launches: the far
+ * tier one launch per colour of test tiles over every system, the near tier's lanes and the rest kernels one launch
+ * per colour of test triangles over every system, and the self, touching and contact pairs of all of them in one
+ * persistent launch. Every system's A and b are those vp_assemble gives it, bit for bit. One options set and
+ * precision for the whole batch. out[k] receives system k; stats (nsys entries) may be NULL. No counterpart in the
+ * reference, which assembles one body at a time. */
+int vp_assemble_batch(vp_ctx* ctx, const vp_assembly_options* opts, int nsys, const vp_assembly_input* in,
+                      vp_system** out, vp_assembly_stats* stats);
+
 /* Rows and columns of the assembled A. */
 int vp_system_shape(const vp_system* sys, int* nrows, int* ncols);
 /* Copy A (row-major, nrows x ncols) and/or b (nrows) to the host; either pointer may be NULL. */

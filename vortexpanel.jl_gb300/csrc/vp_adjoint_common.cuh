@@ -8,6 +8,9 @@
 // Sums over a pair's points of W nu(q) times: w (Q); lambda_k ds/dx (Xg); ds/dr_a at fixed shape (Gr, exact form);
 // the edge logs (L), dL_e/dlen_e (N) and the solid angle (O) of the exact form; ds/dr (Grf), ds/dd_a (Gd) and
 // ds/darea (A) of the multipole form.
+// adjoint vectors one pass carries at most (the loops over them unroll, so that per-vector sums stay in registers)
+constexpr int ADJ_VEC_MAX = 2;
+
 template <class T>
 struct AdjSums {
     v3<T> Q, Xg[3], Gr[3], Grf, Gd[3];
@@ -80,7 +83,9 @@ __device__ __forceinline__ T adj_point_far(AdjSums<T>& acc, const SrcKern<T>& S,
 template <class T>
 __device__ __forceinline__ void adj_acc_exact(AdjSums<T>* acc, int nk, const T* Wn, T l0, T l1, T l2, v3<T> w,
                                               v3<T> gx, v3<T> g0, v3<T> g1, v3<T> g2, const T* L, const T* dL, T Om) {
-    for (int k = 0; k < nk; ++k) {
+#pragma unroll
+    for (int k = 0; k < ADJ_VEC_MAX; ++k) {
+        if (k >= nk) break;
         AdjSums<T>& a = acc[k];
         const T wn = Wn[k];
         a.Q += wn * w;
@@ -102,7 +107,9 @@ __device__ __forceinline__ void adj_acc_exact(AdjSums<T>* acc, int nk, const T* 
 template <class T>
 __device__ __forceinline__ void adj_acc_far(AdjSums<T>* acc, int nk, const T* Wn, T l0, T l1, T l2, v3<T> w, v3<T> gx,
                                             const v3<T>* gd, T ga) {
-    for (int k = 0; k < nk; ++k) {
+#pragma unroll
+    for (int k = 0; k < ADJ_VEC_MAX; ++k) {
+        if (k >= nk) break;
         AdjSums<T>& a = acc[k];
         const T wn = Wn[k];
         a.Q += wn * w;

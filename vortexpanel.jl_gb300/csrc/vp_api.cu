@@ -7,6 +7,8 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
                      const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                      const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
                      const int* fil, vp_system** out, vp_assembly_stats* stats, int body_sources);
+int vp_assemble_batch_impl(vp_ctx* ctx, const vp_assembly_options* o, int nsys, const vp_assembly_input* in,
+                           vp_system** out, vp_assembly_stats* stats);
 int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const double* x, int ntri, const int* tris,
                     const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                     const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
@@ -142,6 +144,27 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
     if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
     return vp_assemble_impl(ctx, opts, nnode, x, ntri, tris, corner_slot, nslot, ntouch, touch_pairs, sigma, vinf,
                             nwnode, wx, nwtri, wtris, nfil, fil, out, stats, 1);
+}
+
+int vp_set_far_tile(vp_ctx* ctx, int precision, int tile) {
+    if (!ctx) return VP_ERR_ARG;
+    if (precision != VP_FP64 && precision != VP_MIXED) return vp_fail(ctx, VP_ERR_ARG, "unknown precision");
+    const bool ok = precision == VP_MIXED ? (tile == 4 || tile == 8) : (tile == 2 || tile == 4);
+    if (!ok) return vp_fail(ctx, VP_ERR_ARG, "far tile: 2 or 4 test triangles in FP64, 4 or 8 in mixed precision");
+    ctx->far_tile[precision] = tile;
+    return VP_OK;
+}
+
+int vp_get_far_tile(const vp_ctx* ctx, int precision) {
+    if (!ctx || (precision != VP_FP64 && precision != VP_MIXED)) return 0;
+    return ctx->far_tile[precision];
+}
+
+int vp_assemble_batch(vp_ctx* ctx, const vp_assembly_options* opts, int nsys, const vp_assembly_input* in,
+                      vp_system** out, vp_assembly_stats* stats) {
+    if (!ctx) return VP_ERR_ARG;
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
+    return vp_assemble_batch_impl(ctx, opts, nsys, in, out, stats);
 }
 
 int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,

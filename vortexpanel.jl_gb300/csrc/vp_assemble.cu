@@ -21,6 +21,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <unordered_map>
 
@@ -31,7 +32,7 @@ namespace {
 // ------------------------------------------------------------------------------------------------------------------
 // device: the far tier
 template <class T, int TT>
-__global__ void __launch_bounds__(FAR_NT) far_kernel(FarArgs a) {
+__device__ __forceinline__ void far_body(const FarArgs& a, const int tile) {
     __shared__ FarTest<T> ts[TT];
     __shared__ T blk[TT][FAR_NT][9];
     __shared__ T rbsum[TT * 3][FAR_NT / 32];
@@ -43,7 +44,6 @@ __global__ void __launch_bounds__(FAR_NT) far_kernel(FarArgs a) {
     __shared__ short s_rent[3 * TT];
     __shared__ int s_ncol, s_nrow;
 
-    const int tile = a.tiles[blockIdx.x];
     const int tid = threadIdx.x;
     // the test tile
     for (int i = tid; i < TT; i += FAR_NT) {
@@ -200,6 +200,20 @@ __global__ void __launch_bounds__(FAR_NT) far_kernel(FarArgs a) {
     }
 }
 
+// one system: block b takes test tile a.tiles[b]
+template <class T, int TT>
+__global__ void __launch_bounds__(FAR_NT) far_kernel(FarArgs a) {
+    far_body<T, TT>(a, a.tiles[blockIdx.x]);
+}
+
+// a batch of systems in one launch: block b takes test tile work[b].y of system work[b].x
+template <class T, int TT>
+__global__ void __launch_bounds__(FAR_NT) far_kernel_batch(const FarArgs* __restrict__ sys,
+                                                          const int2* __restrict__ work) {
+    const int2 wk = work[blockIdx.x];
+    far_body<T, TT>(sys[wk.x], wk.y);
+}
+
 // ---- the near tier, one pair per lane ---------------------------------------------------------------------------
 // A warp takes up to 32 sources of its test triangle at once. Each lane decides its own pair's tier (FP64, exactly as
 // pair_rule / wake_pair_rule) and, for a pair in the near tier, walks near_pieces' quadtree to its leaves. The
@@ -290,7 +304,7 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
     __syncwarp();
     // 3. every leaf point of the chunk, one per lane
     const float kf = float(a.kernel_far), areaT = float(T.area);
-    const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+    const Fp32Guard g{PAIR_GUARD};
     int nq = 0;
     unsigned long long n64 = 0;
     for (int i0 = 0; i0 < total; i0 += 32) {
@@ -436,14 +450,9 @@ __device__ unsigned near_chunk(PairCtx& pc, NearChunkSh& ns, int t, const int* l
     return __ballot_sync(FULL, valid && !near);
 }
 
-// near tier, one pair per lane; the other pairs are listed for near_kernel_pairs
-__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a) {
-    extern __shared__ __align__(16) unsigned char near_smem[];
-    NearChunkSh* shm = reinterpret_cast<NearChunkSh*>(near_smem);
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int idx = blockIdx.x * NEAR_WARPS + w;
-    if (idx >= a.ntests) return;
-    const int t = a.tests[idx];
+// near tier, one pair per lane; the other pairs are listed for near_kernel_pairs. One warp, test triangle t.
+__device__ __forceinline__ void near_lanes_body(const NearArgs& a, const int t, NearChunkSh& sh) {
+    const int lane = threadIdx.x & 31;
     const TriGeo& T = a.tri[t];
     PairCtx pc;
     pc.a = &a;
@@ -461,7 +470,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a)
         int nrest = 0;
         for (long long c0 = e0; c0 < e1; c0 += 32) {
             const int cnt = int(e1 - c0 < 32 ? e1 - c0 : 32);
-            unsigned m = near_chunk(pc, shm[w], t, src + c0, cnt, wake, col0, rbt, P, Q, Q64);
+            unsigned m = near_chunk(pc, sh, t, src + c0, cnt, wake, col0, rbt, P, Q, Q64);
             if ((m >> lane) & 1u) rest[e0 + nrest + __popc(m & ((1u << lane) - 1u))] = src[c0 + lane];
             nrest += __popc(m);
             __syncwarp();
@@ -476,6 +485,25 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a)
         }
         if (Q64) atomicAdd(a.stats + 12, Q64);
     }
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes(NearArgs a) {
+    extern __shared__ __align__(16) unsigned char near_smem[];
+    NearChunkSh* shm = reinterpret_cast<NearChunkSh*>(near_smem);
+    const int idx = blockIdx.x * NEAR_WARPS + (threadIdx.x >> 5);
+    if (idx >= a.ntests) return;
+    near_lanes_body(a, a.tests[idx], shm[threadIdx.x >> 5]);
+}
+
+// a batch of systems: warp i takes test triangle work[i].y of system work[i].x
+__global__ void __launch_bounds__(32 * NEAR_WARPS) near_kernel_lanes_batch(const NearArgs* __restrict__ sys,
+                                                                        const int2* __restrict__ work, int nwork) {
+    extern __shared__ __align__(16) unsigned char near_smem[];
+    NearChunkSh* shm = reinterpret_cast<NearChunkSh*>(near_smem);
+    const int idx = blockIdx.x * NEAR_WARPS + (threadIdx.x >> 5);
+    if (idx >= nwork) return;
+    const int2 wk = work[idx];
+    near_lanes_body(sys[wk.x], wk.y, shm[threadIdx.x >> 5]);
 }
 
 // the block of one pair: the per-lane sums reduced and contracted with n_T x gamma_b (9 values, row-major), and the
@@ -504,19 +532,12 @@ __device__ void pair_block_out(PairCtx& pc, FwdAcc& acc, const TriGeo& S, double
 // the self, touching and contact pairs, one warp per pair: a persistent grid whose warps take the next pair of the
 // list from a counter, so that test triangles with many contact pairs (thin panels at a sharp trailing edge) do not
 // hold a launch; the blocks go to pair_out and near_kernel_rest adds them in the list's order
-__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_pairs(NearArgs a) {
-    __shared__ WarpSh shm[NEAR_WARPS];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n = 2 * a.ntri;
-    const long long total = a.rest_off[n];
-    PairCtx pc;
-    pc.a = &a;
-    pc.sh = &shm[w];
-    pc.lane = lane;
-    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
-    for (;;) {
-        const long long idx = next_rest_pair(a.next, lane);
-        if (idx >= total) break;
+// rest pair idx of system a: its block to a.pair_out, its tier and points counted in P, Q, Q64
+__device__ __forceinline__ void near_pair_item(const NearArgs& a, PairCtx& pc, const long long idx,
+                                               unsigned long long* P, unsigned long long* Q,
+                                               unsigned long long& Q64) {
+        const int lane = pc.lane;
+        const int n = 2 * a.ntri;
         const int g = rest_entry(a.rest_off, n, idx);
         const int t = g >> 1;
         const bool wake = (g & 1) != 0;
@@ -534,6 +555,22 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_pairs(NearArgs
         P[tier] += 1;
         Q[tier] += pc.npts;
         Q64 += pc.n64;
+        (void)lane;
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_pairs(NearArgs a) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long total = a.rest_off[2 * a.ntri];
+    PairCtx pc;
+    pc.a = &a;
+    pc.sh = &shm[w];
+    pc.lane = lane;
+    unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+    for (;;) {
+        const long long idx = next_rest_pair(a.next, lane);
+        if (idx >= total) break;
+        near_pair_item(a, pc, idx, P, Q, Q64);
     }
     if (lane == 0) {
         for (int k = 0; k < 6; ++k) {
@@ -541,6 +578,40 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_pairs(NearArgs
             if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
         }
         if (Q64) atomicAdd(a.stats + 12, Q64);
+    }
+}
+
+// a batch of systems in one persistent launch: the systems' rest pairs in one index space (system k's pairs at
+// base[k] .. base[k + 1]), taken from one counter; each pair's counts go to its own system's statistics
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_pairs_batch(const NearArgs* __restrict__ sys, int nsys,
+                                                                           const long long* __restrict__ base,
+                                                                           unsigned long long* next) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long total = base[nsys];
+    PairCtx pc;
+    pc.sh = &shm[w];
+    pc.lane = lane;
+    for (;;) {
+        const long long idx = next_rest_pair(next, lane);
+        if (idx >= total) break;
+        int lo = 0, hi = nsys - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (base[mid] <= idx) lo = mid;
+            else hi = mid - 1;
+        }
+        const NearArgs& a = sys[lo];
+        pc.a = &a;
+        unsigned long long P[6] = {0, 0, 0, 0, 0, 0}, Q[6] = {0, 0, 0, 0, 0, 0}, Q64 = 0;
+        near_pair_item(a, pc, idx - base[lo], P, Q, Q64);
+        if (lane == 0) {
+            for (int k = 0; k < 6; ++k) {
+                if (P[k]) atomicAdd(a.stats + k, P[k]);
+                if (Q[k]) atomicAdd(a.stats + 6 + k, Q[k]);
+            }
+            if (Q64) atomicAdd(a.stats + 12, Q64);
+        }
     }
 }
 
@@ -575,17 +646,13 @@ __device__ void far_filament_fwd(const NearArgs& a, const TriGeo& T, v3<double> 
 
 // the blocks of the self, touching and contact pairs (from near_kernel_pairs, added in the order of the test
 // triangle's list), the tip filaments and the freestream: one warp per test triangle, a launch per colour
-__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_rest(NearArgs a) {
-    __shared__ WarpSh shm[NEAR_WARPS];
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int idx = blockIdx.x * NEAR_WARPS + w;
-    if (idx >= a.ntests) return;
-    const int t = a.tests[idx];
+__device__ __forceinline__ void near_rest_body(const NearArgs& a, const int t, WarpSh& wsh) {
+    const int lane = threadIdx.x & 31;
     const TriGeo& T = a.tri[t];
     PairCtx pc;
     pc.a = &a;
     pc.T = &T;
-    pc.sh = &shm[w];
+    pc.sh = &wsh;
     pc.lane = lane;
     pc.nleaf = 0;
     pc.nq64 = 0;
@@ -707,13 +774,31 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_rest(NearArgs 
     }
 }
 
-// ------------------------------------------------------------------------------------------------------------------
-// host: the far launches
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_rest(NearArgs a) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int idx = blockIdx.x * NEAR_WARPS + (threadIdx.x >> 5);
+    if (idx >= a.ntests) return;
+    near_rest_body(a, a.tests[idx], shm[threadIdx.x >> 5]);
+}
 
-template <class T, int TT>
-int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::vector<int>& cslot, int nslot,
-            DevList& dl) {
-    int nt = (int)tg.size();
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 3) near_kernel_rest_batch(const NearArgs* __restrict__ sys,
+                                                                          const int2* __restrict__ work, int nwork) {
+    __shared__ WarpSh shm[NEAR_WARPS];
+    const int idx = blockIdx.x * NEAR_WARPS + (threadIdx.x >> 5);
+    if (idx >= nwork) return;
+    const int2 wk = work[idx];
+    near_rest_body(sys[wk.x], wk.y, shm[threadIdx.x >> 5]);
+}
+
+// ------------------------------------------------------------------------------------------------------------------
+// host: one system's assembly, prepared (classification, pair lists, far tiles and their colours, near colours) and
+// then launched; a batch prepares every system and launches each phase once over all of them
+
+// the far tier's test tiles of TT triangles: their unique row slots, uploaded; the tiles grouped by colour (no two
+// tiles of a colour share a row slot)
+template <int TT>
+int far_prepare(vp_ctx* ctx, FarArgs& fa, int nt, const int* cslot, int nslot, DevList& dl,
+                std::vector<std::vector<int>>& colours) {
     int ntiles = (nt + TT - 1) / TT;
     std::vector<int> trow(size_t(ntiles) * 3 * TT), tnrow(ntiles);
     std::vector<short> trptr(size_t(ntiles) * (3 * TT + 1)), trent(size_t(ntiles) * 3 * TT);
@@ -729,7 +814,7 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
                    &trent[size_t(k) * 3 * TT]);
         for (int j = 0; j < tnrow[k]; ++j) groups[k].push_back(trow[size_t(k) * 3 * TT + j]);
     }
-    auto colours = colour_groups(groups, nslot);
+    colours = colour_groups(groups, nslot);
     int *d_trow, *d_tnrow;
     short *d_trptr, *d_trent;
     int r;
@@ -740,16 +825,167 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
     fa.tnrow = d_tnrow;
     fa.trptr = d_trptr;
     fa.trent = d_trent;
+    return VP_OK;
+}
+
+// one system of an assembly between its phases
+struct AsmJob {
+    PairInput in;
+    int tt = 8;  // test triangles per far tile
+    PairSetup ps;
+    vp_system* sys = nullptr;
+    FarArgs fa{};
+    std::vector<std::vector<int>> far_col;   // far test tiles, per colour
+    std::vector<std::vector<int>> near_col;  // test triangles, per colour
+    NearArgs na{};
+    unsigned long long* d_stats = nullptr;
+    long long nrest = 0;
+    std::chrono::steady_clock::time_point t0;
+    ~AsmJob() {
+        if (sys) vp_system_free(sys);
+    }
+};
+
+// classification, pair lists, the zeroed system, the far tier's source tiles and arrays, its test tiles and their
+// colours, the near tier's colours and arguments
+int job_prepare(vp_ctx* ctx, AsmJob& j) {
+    j.t0 = std::chrono::steady_clock::now();
+    const PairInput& in = j.in;
+    const vp_assembly_options* o = in.o;
+    int r = setup_pairs(ctx, in, PH_SETUP, PH_CLASSIFY, j.ps);
+    if (r) return r;
+    PairSetup& ps = j.ps;
+    DevList& dl = ps.dl;
+    const int ntri = in.ntri, nslot = in.nslot, nwtri = in.nwtri, ncols = ps.ncols;
+    vp_system* sys = new vp_system();
+    j.sys = sys;
+    sys->nslot = nslot;
+    sys->ncols = ncols;
+    sys->nwnode = in.nwnode;
+    if ((r = vp_alloc(ctx, &sys->A, size_t(nslot) * ncols)) || (r = vp_alloc(ctx, &sys->b, size_t(nslot)))) return r;
+    VP_CUDA(ctx, cudaMemsetAsync(sys->A, 0, sizeof(double) * size_t(nslot) * ncols, ctx->stream));
+    VP_CUDA(ctx, cudaMemsetAsync(sys->b, 0, sizeof(double) * nslot, ctx->stream));
+    // far tier
+    FarArgs& fa = j.fa;
+    fa.ntest = ntri;
+    fa.nq = ps.nq;
+    fa.test_mode = o->test;
+    fa.tq = ps.d_tq;
+    fa.tw = ps.d_tw;
+    fa.tgeo = ps.d_tg;
+    fa.tcent = ps.d_tc;
+    fa.nset = nwtri > 0 ? 2 : 1;
+    fa.A = sys->A;
+    fa.lda = ncols;
+    fa.b = sys->b;
+    fa.ratio32 = ps.ratio32;
+    fa.ratio = o->far_ratio;
+    fa.kernel_far = o->kernel_far;
+    const std::vector<TriGeo>* sets[2] = {&ps.tg, &ps.wg};
+    int nsrc[2] = {in.body_sources ? ntri : 0, nwtri};
+    for (int set = 0; set < fa.nset; ++set) {
+        std::vector<TriGeo> g(sets[set]->begin(), sets[set]->begin() + nsrc[set]);
+        SrcTiles st = make_src_tiles(g);
+        int *d_cols, *d_ncol;
+        short *d_cptr, *d_cent;
+        if ((r = dl.up(ctx, &d_cols, st.cols)) || (r = dl.up(ctx, &d_ncol, st.ncol)) ||
+            (r = dl.up(ctx, &d_cptr, st.cptr)) || (r = dl.up(ctx, &d_cent, st.cent)))
+            return r;
+        fa.nsrc[set] = nsrc[set];
+        fa.ntile[set] = st.ntile;
+        fa.col_off[set] = set == 0 ? 0 : nslot;
+        fa.scent[set] = set == 0 ? ps.d_tc : ps.d_wc;
+        fa.sgeo[set] = set == 0 ? ps.d_tg : ps.d_wg;
+        fa.tile_cols[set] = d_cols;
+        fa.tile_ncol[set] = d_ncol;
+        fa.tile_cptr[set] = d_cptr;
+        fa.tile_cent[set] = d_cent;
+        if (ps.mixed) {
+            std::vector<float> soa;
+            float* d;
+            fill_soa(g, soa, fa.pad[set]);
+            if ((r = dl.up(ctx, &d, soa))) return r;
+            fa.soa[set] = d;
+        } else {
+            std::vector<double> soa;
+            double* d;
+            fill_soa(g, soa, fa.pad[set]);
+            if ((r = dl.up(ctx, &d, soa))) return r;
+            fa.soa[set] = d;
+        }
+    }
+    j.tt = ctx->far_tile[ps.mixed ? 1 : 0];
+    switch (j.tt) {
+        case 2: r = far_prepare<2>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
+        case 4: r = far_prepare<4>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
+        case 8: r = far_prepare<8>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
+        default: return vp_fail(ctx, VP_ERR_ARG, "far tile must be 2, 4 or 8 test triangles");
+    }
+    if (r) return r;
+    // near, touching and contact tiers
+    if ((r = dl.alloc(ctx, &j.d_stats, 13))) return r;
+    VP_CUDA(ctx, cudaMemsetAsync(j.d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
+    std::vector<std::vector<int>> groups(ntri);
+    for (int t = 0; t < ntri; ++t)
+        groups[t] = {in.corner_slot[3 * t], in.corner_slot[3 * t + 1], in.corner_slot[3 * t + 2]};
+    j.near_col = colour_groups(groups, nslot);
+    j.na = near_args(ps, in);
+    j.na.A = sys->A;
+    j.na.b = sys->b;
+    j.na.stats = j.d_stats;
+    int *d_rest, *d_wrest, *d_rcnt;
+    if ((r = dl.alloc(ctx, &d_rest, size_t(std::max(ps.nfptr[ntri], 1LL)))) ||
+        (r = dl.alloc(ctx, &d_wrest, size_t(std::max(ps.wfptr[ntri], 1LL)))) ||
+        (r = dl.alloc(ctx, &d_rcnt, size_t(2) * ntri)))
+        return r;
+    j.na.rest_src = d_rest;
+    j.na.wrest_src = d_wrest;
+    j.na.rest_cnt = d_rcnt;
+    return VP_OK;
+}
+
+// the statistics and the system of a finished job (the stream is synchronised)
+int job_finish(vp_ctx* ctx, AsmJob& j, vp_system** out, vp_assembly_stats* stats) {
+    unsigned long long hs[13];
+    VP_CUDA(ctx, vp_d2h(ctx, hs, j.d_stats, sizeof(hs)));
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("assembly kernels: ") + cudaGetErrorString(e));
+    if (stats) {
+        const PairInput& in = j.in;
+        long long total = (long long)in.ntri * (in.ntri + in.nwtri) + (long long)in.ntri * in.nfil;
+        long long nonfar = 0;
+        for (int k = 0; k < 6; ++k) {
+            stats->pairs[k] = (long long)hs[k];
+            stats->points[k] = (long long)hs[6 + k];
+            if (k != TIER_FAR) nonfar += (long long)hs[k];
+        }
+        long long far_fil = (long long)hs[TIER_FAR];
+        long long far_tri = total - nonfar - far_fil;
+        stats->pairs[TIER_FAR] = far_tri + far_fil;
+        stats->points[TIER_FAR] = (long long)hs[6 + TIER_FAR] + far_tri * j.ps.nq;
+        stats->points_fp64 = (long long)hs[12] + (j.ps.mixed ? 0 : far_tri * j.ps.nq);
+        stats->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - j.t0).count();
+    }
+    *out = j.sys;
+    j.sys = nullptr;
+    return VP_OK;
+}
+
+// one system: the far tiles of a colour per launch
+template <class T, int TT>
+int far_launch(vp_ctx* ctx, AsmJob& j) {
     std::vector<int> all;
     std::vector<int> off{0};
-    for (auto& c : colours) {
+    for (auto& c : j.far_col) {
         all.insert(all.end(), c.begin(), c.end());
         off.push_back((int)all.size());
     }
     int* d_tiles;
-    if ((r = dl.up(ctx, &d_tiles, all))) return r;
+    int r;
+    if ((r = j.ps.dl.up(ctx, &d_tiles, all))) return r;
+    FarArgs fa = j.fa;
     vp_phase_begin(ctx, PH_FAR);
-    for (size_t c = 0; c < colours.size(); ++c) {
+    for (size_t c = 0; c < j.far_col.size(); ++c) {
         fa.tiles = d_tiles + off[c];
         int nb = off[c + 1] - off[c];
         if (nb) {
@@ -762,6 +998,186 @@ int run_far(vp_ctx* ctx, FarArgs fa, const std::vector<TriGeo>& tg, const std::v
     return VP_OK;
 }
 
+// a batch: colour c's far tiles of every system in one launch
+template <class T, int TT>
+int far_launch_batch(vp_ctx* ctx, std::vector<std::unique_ptr<AsmJob>>& jobs, DevList& dl) {
+    std::vector<FarArgs> args;
+    size_t ncol = 0;
+    for (auto& j : jobs) {
+        args.push_back(j->fa);
+        ncol = std::max(ncol, j->far_col.size());
+    }
+    FarArgs* d_args;
+    int r;
+    if ((r = dl.up(ctx, &d_args, args))) return r;
+    vp_phase_begin(ctx, PH_FAR);
+    for (size_t c = 0; c < ncol; ++c) {
+        std::vector<int2> work;
+        for (size_t k = 0; k < jobs.size(); ++k)
+            if (c < jobs[k]->far_col.size())
+                for (int tile : jobs[k]->far_col[c]) work.push_back(make_int2(int(k), tile));
+        if (work.empty()) continue;
+        int2* d_work;
+        if ((r = dl.up(ctx, &d_work, work))) return r;
+        far_kernel_batch<T, TT><<<int(work.size()), FAR_NT, 0, ctx->stream>>>(d_args, d_work);
+        ctx->launches++;
+    }
+    vp_phase_end(ctx);
+    VP_CUDA(ctx, cudaGetLastError());
+    return VP_OK;
+}
+
+// one system: the near tier's lanes per colour, the rest pairs' list, the persistent pair kernel, the rest per colour
+int near_launch(vp_ctx* ctx, AsmJob& j) {
+    DevList& dl = j.ps.dl;
+    NearArgs& na = j.na;
+    std::vector<int> all;
+    std::vector<int> off{0};
+    for (auto& c : j.near_col) {
+        all.insert(all.end(), c.begin(), c.end());
+        off.push_back((int)all.size());
+    }
+    int* d_tests;
+    int r;
+    if ((r = dl.up(ctx, &d_tests, all))) return r;
+    vp_phase_begin(ctx, PH_NEAR);
+    const size_t near_smem = sizeof(NearChunkSh) * NEAR_WARPS;
+    VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, int(near_smem)));
+    for (int pass = 0; pass < 2; ++pass) {
+        if (pass == 1) {
+            // the rest pairs as one list, evaluated pair-parallel into per-pair blocks
+            long long nrest = 0;
+            double* d_pairs;
+            if ((r = rest_list(ctx, dl, na, &nrest)) ||
+                (r = dl.alloc(ctx, &d_pairs, size_t(12) * size_t(std::max(nrest, 1LL)))))
+                return r;
+            na.pair_out = d_pairs;
+            if (nrest > 0) {
+                const int nb = persistent_blocks(ctx, near_kernel_pairs, 32 * NEAR_WARPS, 0);
+                vp_phase_end(ctx);
+                vp_phase_begin(ctx, PH_NEAR_PAIRS);
+                near_kernel_pairs<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+                vp_phase_end(ctx);
+                vp_phase_begin(ctx, PH_NEAR);
+                ctx->launches++;
+            }
+        }
+        for (size_t c = 0; c < j.near_col.size(); ++c) {
+            na.tests = d_tests + off[c];
+            na.ntests = off[c + 1] - off[c];
+            int nb = (na.ntests + NEAR_WARPS - 1) / NEAR_WARPS;
+            if (!nb) continue;
+            if (pass == 0)
+                near_kernel_lanes<<<nb, 32 * NEAR_WARPS, near_smem, ctx->stream>>>(na);
+            else
+                near_kernel_rest<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
+            ctx->launches++;
+        }
+    }
+    vp_phase_end(ctx);
+    VP_CUDA(ctx, cudaGetLastError());
+    return VP_OK;
+}
+
+// a batch: the lanes kernel per colour over every system, every system's rest list, one persistent launch of the
+// pair kernel over all of them, the rest kernel per colour over every system
+int near_launch_batch(vp_ctx* ctx, std::vector<std::unique_ptr<AsmJob>>& jobs, DevList& dl) {
+    int r;
+    const int nsys = int(jobs.size());
+    size_t ncol = 0;
+    for (auto& j : jobs) ncol = std::max(ncol, j->near_col.size());
+    auto colour_work = [&](size_t c) {
+        std::vector<int2> work;
+        for (int k = 0; k < nsys; ++k)
+            if (c < jobs[k]->near_col.size())
+                for (int t : jobs[k]->near_col[c]) work.push_back(make_int2(k, t));
+        return work;
+    };
+    auto upload_args = [&](NearArgs** d) {
+        std::vector<NearArgs> args;
+        for (auto& j : jobs) args.push_back(j->na);
+        return dl.up(ctx, d, args);
+    };
+    NearArgs* d_args;
+    if ((r = upload_args(&d_args))) return r;
+    vp_phase_begin(ctx, PH_NEAR);
+    const size_t near_smem = sizeof(NearChunkSh) * NEAR_WARPS;
+    VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel_lanes_batch, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      int(near_smem)));
+    for (size_t c = 0; c < ncol; ++c) {
+        std::vector<int2> work = colour_work(c);
+        if (work.empty()) continue;
+        int2* d_work;
+        if ((r = dl.up(ctx, &d_work, work))) return r;
+        const int n = int(work.size());
+        near_kernel_lanes_batch<<<(n + NEAR_WARPS - 1) / NEAR_WARPS, 32 * NEAR_WARPS, near_smem, ctx->stream>>>(
+            d_args, d_work, n);
+        ctx->launches++;
+    }
+    // every system's rest list and block buffer; their pairs in one index space
+    std::vector<long long> base{0};
+    for (auto& j : jobs) {
+        if ((r = rest_list(ctx, j->ps.dl, j->na, &j->nrest))) return r;
+        double* d_pairs;
+        if ((r = j->ps.dl.alloc(ctx, &d_pairs, size_t(12) * size_t(std::max(j->nrest, 1LL))))) return r;
+        j->na.pair_out = d_pairs;
+        base.push_back(base.back() + j->nrest);
+    }
+    if ((r = upload_args(&d_args))) return r;
+    if (base.back() > 0) {
+        long long* d_base;
+        unsigned long long* d_next;
+        if ((r = dl.up(ctx, &d_base, base)) || (r = dl.alloc(ctx, &d_next, 1))) return r;
+        VP_CUDA(ctx, cudaMemsetAsync(d_next, 0, sizeof(unsigned long long), ctx->stream));
+        const int nb = persistent_blocks(ctx, near_kernel_pairs_batch, 32 * NEAR_WARPS, 0);
+        vp_phase_end(ctx);
+        vp_phase_begin(ctx, PH_NEAR_PAIRS);
+        near_kernel_pairs_batch<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(d_args, nsys, d_base, d_next);
+        vp_phase_end(ctx);
+        vp_phase_begin(ctx, PH_NEAR);
+        ctx->launches++;
+    }
+    for (size_t c = 0; c < ncol; ++c) {
+        std::vector<int2> work = colour_work(c);
+        if (work.empty()) continue;
+        int2* d_work;
+        if ((r = dl.up(ctx, &d_work, work))) return r;
+        const int n = int(work.size());
+        near_kernel_rest_batch<<<(n + NEAR_WARPS - 1) / NEAR_WARPS, 32 * NEAR_WARPS, 0, ctx->stream>>>(d_args, d_work,
+                                                                                                      n);
+        ctx->launches++;
+    }
+    vp_phase_end(ctx);
+    VP_CUDA(ctx, cudaGetLastError());
+    return VP_OK;
+}
+
+// the far launches of the job's precision and tile (FP64: 2 or 4 test triangles per tile, mixed: 4 or 8)
+int far_dispatch(vp_ctx* ctx, AsmJob& j) {
+    if (j.ps.mixed) {
+        if (j.tt == 4) return far_launch<float, 4>(ctx, j);
+        if (j.tt == 8) return far_launch<float, 8>(ctx, j);
+    } else {
+        if (j.tt == 2) return far_launch<double, 2>(ctx, j);
+        if (j.tt == 4) return far_launch<double, 4>(ctx, j);
+    }
+    return vp_fail(ctx, VP_ERR_ARG, "far tile not built for this precision");
+}
+int far_dispatch_batch(vp_ctx* ctx, std::vector<std::unique_ptr<AsmJob>>& jobs, DevList& dl) {
+    const bool mixed = jobs[0]->ps.mixed;
+    const int tt = jobs[0]->tt;
+    for (auto& j : jobs)
+        if (j->ps.mixed != mixed) return vp_fail(ctx, VP_ERR_ARG, "one precision for the whole batch");
+    if (mixed) {
+        if (tt == 4) return far_launch_batch<float, 4>(ctx, jobs, dl);
+        if (tt == 8) return far_launch_batch<float, 8>(ctx, jobs, dl);
+    } else {
+        if (tt == 2) return far_launch_batch<double, 2>(ctx, jobs, dl);
+        if (tt == 4) return far_launch_batch<double, 4>(ctx, jobs, dl);
+    }
+    return vp_fail(ctx, VP_ERR_ARG, "far tile not built for this precision");
+}
+
 }  // namespace
 
 // body_sources = 0: the columns of the wake's sheets and filaments alone (explicit_rhs); A's body columns stay zero
@@ -769,185 +1185,40 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
                      const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                      const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil,
                      const int* fil, vp_system** out, vp_assembly_stats* stats, int body_sources) {
-    auto t0 = std::chrono::steady_clock::now();
     if (!out) return vp_fail(ctx, VP_ERR_ARG, "null argument");
     *out = nullptr;
-    const PairInput in{o,     nnode, x,     ntri, tris,  corner_slot, nslot, ntouch, touch_pairs,
-                       sigma, vinf,  nwnode, wx,  nwtri, wtris,       nfil,  fil,   body_sources != 0};
-    PairSetup ps;
-    int r = setup_pairs(ctx, in, PH_SETUP, PH_CLASSIFY, ps);
-    if (r) return r;
-    const bool mixed = ps.mixed;
-    const int ncols = ps.ncols, nq = ps.nq;
-    const float ratio32 = ps.ratio32;
-    const std::vector<TriGeo>& tg = ps.tg;
-    const std::vector<TriGeo>& wg = ps.wg;
-    DevList& dl = ps.dl;
-    TriGeo *d_tg = ps.d_tg, *d_wg = ps.d_wg;
-    CentF *d_tc = ps.d_tc, *d_wc = ps.d_wc;
-    const std::vector<long long>& nfptr = ps.nfptr;
-    const std::vector<long long>& wfptr = ps.wfptr;
+    AsmJob j;
+    j.in = PairInput{o,     nnode, x,     ntri, tris,  corner_slot, nslot, ntouch, touch_pairs,
+                     sigma, vinf,  nwnode, wx,  nwtri, wtris,       nfil,  fil,   body_sources != 0};
+    int r;
+    if ((r = job_prepare(ctx, j)) || (r = far_dispatch(ctx, j)) || (r = near_launch(ctx, j))) return r;
+    return job_finish(ctx, j, out, stats);
+}
 
-    // the system
-    vp_system* sys = new vp_system();
-    sys->nslot = nslot;
-    sys->ncols = ncols;
-    sys->nwnode = nwnode;
-    if ((r = vp_alloc(ctx, &sys->A, size_t(nslot) * ncols)) || (r = vp_alloc(ctx, &sys->b, size_t(nslot)))) {
-        vp_system_free(sys);
-        return r;
+// the batch: every system prepared, then each phase launched once over all of them (one precision for all)
+int vp_assemble_batch_impl(vp_ctx* ctx, const vp_assembly_options* o, int nsys, const vp_assembly_input* in,
+                           vp_system** out, vp_assembly_stats* stats) {
+    if (!out || !in || !o || nsys < 1) return vp_fail(ctx, VP_ERR_ARG, "null argument or empty batch");
+    for (int k = 0; k < nsys; ++k) out[k] = nullptr;
+    std::vector<std::unique_ptr<AsmJob>> jobs;
+    DevList dl;
+    int r;
+    for (int k = 0; k < nsys; ++k) {
+        const vp_assembly_input& w = in[k];
+        jobs.emplace_back(new AsmJob());
+        jobs.back()->in = PairInput{o,       w.nnode,  w.x,      w.ntri,  w.tris, w.corner_slot, w.nslot,
+                                    w.ntouch, w.touch_pairs, w.sigma, w.vinf, w.nwnode, w.wx, w.nwtri,
+                                    w.wtris, w.nfil,   w.fil,    true};
+        if ((r = job_prepare(ctx, *jobs.back()))) return r;
     }
-    VP_CUDA(ctx, cudaMemsetAsync(sys->A, 0, sizeof(double) * size_t(nslot) * ncols, ctx->stream));
-    VP_CUDA(ctx, cudaMemsetAsync(sys->b, 0, sizeof(double) * nslot, ctx->stream));
-
-    // far tier
-    {
-        FarArgs fa{};
-        fa.ntest = ntri;
-        fa.nq = nq;
-        fa.test_mode = o->test;
-        fa.tq = ps.d_tq;
-        fa.tw = ps.d_tw;
-        fa.tgeo = d_tg;
-        fa.tcent = d_tc;
-        fa.nset = nwtri > 0 ? 2 : 1;
-        fa.A = sys->A;
-        fa.lda = ncols;
-        fa.b = sys->b;
-        fa.ratio32 = ratio32;
-        fa.ratio = o->far_ratio;
-        fa.kernel_far = o->kernel_far;
-        const std::vector<TriGeo>* sets[2] = {&tg, &wg};
-        int nsrc[2] = {body_sources ? ntri : 0, nwtri};
-        for (int set = 0; set < fa.nset; ++set) {
-            std::vector<TriGeo> g(sets[set]->begin(), sets[set]->begin() + nsrc[set]);
-            SrcTiles st = make_src_tiles(g);
-            int *d_cols, *d_ncol;
-            short *d_cptr, *d_cent;
-            if ((r = dl.up(ctx, &d_cols, st.cols)) || (r = dl.up(ctx, &d_ncol, st.ncol)) ||
-                (r = dl.up(ctx, &d_cptr, st.cptr)) || (r = dl.up(ctx, &d_cent, st.cent))) {
-                vp_system_free(sys);
-                return r;
+    if ((r = far_dispatch_batch(ctx, jobs, dl)) || (r = near_launch_batch(ctx, jobs, dl))) return r;
+    for (int k = 0; k < nsys; ++k)
+        if ((r = job_finish(ctx, *jobs[k], &out[k], stats ? stats + k : nullptr))) {
+            for (int i = 0; i < k; ++i) {
+                vp_system_free(out[i]);
+                out[i] = nullptr;
             }
-            fa.nsrc[set] = nsrc[set];
-            fa.ntile[set] = st.ntile;
-            fa.col_off[set] = set == 0 ? 0 : nslot;
-            fa.scent[set] = set == 0 ? d_tc : d_wc;
-            fa.sgeo[set] = set == 0 ? d_tg : d_wg;
-            fa.tile_cols[set] = d_cols;
-            fa.tile_ncol[set] = d_ncol;
-            fa.tile_cptr[set] = d_cptr;
-            fa.tile_cent[set] = d_cent;
-            if (mixed) {
-                std::vector<float> soa;
-                float* d;
-                fill_soa(g, soa, fa.pad[set]);
-                if ((r = dl.up(ctx, &d, soa))) { vp_system_free(sys); return r; }
-                fa.soa[set] = d;
-            } else {
-                std::vector<double> soa;
-                double* d;
-                fill_soa(g, soa, fa.pad[set]);
-                if ((r = dl.up(ctx, &d, soa))) { vp_system_free(sys); return r; }
-                fa.soa[set] = d;
-            }
-        }
-        std::vector<int> cs(corner_slot, corner_slot + 3 * ntri);
-        r = mixed ? run_far<float, 8>(ctx, fa, tg, cs, nslot, dl) : run_far<double, 4>(ctx, fa, tg, cs, nslot, dl);
-        if (r) { vp_system_free(sys); return r; }
-    }
-
-    // near, touching and contact tiers, one launch per colour of test triangles
-    unsigned long long* d_stats;
-    if ((r = dl.alloc(ctx, &d_stats, 13))) { vp_system_free(sys); return r; }
-    VP_CUDA(ctx, cudaMemsetAsync(d_stats, 0, sizeof(unsigned long long) * 13, ctx->stream));
-    {
-        std::vector<std::vector<int>> groups(ntri);
-        for (int t = 0; t < ntri; ++t) groups[t] = {corner_slot[3 * t], corner_slot[3 * t + 1], corner_slot[3 * t + 2]};
-        auto colours = colour_groups(groups, nslot);
-        std::vector<int> all;
-        std::vector<int> off{0};
-        for (auto& c : colours) {
-            all.insert(all.end(), c.begin(), c.end());
-            off.push_back((int)all.size());
-        }
-        int* d_tests;
-        if ((r = dl.up(ctx, &d_tests, all))) { vp_system_free(sys); return r; }
-        NearArgs na = near_args(ps, in);
-        na.A = sys->A;
-        na.b = sys->b;
-        na.stats = d_stats;
-        int *d_rest, *d_wrest, *d_rcnt;
-        if ((r = dl.alloc(ctx, &d_rest, size_t(std::max(nfptr[ntri], 1LL)))) ||
-            (r = dl.alloc(ctx, &d_wrest, size_t(std::max(wfptr[ntri], 1LL)))) ||
-            (r = dl.alloc(ctx, &d_rcnt, size_t(2) * ntri))) {
-            vp_system_free(sys);
             return r;
         }
-        na.rest_src = d_rest;
-        na.wrest_src = d_wrest;
-        na.rest_cnt = d_rcnt;
-        vp_phase_begin(ctx, PH_NEAR);
-        const size_t near_smem = sizeof(NearChunkSh) * NEAR_WARPS;
-        VP_CUDA(ctx, cudaFuncSetAttribute(near_kernel_lanes, cudaFuncAttributeMaxDynamicSharedMemorySize, int(near_smem)));
-        for (int pass = 0; pass < 2; ++pass) {
-            if (pass == 1) {
-                // the rest pairs as one list, evaluated pair-parallel into per-pair blocks
-                long long nrest = 0;
-                double* d_pairs;
-                if ((r = rest_list(ctx, dl, na, &nrest)) ||
-                    (r = dl.alloc(ctx, &d_pairs, size_t(12) * size_t(std::max(nrest, 1LL))))) {
-                    vp_system_free(sys);
-                    return r;
-                }
-                na.pair_out = d_pairs;
-                if (nrest > 0) {
-                    const int nb = persistent_blocks(ctx, near_kernel_pairs, 32 * NEAR_WARPS, 0);
-                    vp_phase_end(ctx);
-                    vp_phase_begin(ctx, PH_NEAR_PAIRS);
-                    near_kernel_pairs<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
-                    vp_phase_end(ctx);
-                    vp_phase_begin(ctx, PH_NEAR);
-                    ctx->launches++;
-                }
-            }
-            for (size_t c = 0; c < colours.size(); ++c) {
-                na.tests = d_tests + off[c];
-                na.ntests = off[c + 1] - off[c];
-                int nb = (na.ntests + NEAR_WARPS - 1) / NEAR_WARPS;
-                if (!nb) continue;
-                if (pass == 0)
-                    near_kernel_lanes<<<nb, 32 * NEAR_WARPS, near_smem, ctx->stream>>>(na);
-                else
-                    near_kernel_rest<<<nb, 32 * NEAR_WARPS, 0, ctx->stream>>>(na);
-                ctx->launches++;
-            }
-        }
-        vp_phase_end(ctx);
-        VP_CUDA(ctx, cudaGetLastError());
-    }
-    unsigned long long hs[13];
-    VP_CUDA(ctx, vp_d2h(ctx, hs, d_stats, sizeof(hs)));
-    cudaError_t e = cudaStreamSynchronize(ctx->stream);
-    if (e != cudaSuccess) {
-        vp_system_free(sys);
-        return vp_fail(ctx, VP_ERR_CUDA, std::string("assembly kernels: ") + cudaGetErrorString(e));
-    }
-    if (stats) {
-        long long total = (long long)ntri * (ntri + nwtri) + (long long)ntri * nfil;
-        long long nonfar = 0;
-        for (int k = 0; k < 6; ++k) {
-            stats->pairs[k] = (long long)hs[k];
-            stats->points[k] = (long long)hs[6 + k];
-            if (k != TIER_FAR) nonfar += (long long)hs[k];
-        }
-        long long far_fil = (long long)hs[TIER_FAR];
-        long long far_tri = total - nonfar - far_fil;
-        stats->pairs[TIER_FAR] = far_tri + far_fil;
-        stats->points[TIER_FAR] = (long long)hs[6 + TIER_FAR] + far_tri * nq;
-        stats->points_fp64 = (long long)hs[12] + (mixed ? 0 : far_tri * nq);
-        stats->time_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    }
-    *out = sys;
     return VP_OK;
 }

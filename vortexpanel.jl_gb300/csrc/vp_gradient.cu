@@ -391,7 +391,9 @@ __device__ void adj_point64(const NearArgs& a, const TriGeo& T, const TriGeo& S,
         adj_point_far_multi(as, K, Wn, Kd, l0, l1, l2, r, mm, gx);
     else
         adj_point_exact_multi(as, K, Wn, Kd, l0, l1, l2, R[0], R[1], R[2], r, mm, 0, 1e-12, gx);
-    for (int j = 0; j < K; ++j) {
+#pragma unroll
+    for (int j = 0; j < ADJ_MAX; ++j) {
+        if (j >= K) break;
         double f[NSUM];
         sums_flat(as[j], f);
         for (int z = 0; z < NSUM; ++z) v[j][z] = float(f[z]);
@@ -507,9 +509,13 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjMulti& mx, i
             if (need)
                 for (int j = 0; j < ADJ_MAX; ++j) adj_zero(as[j]);
         }
-        if (a.mixed)
-            for (int j = 0; j < K; ++j)
-                seg_accumulate<NSUM>(ns.accf[j], (double (*)[NSUM])nullptr, lane, p, reinterpret_cast<float*>(&as[j]));
+        if (a.mixed) {
+#pragma unroll
+            for (int j = 0; j < ADJ_MAX; ++j)
+                if (j < K)
+                    seg_accumulate<NSUM>(ns.accf[j], (double (*)[NSUM])nullptr, lane, p,
+                                         reinterpret_cast<float*>(&as[j]));
+        }
         unsigned mq = __ballot_sync(FULL, need);
         if (mq) {
             int pos = nq + __popc(mq & ((1u << lane) - 1u));
@@ -531,8 +537,9 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjMulti& mx, i
                 const TriGeo& Sq = wake ? a.wtri[list[qpair]] : a.tri[list[qpair]];
                 adj_point64(a, T, Sq, ns, pc.nuk, K, qpair, ns.qk[lane], qv);
             }
-            for (int j = 0; j < K; ++j)
-                seg_accumulate<NSUM>(ns.accf[j], (double (*)[NSUM])nullptr, lane, qpair, qv[j]);
+#pragma unroll
+            for (int j = 0; j < ADJ_MAX; ++j)
+                if (j < K) seg_accumulate<NSUM>(ns.accf[j], (double (*)[NSUM])nullptr, lane, qpair, qv[j]);
             const int rest = nq - take;
             int mp = 0, mk = 0;
             if (lane < rest) {

@@ -52,6 +52,8 @@ struct vp_ctx {
     long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device copies made by the library
     std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
     TcWork tc;
+    // test triangles per far-tier tile, per precision (vp_precision): set by vp_set_far_tile (the autotuner's choice)
+    int far_tile[2] = {4, 8};
 };
 
 // record the start/end of a phase on the context's stream; vp_phase_flush() accumulates the elapsed times

@@ -21,10 +21,17 @@ constexpr int NQMAX = 7;     // points of the far rule, at most
 constexpr int NFIELD = 42;   // scalar fields per source in the far kernel's SoA
 constexpr int NEAR_WARPS = 4;
 constexpr int LEAFBUF = 32;
-constexpr int ADJ_MAX = 2;  // adjoint vectors of one pass
+constexpr int ADJ_MAX = ADJ_VEC_MAX;  // adjoint vectors of one pass
 // FP32 guard of the adjoint's derivative evaluations (corner, edge sin^2, plane): the forward's (the derivatives keep
 // the accuracy of the values there: adjoint gradients within 3e-6 of the FP64 path's on the wings measured)
-#define ADJ_GUARD 1e-2f, 4e-2f, 1e-4f
+// The FP32 guard of the pair integrals (Fp32Guard: corner, edge_sin2, plane), forward and adjoint: a point goes to FP64
+// where it sees a source edge at an angle whose sine squared is below 1e-2 from inside the edge's span, or lies within
+// 1e-4 of the plane over the triangle, or within 1e-4 source diameters of a corner. Measured against FP64 on the
+// touching and contact tiers of a lifting wing (offsets interpolated in FP32 as the kernels form them), the FP32
+// error does not grow toward a corner, so the corner bound only keeps the offsets from vanishing; it grows as the
+// edge angle closes, by ~1e-5 of the point's value at a sine squared of 1e-2.
+#define PAIR_GUARD 1e-4f, 1e-2f, 1e-4f
+#define ADJ_GUARD PAIR_GUARD
 
 // ------------------------------------------------------------------------------------------------------------------
 // host: quadrature rules (src/elements/rules.jl)
@@ -566,7 +573,7 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float 
         v3<float> ra = l0 * mk3(E[0], E[1], E[2]) + l1 * mk3(E[9], E[10], E[11]) + l2 * mk3(E[18], E[19], E[20]);
         v3<float> rb = l0 * mk3(E[3], E[4], E[5]) + l1 * mk3(E[12], E[13], E[14]) + l2 * mk3(E[21], E[22], E[23]);
         v3<float> rc = l0 * mk3(E[6], E[7], E[8]) + l1 * mk3(E[15], E[16], E[17]) + l2 * mk3(E[24], E[25], E[26]);
-        const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+        const Fp32Guard g{PAIR_GUARD};
         if (!sv_exact3_guarded(S, ra, rb, rc, pc.side, g, w)) return false;
     }
     v3<float> psi = pc.a->test_mode == 0 ? mk3(l0, l1, l2) : mk3(1.f, 1.f, 1.f);

@@ -269,7 +269,7 @@ __device__ v3<double> sheet_w(const TriGeo& S, v3<double> x, double kfar) {
         if (dot(r64, r64) > fd * fd) {
             w = sv_far(K, r);
         } else {
-            const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+            const Fp32Guard g{PAIR_GUARD};
             done = sv_exact3_guarded(K, r - K.d[0], r - K.d[1], r - K.d[2], 0, g, w);
         }
         if (done) return mk3(double(w.x), double(w.y), double(w.z));
@@ -620,7 +620,7 @@ __global__ void __launch_bounds__(NB_TPB) body_vel_kernel(BVelArgs a) {
     split_hi_lo(x.y, xh[1], xl[1]);
     split_hi_lo(x.z, xh[2], xl[2]);
     const float kf = float(a.kernel_far);
-    const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+    const Fp32Guard g{PAIR_GUARD};
     v3<double> acc = mk3(0.0, 0.0, 0.0);
     const int s0 = blockIdx.y * NB_CHUNK, s1 = min(a.ntri, s0 + NB_CHUNK);
     for (int t0 = s0; t0 < s1; t0 += BV_TILE) {

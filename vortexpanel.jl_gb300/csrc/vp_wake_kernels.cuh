@@ -153,7 +153,7 @@ __global__ void __launch_bounds__(NB_THREADS) body_kernel(int nsrc, const BodySr
     const bool valid = i < npts;
     const v3<double> x = valid ? mk3(X[3 * i], X[3 * i + 1], X[3 * i + 2]) : mk3(0.0, 0.0, 0.0);
     v3<double> acc = mk3(0.0, 0.0, 0.0);
-    const Fp32Guard g{1e-2f, 4e-2f, 1e-4f};
+    const Fp32Guard g{PAIR_GUARD};
     for (int s0 = 0; s0 < nsrc; s0 += 32) {
         const int ns = min(32, nsrc - s0);
         __syncthreads();

@@ -56,6 +56,13 @@ class vp_freewake_counts(ctypes.Structure):
                 ("conversions", ctypes.c_int), ("I_prev", ctypes.c_double * 3)]
 
 
+class vp_assembly_input(ctypes.Structure):
+    _fields_ = [("nnode", ctypes.c_int), ("x", D), ("ntri", ctypes.c_int), ("tris", I), ("corner_slot", I),
+                ("nslot", ctypes.c_int), ("ntouch", ctypes.c_int), ("touch_pairs", I), ("sigma", D), ("vinf", D),
+                ("nwnode", ctypes.c_int), ("wx", D), ("nwtri", ctypes.c_int), ("wtris", I), ("nfil", ctypes.c_int),
+                ("fil", I)]
+
+
 B8 = ctypes.POINTER(ctypes.c_byte)
 
 # (name, restype, argtypes) of every entry point declared in include/vortexpanel_gpu.h
@@ -68,6 +75,11 @@ SIGNATURES = [
      [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, D, ctypes.c_int, I, I, ctypes.c_int,
       ctypes.c_int, I, D, D, ctypes.c_int, D, ctypes.c_int, I, ctypes.c_int, I, ctypes.POINTER(ctypes.c_void_p),
       ctypes.POINTER(vp_assembly_stats)]),
+    ("vp_set_far_tile", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    ("vp_get_far_tile", ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    ("vp_assemble_batch", ctypes.c_int,
+     [ctypes.c_void_p, ctypes.POINTER(vp_assembly_options), ctypes.c_int, ctypes.POINTER(vp_assembly_input),
+      ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(vp_assembly_stats)]),
     ("vp_system_shape", ctypes.c_int, [ctypes.c_void_p, I, I]),
     ("vp_system_download", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, D, D]),
     ("vp_system_download_rows", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, D, D]),

@@ -20,7 +20,7 @@ from dataclasses import dataclass, fields
 import numpy as np
 import scipy.sparse as sp
 
-from . import _lib
+from . import _lib, autotune
 from ._lib import D, I, check, default_context, load
 
 TIER_NAMES = ("self", "edge", "vertex", "contact", "near", "far")
@@ -194,12 +194,15 @@ def external_rhs(els: Elements, dm, external, test="hat"):
     return b
 
 
-def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, wake=None, ctx=None):
+def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, wake=None, ctx=None, tune=True):
     """A, b and stats (assemble.jl:377-447). A is a DeviceSystem; b and stats are on the host. `external`, if given,
     is a velocity field (e.g. particles), a function of points (n x 3) returning velocities (n x 3): its part of b is
-    added on the host (external_rhs) to the b of the device, which then differs from A.rhs()."""
+    added on the host (external_rhs) to the b of the device, which then differs from A.rhs(). With `tune`, the far
+    tier's tile is the autotuner's choice for the mesh's size (autotune.py, the committed sweep)."""
     opts = opts or AssemblyOptions()
     ctx = ctx or default_context()
+    if tune:
+        autotune.apply(ctx, opts.precision, g.ntri)
     o = opts.c_struct()
     x, px = _dp(g.x)
     tr, pt = _ip(g.tris)
@@ -230,6 +233,55 @@ def assemble(g, dm, els, sigma, V, opts: AssemblyOptions = None, external=None, 
     if external is not None:
         b = b + external_rhs(els, dm, external, opts.test)
     return A, b, stats
+
+
+def assemble_batch(cases, opts: AssemblyOptions = None, ctx=None, tune=True):
+    """assemble for a batch of independent bodies of uneven sizes in shared launches (vp_assemble_batch): cases is a
+    list of (g, dm, sigma, V, wake or None); returns a list of (A, b, stats) as assemble gives them with the same far
+    tile, A and b the same bit for bit. One options set (and precision) and one far tile (with `tune`, the
+    autotuner's choice for the largest body) for the whole batch."""
+    opts = opts or AssemblyOptions()
+    ctx = ctx or default_context()
+    if tune:
+        autotune.apply(ctx, opts.precision, max(c[0].ntri for c in cases))
+    o = opts.c_struct()
+    keep = []
+    ins = (_lib.vp_assembly_input * len(cases))()
+    shapes = []
+    for k, (g, dm, sigma, V, wake) in enumerate(cases):
+        x, px = _dp(g.x)
+        tr, pt = _ip(g.tris)
+        cs, pc = _ip(dm.corner_slot)
+        tp = np.asarray(g.touch_pairs, np.int32).reshape(-1, 2)
+        tpp, ptp = _ip(tp if len(tp) else np.zeros((1, 2), np.int32))
+        sg, ps = _dp(sigma)
+        if sg.shape != (g.ntri,):
+            raise ValueError(f"case {k}: σ has {sg.shape[0]} entries, expected {g.ntri}")
+        VV, pV = _dp(V)
+        keep += [x, tr, cs, tpp, sg, VV]
+        it = ins[k]
+        it.nnode, it.x, it.ntri, it.tris, it.corner_slot, it.nslot = g.nnode, px, g.ntri, pt, pc, dm.nslot
+        it.ntouch, it.touch_pairs, it.sigma, it.vinf = len(tp), ptp, ps, pV
+        nw = 0
+        if wake is not None:
+            wx, pwx = _dp(wake.x)
+            wt, pwt = _ip(wake.tris if len(wake.tris) else np.zeros((1, 3)))
+            wf, pwf = _ip(wake.filaments if len(wake.filaments) else np.zeros((1, 2)))
+            keep += [wx, wt, wf]
+            nw = wake.x.shape[0]
+            it.nwnode, it.wx, it.nwtri, it.wtris, it.nfil, it.fil = nw, pwx, len(wake.tris), pwt, len(wake.filaments), pwf
+        shapes.append((dm.nslot, dm.nslot + nw))
+    hs = (ctypes.c_void_p * len(cases))()
+    sts = (_lib.vp_assembly_stats * len(cases))()
+    check(ctx.h, load().vp_assemble_batch(ctx.h, ctypes.byref(o), len(cases), ins, hs, sts))
+    out = []
+    for k, (nr, nc) in enumerate(shapes):
+        A = DeviceSystem(ctx, ctypes.c_void_p(hs[k]), nr, nc)
+        st = sts[k]
+        stats = {"pairs": dict(zip(TIER_NAMES, list(st.pairs))), "points": dict(zip(TIER_NAMES, list(st.points))),
+                 "time": st.time_ms / 1e3, "points_fp64": st.points_fp64}
+        out.append((A, A.rhs(), stats))
+    return out
 
 
 # ---- the bordered solve ------------------------------------------------------------------------------------------------
