@@ -72,7 +72,8 @@ KINDS = {
     "vp_system**": {"Ref{Ptr{Cvoid}}"}, "vp_factor**": {"Ref{Ptr{Cvoid}}"}, "vp_freewake**": {"Ref{Ptr{Cvoid}}"},
     "vp_assembly_options*": {"Ref{VpOptions}"}, "vp_assembly_stats*": {"Ref{VpStats}", "Ptr{VpStats}"},
     "vp_freewake_setup*": {"Ref{VpFreeWakeSetup}"}, "vp_freewake_record*": {"Ref{VpFreeWakeRecord}"},
-    "vp_freewake_counts*": {"Ref{VpFreeWakeCounts}"},
+    "vp_freewake_counts*": {"Ref{VpFreeWakeCounts}"}, "vp_assembly_input*": {"Ptr{VpInput}"},
+    "vp_system**": {"Ref{Ptr{Cvoid}}", "Ptr{Ptr{Cvoid}}"},
 }
 RET = {"int": "Cint", "void": "Cvoid", "constchar*": "Cstring", "const char*": "Cstring"}
 

@@ -162,6 +162,55 @@ function assemble(g::SurfaceGeometry, dm::DOFMapping, els, σ, V∞; opts=Assemb
     return A, b, st[]
 end
 
+# vp_assembly_input (vortexpanel_gpu.h): one body of a batch; the arrays it points to are kept alive by the caller
+struct VpInput
+    nnode::Cint; x::Ptr{Cdouble}; ntri::Cint; tris::Ptr{Cint}; corner_slot::Ptr{Cint}; nslot::Cint
+    ntouch::Cint; touch_pairs::Ptr{Cint}; sigma::Ptr{Cdouble}; vinf::Ptr{Cdouble}
+    nwnode::Cint; wx::Ptr{Cdouble}; nwtri::Cint; wtris::Ptr{Cint}; nfil::Cint; fil::Ptr{Cint}
+end
+
+# assemble for several bodies of uneven sizes in shared launches (vp_assemble_batch); cases: (g, dm, σ, V∞, wake)
+function assemble_batch(cases; opts=AssemblyOptions(), precision::Symbol=:fp64, ctx::Context=default_context())
+    o = Ref(VpOptions(opts; precision))
+    keep = Any[]
+    ins = VpInput[]
+    for (g, dm, σ, V∞, wake) in cases
+        a = (flat(g.x), idx0(g.tris), idx0(dm.corner_slot),
+             isempty(g.touch_pairs) ? Cint[0, 0] : idx0(g.touch_pairs), collect(Cdouble, σ), collect(Cdouble, V∞),
+             wake === nothing ? Cdouble[0] : flat(wake.x),
+             wake === nothing || isempty(wake.tris) ? Cint[0, 0, 0] : idx0(wake.tris),
+             wake === nothing || isempty(wake.filaments) ? Cint[0, 0] : idx0(wake.filaments))
+        push!(keep, a)
+        nw = wake === nothing ? 0 : length(wake.x)
+        push!(ins, VpInput(length(g.x), pointer(a[1]), length(g.tris), pointer(a[2]), pointer(a[3]), dm.nslot,
+                           length(g.touch_pairs), pointer(a[4]), pointer(a[5]), pointer(a[6]), nw, pointer(a[7]),
+                           wake === nothing ? 0 : length(wake.tris), pointer(a[8]),
+                           wake === nothing ? 0 : length(wake.filaments), pointer(a[9])))
+    end
+    hs = fill(Ptr{Cvoid}(C_NULL), length(cases))
+    sts = Vector{VpStats}(undef, length(cases))
+    GC.@preserve keep check(ctx.h, ccall((:vp_assemble_batch, LIB), Cint,
+        (Ptr{Cvoid}, Ref{VpOptions}, Cint, Ptr{VpInput}, Ptr{Ptr{Cvoid}}, Ptr{VpStats}),
+        ctx.h, o, length(cases), ins, hs, sts))
+    out = []
+    for (k, (g, dm, σ, V∞, wake)) in enumerate(cases)
+        nw = wake === nothing ? 0 : length(wake.x)
+        A = DeviceSystem(ctx, hs[k], dm.nslot, dm.nslot + nw)
+        finalizer(a -> ccall((:vp_system_free, LIB), Cvoid, (Ptr{Cvoid},), a.h), A)
+        b = Vector{Cdouble}(undef, dm.nslot)
+        check(ctx.h, ccall((:vp_system_download, LIB), Cint, (Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Cdouble}, Ptr{Cdouble}),
+            ctx.h, A.h, C_NULL, b))
+        push!(out, (A, b, sts[k]))
+    end
+    return out
+end
+
+# the far tier's test triangles per tile (the autotuner's setting): 2 or 4 in FP64, 4 or 8 mixed
+set_far_tile(ctx::Context, precision::Symbol, tile::Integer) = check(ctx.h, ccall((:vp_set_far_tile, LIB), Cint,
+    (Ptr{Cvoid}, Cint, Cint), ctx.h, precision == :mixed ? 1 : 0, tile))
+far_tile(ctx::Context, precision::Symbol) = ccall((:vp_get_far_tile, LIB), Cint, (Ptr{Cvoid}, Cint), ctx.h,
+    precision == :mixed ? 1 : 0)
+
 # ---- the bordered solve -----------------------------------------------------------------------------------------------
 
 mutable struct GalerkinFactorization
