@@ -83,7 +83,7 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
                 const int* fil, vp_system** out, vp_assembly_stats* stats);
 
 /* Test triangles per tile of the far tier's kernel (the tile each CTA holds in shared memory against a 128-source
- * tile), per precision: 2 or 4 in VP_FP64 (default 4), 4 or 8 in VP_MIXED (default 8). The autotuner
+ * tile), per precision: 1, 2 or 4 in VP_FP64 (default 4), 2, 4 or 8 in VP_MIXED (default 8). The autotuner
  * (vortexpanel_gpu/autotune.py) picks it per mesh size from a measured sweep. No counterpart in the reference. */
 int vp_set_far_tile(vp_ctx* ctx, int precision, int tile);
 /* The current far tile of a precision (0 for a bad argument). */

@@ -149,8 +149,9 @@ int vp_assemble(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const d
 int vp_set_far_tile(vp_ctx* ctx, int precision, int tile) {
     if (!ctx) return VP_ERR_ARG;
     if (precision != VP_FP64 && precision != VP_MIXED) return vp_fail(ctx, VP_ERR_ARG, "unknown precision");
-    const bool ok = precision == VP_MIXED ? (tile == 4 || tile == 8) : (tile == 2 || tile == 4);
-    if (!ok) return vp_fail(ctx, VP_ERR_ARG, "far tile: 2 or 4 test triangles in FP64, 4 or 8 in mixed precision");
+    const bool ok = precision == VP_MIXED ? (tile == 2 || tile == 4 || tile == 8) : (tile == 1 || tile == 2 || tile == 4);
+    if (!ok)
+        return vp_fail(ctx, VP_ERR_ARG, "far tile: 1, 2 or 4 test triangles in FP64, 2, 4 or 8 in mixed precision");
     ctx->far_tile[precision] = tile;
     return VP_OK;
 }

@@ -916,10 +916,11 @@ int job_prepare(vp_ctx* ctx, AsmJob& j) {
     }
     j.tt = ctx->far_tile[ps.mixed ? 1 : 0];
     switch (j.tt) {
+        case 1: r = far_prepare<1>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
         case 2: r = far_prepare<2>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
         case 4: r = far_prepare<4>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
         case 8: r = far_prepare<8>(ctx, fa, ntri, in.corner_slot, nslot, dl, j.far_col); break;
-        default: return vp_fail(ctx, VP_ERR_ARG, "far tile must be 2, 4 or 8 test triangles");
+        default: return vp_fail(ctx, VP_ERR_ARG, "far tile must be 1, 2, 4 or 8 test triangles");
     }
     if (r) return r;
     // near, touching and contact tiers
@@ -1152,12 +1153,14 @@ int near_launch_batch(vp_ctx* ctx, std::vector<std::unique_ptr<AsmJob>>& jobs, D
     return VP_OK;
 }
 
-// the far launches of the job's precision and tile (FP64: 2 or 4 test triangles per tile, mixed: 4 or 8)
+// the far launches of the job's precision and tile (FP64: 1, 2 or 4 test triangles per tile, mixed: 2, 4 or 8)
 int far_dispatch(vp_ctx* ctx, AsmJob& j) {
     if (j.ps.mixed) {
+        if (j.tt == 2) return far_launch<float, 2>(ctx, j);
         if (j.tt == 4) return far_launch<float, 4>(ctx, j);
         if (j.tt == 8) return far_launch<float, 8>(ctx, j);
     } else {
+        if (j.tt == 1) return far_launch<double, 1>(ctx, j);
         if (j.tt == 2) return far_launch<double, 2>(ctx, j);
         if (j.tt == 4) return far_launch<double, 4>(ctx, j);
     }
@@ -1169,9 +1172,11 @@ int far_dispatch_batch(vp_ctx* ctx, std::vector<std::unique_ptr<AsmJob>>& jobs, 
     for (auto& j : jobs)
         if (j->ps.mixed != mixed) return vp_fail(ctx, VP_ERR_ARG, "one precision for the whole batch");
     if (mixed) {
+        if (tt == 2) return far_launch_batch<float, 2>(ctx, jobs, dl);
         if (tt == 4) return far_launch_batch<float, 4>(ctx, jobs, dl);
         if (tt == 8) return far_launch_batch<float, 8>(ctx, jobs, dl);
     } else {
+        if (tt == 1) return far_launch_batch<double, 1>(ctx, jobs, dl);
         if (tt == 2) return far_launch_batch<double, 2>(ctx, jobs, dl);
         if (tt == 4) return far_launch_batch<double, 4>(ctx, jobs, dl);
     }

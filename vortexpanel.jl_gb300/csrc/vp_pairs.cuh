@@ -30,9 +30,11 @@ constexpr int ADJ_MAX = ADJ_VEC_MAX;  // adjoint vectors of one pass
 // contact tiers of a lifting wing (offsets interpolated in FP32 as the kernels form them), the FP32 error of a value
 // does not grow toward a corner, so the corner bound only keeps the offsets from vanishing; it grows as the edge angle
 // closes, to ~1e-5 of the point's value at a sine squared of 1e-2 (the forward's bound). The adjoint's derivatives
-// grow faster toward an edge: at 1e-2 the 25k wing's mixed gradients moved to 6e-5 of FP64, so the adjoint keeps 4e-2.
+// grow like 1/r toward a corner and an edge, and their FP32 sums over a piece cancel: with a corner bound of 1e-4 the
+// 25k wing's mixed gradients moved from 5e-6 to 5e-5 of FP64 (6e-5 with the edge bound of 1e-2 as well), so the
+// adjoint keeps 1e-2 diameters at corners and 4e-2 at edges.
 #define PAIR_GUARD 1e-4f, 1e-2f, 1e-4f
-#define ADJ_GUARD 1e-4f, 4e-2f, 1e-4f
+#define ADJ_GUARD 1e-2f, 4e-2f, 1e-4f
 
 // ------------------------------------------------------------------------------------------------------------------
 // host: quadrature rules (src/elements/rules.jl)

@@ -205,7 +205,7 @@ function assemble_batch(cases; opts=AssemblyOptions(), precision::Symbol=:fp64, 
     return out
 end
 
-# the far tier's test triangles per tile (the autotuner's setting): 2 or 4 in FP64, 4 or 8 mixed
+# the far tier's test triangles per tile (the autotuner's setting): 1, 2 or 4 in FP64, 2, 4 or 8 mixed
 set_far_tile(ctx::Context, precision::Symbol, tile::Integer) = check(ctx.h, ccall((:vp_set_far_tile, LIB), Cint,
     (Ptr{Cvoid}, Cint, Cint), ctx.h, precision == :mixed ? 1 : 0, tile))
 far_tile(ctx::Context, precision::Symbol) = ccall((:vp_get_far_tile, LIB), Cint, (Ptr{Cvoid}, Cint), ctx.h,

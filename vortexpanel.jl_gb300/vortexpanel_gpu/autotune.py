@@ -21,7 +21,7 @@ import time
 
 import numpy as np
 
-TILES = {"fp64": (2, 4), "mixed": (4, 8)}
+TILES = {"fp64": (1, 2, 4), "mixed": (2, 4, 8)}
 TABLE_FILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tuning.json")
 _table = None
 
