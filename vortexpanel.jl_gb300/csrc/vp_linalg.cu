@@ -720,7 +720,11 @@ static int solve_core(vp_ctx* ctx, const vp_factor* F, int nrhs, double* x, bool
     double prev = INFINITY;
     for (it = 1; it <= 30; ++it) {
         VP_CUDA(ctx, cudaMemcpyAsync(res, rhs, sizeof(double) * tot, cudaMemcpyDeviceToDevice, ctx->stream));
-        VP_BLAS(ctx, cublasDgemm(ctx->blas, op, CUBLAS_OP_N, n, nrhs, n, &mone, F->M, n, x, n, &one, res, n));
+        // a matrix-vector product per column: M is read once per column at the HBM rate (a GEMM with a few columns
+        // takes a tile shape that reads it far slower)
+        for (int k = 0; k < nrhs; ++k)
+            VP_BLAS(ctx, cublasDgemv(ctx->blas, op, n, n, &mone, F->M, n, x + size_t(k) * n, 1, &one,
+                                     res + size_t(k) * n, 1));
         // convergence: every column's residual at FP64 rounding of |M| |x|
         bool ok = true;
         double worst = 0;
