@@ -35,14 +35,14 @@ sys.path.insert(0, os.path.join(ROOT, "vortexpanel.jl_gb300"))
 METRIC = "assemble+factor+solve+adjoint s at 25k tris: mixed vs FP64 GPU, |ΔCL|<1e-6"
 # algorithmic flops per quadrature point: forward (kernel evaluation ~230 + contraction into the hat block 18) and
 # adjoint (value and reverse-mode derivatives of the kernel ~620, once per point, + the sums of the test and source
-# sides ~110 per adjoint vector; the CL and CDi vectors share a pass of the non-far kernels, the far tier runs each)
+# sides ~110 per adjoint vector; the CL and CDi vectors share one pass of every adjoint kernel)
 FLOP_FWD_POINT = 248
 FLOP_ADJ_EVAL = 620
 FLOP_ADJ_SUMS = 110
 # DRAM bytes per touching/contact point of the pair-parallel kernels, from ncu captures on the 28 x 14 per side wing
-# (115.3M such points): adj_pairs_kernel 0.38 GB read + 4.50 GB written, near_kernel_pairs 0.012 + 0.180 GB. It is
-# the per-lane accumulators' stack traffic, which grows with the points; the algorithmic bytes are a few MB.
-DRAM_PER_TOUCH_POINT = {"adj_pairs": 42.3, "near_pairs": 1.66}
+# (115.3M such points): adj_pairs_kernel 0.048 GB read + 0.835 GB written, near_kernel_pairs 0.011 + 0.187 GB. It is
+# stack traffic of the walkers' frames and spills, which grows with the points; the algorithmic bytes are a few MB.
+DRAM_PER_TOUCH_POINT = {"adj_pairs": 7.66, "near_pairs": 1.72}
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
 SIZES = {"wing25k": (112, 56), "medium": (56, 28), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
@@ -300,15 +300,15 @@ def rooflines(per, points, adjoint_points, n, pk_src):
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, nominal FP32 FMA rate at the max SM clock
     pts, apts = points, adjoint_points
     touch = lambda p: sum(v for k, v in p.items() if k not in ("far", "near"))  # noqa: E731  self/edge/vertex/contact
-    adj_pt = FLOP_ADJ_EVAL + FLOP_ADJ_SUMS
     kern = {  # phase: (kernels, bound, flops, points)
-        "far": ("far_kernel<float,8>", "fp32", pts["far"] * FLOP_FWD_POINT, pts["far"]),
+        "far": ("far_kernel<float,TT> (TT the autotuner's tile)", "fp32", pts["far"] * FLOP_FWD_POINT, pts["far"]),
         "near": ("near_kernel_lanes (+ near_kernel_rest)", "fp32", pts["near"] * FLOP_FWD_POINT, pts["near"]),
         "near_pairs": ("near_kernel_pairs", "fp32", touch(pts) * FLOP_FWD_POINT, touch(pts)),
         "adj_far": ("adj_far_kernel<float,8,2>", "fp32", apts["far"] * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), apts["far"]),
-        "adj_near": ("adj_lanes_kernel x2 (+ adj_near_kernel)", "fp32", 2 * apts["near"] * adj_pt, apts["near"]),
-        "adj_pairs": ("adj_pairs_kernel", "fp32", touch(apts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), touch(apts)),
-        "lu": ("lu (cluster panels + cuBLAS SGEMM, FP32 CUDA cores)", "fp32", 2 / 3 * n ** 3, None),
+        "adj_near": ("adj_lanes_kernel, both vectors (+ adj_near_kernel)", "fp32",
+                     apts["near"] * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), apts["near"]),
+        "adj_pairs": ("adj_pairs_kernel<AdjAccW>", "fp32", touch(apts) * (FLOP_ADJ_EVAL + 2 * FLOP_ADJ_SUMS), touch(apts)),
+        "lu": ("lu (cluster leaf panels + tcgen05 bf16x3 trailing updates)", "fp32", 2 / 3 * n ** 3, None),
     }
     kernels = {}
     for ph, (name, bound, flops, npts) in kern.items():

@@ -65,7 +65,7 @@ def test_rooflines_of_the_pair_kernels():
            "adj_pairs": 2135.2, "setup": 0.9, "wake": 0.0}
     kernels, roof = bench.rooflines(per, pts, pts, 12824, ({"sm_max_mhz": 2070.0}, "measured"))
     touch = 115813152 + 59978016 + 46096344 + 1747470186
-    assert roof["kernel"] == "adj_pairs_kernel"
+    assert roof["kernel"] == "adj_pairs_kernel<AdjAccW>"
     assert abs(roof["achieved"] - touch * (bench.FLOP_ADJ_EVAL + 2 * bench.FLOP_ADJ_SUMS) / 2.1352 / 1e12) < 1e-9
     assert abs(roof["peak"] - 152 * 128 * 2 * 2070e6 / 1e12) < 1e-9
     assert abs(roof["frac"] - roof["achieved"] / roof["peak"]) < 1e-15
