@@ -12,7 +12,6 @@
 #include <unordered_map>
 
 #include "vp_adjoint_common.cuh"
-#include "vp_ff.cuh"
 #include "vp_internal.h"
 #include "vp_math.cuh"
 namespace {
@@ -352,7 +351,6 @@ struct NearArgs {
     int ntouch;
     const RulePt* rule[5];
     const float4* rulef[5];  // the same rules in FP32 (l0, l1, l2, w)
-    const float4* rulel[5];  // and what FP32 leaves of them (rulef + rulel is the rule in float-float)
     int nrule[5];
     double* A;
     long long lda;
@@ -378,11 +376,8 @@ struct WarpSh {
     float E32[27];         // E in FP32
     float D32[9];          // D in FP32
     float Sdf[9], Snf[3], Snuf[9], Slenf[3], Sareaf, Sdiamf;
-    // what FP32 leaves of E, D and the source data (the float-float points: hi the FP32 copy, lo these)
-    float Elo[27], Dlo[9], Sdl[9], Snl[3], Snul[9], Slenl[3], Sareal, Sdiaml;
     double leaf[LEAFBUF][10];
     float leaff[LEAFBUF][10];  // the leaves in FP32: corners, and frac x the test triangle's area
-    float leafl[LEAFBUF][10];  // and what FP32 leaves of them
     int qi[64], ql[64];    // points waiting for FP64: rule point, and leaf (-1: the current piece)
 };
 
@@ -588,60 +583,6 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, FwdAcc& acc, float 
     acc.Pf[0] += (W * psi.x) * w;
     acc.Pf[1] += (W * psi.y) * w;
     acc.Pf[2] += (W * psi.z) * w;
-    if (++acc.nf == 16) fold32(acc);
-    return true;
-}
-
-// the float-float copies of the pair's offsets and source data (hi: the FP32 copy, lo: what FP32 leaves)
-__device__ __forceinline__ v3<ff> ffE(const WarpSh& sh, int i) {
-    return mk3(ff(sh.E32[i], sh.Elo[i]), ff(sh.E32[i + 1], sh.Elo[i + 1]), ff(sh.E32[i + 2], sh.Elo[i + 2]));
-}
-__device__ __forceinline__ v3<ff> ffD(const WarpSh& sh, int i) {
-    return mk3(ff(sh.D32[i], sh.Dlo[i]), ff(sh.D32[i + 1], sh.Dlo[i + 1]), ff(sh.D32[i + 2], sh.Dlo[i + 2]));
-}
-__device__ __forceinline__ SrcKern<ff> srcff(const WarpSh& sh) {
-    SrcKern<ff> S;
-    for (int k = 0; k < 3; ++k) {
-        S.d[k] = mk3(ff(sh.Sdf[3 * k], sh.Sdl[3 * k]), ff(sh.Sdf[3 * k + 1], sh.Sdl[3 * k + 1]),
-                     ff(sh.Sdf[3 * k + 2], sh.Sdl[3 * k + 2]));
-        S.nu[k] = mk3(ff(sh.Snuf[3 * k], sh.Snul[3 * k]), ff(sh.Snuf[3 * k + 1], sh.Snul[3 * k + 1]),
-                      ff(sh.Snuf[3 * k + 2], sh.Snul[3 * k + 2]));
-        S.len[k] = ff(sh.Slenf[k], sh.Slenl[k]);
-    }
-    S.n = mk3(ff(sh.Snf[0], sh.Snl[0]), ff(sh.Snf[1], sh.Snl[1]), ff(sh.Snf[2], sh.Snl[2]));
-    S.area = ff(sh.Sareaf, sh.Sareal);
-    S.diam = ff(sh.Sdiamf, sh.Sdiaml);
-    return S;
-}
-// the offsets of the point l (float-float barycentrics) to the source's corners and centroid
-__device__ __forceinline__ void ff_offsets(const WarpSh& sh, ff l0, ff l1, ff l2, v3<ff>& ra, v3<ff>& rb, v3<ff>& rc,
-                                           v3<ff>& r) {
-    ra = l0 * ffE(sh, 0) + l1 * ffE(sh, 9) + l2 * ffE(sh, 18);
-    rb = l0 * ffE(sh, 3) + l1 * ffE(sh, 12) + l2 * ffE(sh, 21);
-    rc = l0 * ffE(sh, 6) + l1 * ffE(sh, 15) + l2 * ffE(sh, 24);
-    r = l0 * ffD(sh, 0) + l1 * ffD(sh, 3) + l2 * ffD(sh, 6);
-}
-
-// one point of a triangle source in float-float (the mixed path's points that FP32 refuses, near the source's edges,
-// corners or plane): the exact kernel with KMathFF, the contribution added to the FP32 partial sums. False (nothing
-// added) for the points float-float does not take: the multipole's distance, the dual test's ties, values out of
-// FP32's range; those go to FP64.
-__device__ __noinline__ bool eval_point_ff(const PairCtx& pc, FwdAcc& acc, ff l0, ff l1, ff l2, ff W) {
-    if (pc.a->test_mode == 2 || pc.kind != 0) return false;
-    const WarpSh& sh = *pc.sh;
-    v3<ff> ra, rb, rc, r;
-    ff_offsets(sh, l0, l1, l2, ra, rb, rc, r);
-    const SrcKern<ff> S = srcff(sh);
-    const float fd = pc.a->kernel_far32 * sh.Sdiamf;
-    if (ff_f(dot(r, r)) > 0.99f * fd * fd) return false;
-    const v3<ff> w = sv_exact3<ff, KMathFF>(S, ra, rb, rc, r, pc.side, ff(1e-12));
-    if (!(ff_ok(w.x) && ff_ok(w.y) && ff_ok(w.z))) return false;
-    const v3<float> wf = f3(w);
-    const float Wf = ff_f(W);
-    const v3<float> psi = pc.a->test_mode == 0 ? mk3(ff_f(l0), ff_f(l1), ff_f(l2)) : mk3(1.f, 1.f, 1.f);
-    acc.Pf[0] += (Wf * psi.x) * wf;
-    acc.Pf[1] += (Wf * psi.y) * wf;
-    acc.Pf[2] += (Wf * psi.z) * wf;
     if (++acc.nf == 16) fold32(acc);
     return true;
 }
@@ -967,44 +908,6 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAccW& acc, float
     return true;
 }
 
-// the mixed path's refused point in float-float, warp sums: the exact kernel and its derivatives with KMathFF, added
-// to this lane's FP32 partials; false (nothing added) for the points that go to FP64 (as the forward's)
-__device__ __noinline__ bool eval_point_ff(const PairCtx& pc, AdjAccW& acc, ff l0, ff l1, ff l2, ff W) {
-    if (pc.a->test_mode == 2 || pc.kind != 0) return false;
-    const WarpSh& sh = *pc.sh;
-    v3<ff> ra, rb, rc, r;
-    ff_offsets(sh, l0, l1, l2, ra, rb, rc, r);
-    const SrcKern<ff> S = srcff(sh);
-    const float fd = pc.a->kernel_far32 * sh.Sdiamf;
-    if (ff_f(dot(r, r)) > 0.99f * fd * fd) return false;
-    v3<ff> g0, g1, g2;
-    ExactShape<ff> shp;
-    const v3<ff> mff = mk3(ff(pc.mf.x), ff(pc.mf.y), ff(pc.mf.z));
-    const ff sv = sv_exact_vjp<ff, KMathFF>(S, ra, rb, rc, r, mff, pc.side, ff(1e-12), g0, g1, g2, shp);
-    const ff i4pi = ff(1) / (ff(4) * vp_pi<ff>());
-    const v3<ff> w = (shp.L[0] * S.nu[0] + shp.L[1] * S.nu[1] + shp.L[2] * S.nu[2] + shp.Om * S.n) * i4pi;
-    const v3<float> wf = f3(w), g0f = f3(g0), g1f = f3(g1), g2f = f3(g2);
-    const float svf = ff_f(sv);
-    if (!(isfinite(svf) && isfinite(wf.x + wf.y + wf.z) && isfinite(g0f.x + g0f.y + g0f.z) &&
-          isfinite(g1f.x + g1f.y + g1f.z) && isfinite(g2f.x + g2f.y + g2f.z)))
-        return false;
-    const float fl0 = ff_f(l0), fl1 = ff_f(l1), fl2 = ff_f(l2), Wf = ff_f(W);
-    const v3<float> psi = pc.a->test_mode == 0 ? mk3(fl0, fl1, fl2) : mk3(1.f, 1.f, 1.f);
-    float Wn[ADJ_MAX];
-    for (int k = 0; k < ADJ_MAX; ++k)
-        Wn[k] = Wf * (pc.nukf[k][0] * psi.x + pc.nukf[k][1] * psi.y + pc.nukf[k][2] * psi.z);
-    const v3<float> gxf = g0f + g1f + g2f;
-    const float Lf[3] = {ff_f(shp.L[0]), ff_f(shp.L[1]), ff_f(shp.L[2])};
-    const float dLf[3] = {ff_f(shp.dLdlen[0]), ff_f(shp.dLdlen[1]), ff_f(shp.dLdlen[2])};
-    adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, wf, gxf, g0f, g1f, g2f, Lf, dLf, ff_f(shp.Om));
-    if (pc.dep)
-        for (int k = 0; k < pc.nadj; ++k)
-            rule_point(pc, pc.nukf[k], pc.binvf, acc.me->Bbf[k], acc.me->Fbf[k], Wf, fl0, fl1, fl2, svf, gxf, pc.Xcf);
-    return true;
-}
-// the FP64 path's accumulators take no float-float points
-__device__ __forceinline__ bool eval_point_ff(const PairCtx&, AdjAcc&, ff, ff, ff, ff) { return false; }
-
 // the warp's fold after a batch of points (one per lane), every ADJ_FOLD batches; nothing for the other accumulators
 template <class Acc>
 __device__ __forceinline__ void batch_done(PairCtx& pc, Acc& acc) {
@@ -1041,11 +944,8 @@ __device__ __forceinline__ void tri_corners(const TriGeo& g, v3<double>* v) {
 
 // FP64 evaluation of the queued points, 32 at a time (all of them when `all`): rule point qi of the current piece
 // (corners b, fraction frac) or of buffered leaf ql
-// In the mixed path a queued point is first evaluated in float-float (eval_point_ff, from the float-float rule point
-// and piece corners: bf/bl for the current piece, the leaf's leaff/leafl), and in FP64 where float-float gives up.
 template <class Acc>
-__device__ __noinline__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* b, double frac,
-                                     const float* bf, const float* bl) {
+__device__ __noinline__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, const double* b, double frac) {
     const RulePt* R = pc.a->rule[rid];
     const double areaT = pc.T->area;
     while (pc.nq64 >= 32 || (all && pc.nq64 > 0)) {
@@ -1053,27 +953,13 @@ __device__ __noinline__ void drain64(PairCtx& pc, Acc& acc, bool all, int rid, c
         int take = pc.nq64 < 32 ? pc.nq64 : 32;
         if (pc.lane < take) {
             int i = pc.sh->qi[pc.lane], lf = pc.sh->ql[pc.lane];
-            bool done = false;
-            if (pc.fp32) {
-                const float* ch = lf < 0 ? bf : pc.sh->leaff[lf];
-                const float* cl = lf < 0 ? bl : pc.sh->leafl[lf];
-                const float4 mh = pc.a->rulef[rid][i], ml = pc.a->rulel[rid][i];
-                const ff m0(mh.x, ml.x), m1(mh.y, ml.y), m2(mh.z, ml.z);
-                auto cc = [&](int k) { return ff(ch[k], cl[k]); };
-                const ff l0 = m0 * cc(0) + m1 * cc(3) + m2 * cc(6);
-                const ff l1 = m0 * cc(1) + m1 * cc(4) + m2 * cc(7);
-                const ff l2 = m0 * cc(2) + m1 * cc(5) + m2 * cc(8);
-                done = eval_point_ff(pc, acc, l0, l1, l2, ff(mh.w, ml.w) * cc(9));
-            }
-            if (!done) {
-                const double* c = lf < 0 ? b : pc.sh->leaf[lf];
-                double fr = lf < 0 ? frac : pc.sh->leaf[lf][9];
-                RulePt m = R[i];
-                double l0 = m.l0 * c[0] + m.l1 * c[3] + m.l2 * c[6];
-                double l1 = m.l0 * c[1] + m.l1 * c[4] + m.l2 * c[7];
-                double l2 = m.l0 * c[2] + m.l1 * c[5] + m.l2 * c[8];
-                eval_point64(pc, acc, l0, l1, l2, (m.w * fr) * areaT);
-            }
+            const double* c = lf < 0 ? b : pc.sh->leaf[lf];
+            double fr = lf < 0 ? frac : pc.sh->leaf[lf][9];
+            RulePt m = R[i];
+            double l0 = m.l0 * c[0] + m.l1 * c[3] + m.l2 * c[6];
+            double l1 = m.l0 * c[1] + m.l1 * c[4] + m.l2 * c[7];
+            double l2 = m.l0 * c[2] + m.l1 * c[5] + m.l2 * c[8];
+            eval_point64(pc, acc, l0, l1, l2, (m.w * fr) * areaT);
         }
         batch_done(pc, acc);
         __syncwarp();
@@ -1133,20 +1019,15 @@ __device__ __forceinline__ void point_step(PairCtx& pc, Acc& acc, bool valid, in
 template <class Acc>
 __device__ __noinline__ void emit_rule(PairCtx& pc, Acc& acc, int rid, const double* b, double frac) {
     const int n = pc.a->nrule[rid];
-    float bf[10], bl[10];
-    for (int z = 0; z < 9; ++z) {
-        bf[z] = float(b[z]);
-        bl[z] = float(b[z] - double(bf[z]));
-    }
-    const double fa = frac * pc.T->area;
-    bf[9] = float(fa);
-    bl[9] = float(fa - double(bf[9]));
+    float bf[10];
+    for (int z = 0; z < 9; ++z) bf[z] = float(b[z]);
+    bf[9] = float(frac * pc.T->area);
     for (int i0 = 0; i0 < n; i0 += 32) {
         int i = i0 + pc.lane;
         point_step(pc, acc, i < n, rid, i < n ? i : 0, -1, b, bf, frac);
-        if (pc.nq64 >= 32) drain64(pc, acc, false, rid, b, frac, bf, bl);
+        if (pc.nq64 >= 32) drain64(pc, acc, false, rid, b, frac);
     }
-    drain64(pc, acc, true, rid, b, frac, bf, bl);
+    drain64(pc, acc, true, rid, b, frac);
     pc.npts += n;
     if (!pc.fp32) pc.n64 += n;
 }
@@ -1163,9 +1044,9 @@ __device__ __noinline__ void flush_leaves(PairCtx& pc, Acc& acc) {
         int lf = valid ? i / n : 0, q = valid ? i - lf * n : 0;
         const double* b = pc.sh->leaf[lf];
         point_step(pc, acc, valid, R_NEAR, q, lf, b, pc.sh->leaff[lf], b[9]);
-        if (pc.nq64 >= 32) drain64(pc, acc, false, R_NEAR, nullptr, 0.0, nullptr, nullptr);
+        if (pc.nq64 >= 32) drain64(pc, acc, false, R_NEAR, nullptr, 0.0);
     }
-    drain64(pc, acc, true, R_NEAR, nullptr, 0.0, nullptr, nullptr);
+    drain64(pc, acc, true, R_NEAR, nullptr, 0.0);
     pc.npts += (long long)nl * n;
     if (!pc.fp32) pc.n64 += (long long)nl * n;
     __syncwarp();
@@ -1178,12 +1059,9 @@ __device__ void emit_leaf(PairCtx& pc, Acc& acc, const double* b, double frac) {
         for (int k = 0; k < 9; ++k) {
             pc.sh->leaf[pc.nleaf][k] = b[k];
             pc.sh->leaff[pc.nleaf][k] = float(b[k]);
-            pc.sh->leafl[pc.nleaf][k] = float(b[k] - double(pc.sh->leaff[pc.nleaf][k]));
         }
         pc.sh->leaf[pc.nleaf][9] = frac;
-        const double fa = frac * pc.T->area;
-        pc.sh->leaff[pc.nleaf][9] = float(fa);
-        pc.sh->leafl[pc.nleaf][9] = float(fa - double(pc.sh->leaff[pc.nleaf][9]));
+        pc.sh->leaff[pc.nleaf][9] = float(frac * pc.T->area);
     }
     pc.nleaf++;
     if (pc.nleaf == LEAFBUF) flush_leaves(pc, acc);
@@ -1637,19 +1515,6 @@ __device__ void setup_tri_source(PairCtx& pc, const TriGeo& S) {
         sh.Sdiam = S.diam;
         sh.Sareaf = float(S.area);
         sh.Sdiamf = float(S.diam);
-        auto lo = [](double v, float h) { return float(v - double(h)); };
-        for (int k = 0; k < 27; ++k) sh.Elo[k] = lo(sh.E[k], sh.E32[k]);
-        for (int k = 0; k < 9; ++k) {
-            sh.Dlo[k] = lo(sh.D[k], sh.D32[k]);
-            sh.Sdl[k] = lo(sh.Sd[k], sh.Sdf[k]);
-            sh.Snul[k] = lo(sh.Snu[k], sh.Snuf[k]);
-        }
-        for (int k = 0; k < 3; ++k) {
-            sh.Snl[k] = lo(sh.Sn[k], sh.Snf[k]);
-            sh.Slenl[k] = lo(sh.Slen[k], sh.Slenf[k]);
-        }
-        sh.Sareal = lo(sh.Sarea, sh.Sareaf);
-        sh.Sdiaml = lo(sh.Sdiam, sh.Sdiamf);
     }
     __syncwarp();
 }
@@ -2112,7 +1977,6 @@ struct PairSetup {
     int* d_fil = nullptr;
     RulePt* d_rule[5] = {};
     float4* d_rulef[5] = {};
-    float4* d_rulel[5] = {};
     std::vector<long long> nfptr, wfptr;
     long long *d_nfptr = nullptr, *d_wfptr = nullptr;
     int *d_nf = nullptr, *d_wf = nullptr;
@@ -2233,16 +2097,10 @@ int setup_pairs(vp_ctx* ctx, const PairInput& in, int ph_setup, int ph_classify,
     {
         const std::vector<RulePt>* R[5] = {&ps.rnear, &ps.rself, &ps.redge, &ps.rvert, &ps.rfar};
         for (int k = 0; k < 5; ++k) {
-            std::vector<float4> f(R[k]->size()), fl(R[k]->size());
-            for (size_t i = 0; i < f.size(); ++i) {
-                const RulePt& q = (*R[k])[i];
-                f[i] = make_float4(float(q.l0), float(q.l1), float(q.l2), float(q.w));
-                fl[i] = make_float4(float(q.l0 - double(f[i].x)), float(q.l1 - double(f[i].y)),
-                                    float(q.l2 - double(f[i].z)), float(q.w - double(f[i].w)));
-            }
-            if ((r = dl.up(ctx, &ps.d_rule[k], *R[k])) || (r = dl.up(ctx, &ps.d_rulef[k], f)) ||
-                (r = dl.up(ctx, &ps.d_rulel[k], fl)))
-                return r;
+            std::vector<float4> f(R[k]->size());
+            for (size_t i = 0; i < f.size(); ++i)
+                f[i] = make_float4(float((*R[k])[i].l0), float((*R[k])[i].l1), float((*R[k])[i].l2), float((*R[k])[i].w));
+            if ((r = dl.up(ctx, &ps.d_rule[k], *R[k])) || (r = dl.up(ctx, &ps.d_rulef[k], f))) return r;
         }
     }
     // touching pairs, both orders, sorted keys t * ntri + s
@@ -2408,7 +2266,6 @@ NearArgs near_args(const PairSetup& ps, const PairInput& in) {
     for (int k = 0; k < 5; ++k) {
         na.rule[k] = ps.d_rule[k];
         na.rulef[k] = ps.d_rulef[k];
-        na.rulel[k] = ps.d_rulel[k];
         na.nrule[k] = nr[k];
     }
     na.lda = ps.ncols;

@@ -1099,7 +1099,6 @@ struct vp_freewake {
     int *pwte = nullptr, *pt = nullptr, *pf = nullptr;
     RulePt* rule[5] = {};
     float4* rulef[5] = {};
-    float4* rulel[5] = {};
     int nrule[5] = {};
     // state
     double *rx = nullptr, *rmu = nullptr, *mul = nullptr;
@@ -1216,7 +1215,6 @@ NearArgs wake_near_args(const vp_freewake* fw, const vp_assembly_options& o) {
     for (int k = 0; k < 5; ++k) {
         na.rule[k] = fw->rule[k];
         na.rulef[k] = fw->rulef[k];
-        na.rulel[k] = fw->rulel[k];
         na.nrule[k] = fw->nrule[k];
     }
     na.test_mode = o.test;
@@ -1401,16 +1399,10 @@ extern "C" int vp_freewake_create(vp_ctx* ctx, const vp_freewake_setup* s, vp_fr
     if (s->merge && (r = own_up(fw, &fw->merge, s->merge, size_t(s->nstrip)))) return fail(r);
     for (int k = 0; k < 5; ++k) {
         if (rl[k].empty()) rl[k].push_back(RulePt{1.0 / 3, 1.0 / 3, 1.0 / 3, 0.0});
-        std::vector<float4> f(rl[k].size()), fl(rl[k].size());
-        for (size_t i = 0; i < rl[k].size(); ++i) {
-            const RulePt& q = rl[k][i];
-            f[i] = make_float4(float(q.l0), float(q.l1), float(q.l2), float(q.w));
-            fl[i] = make_float4(float(q.l0 - double(f[i].x)), float(q.l1 - double(f[i].y)),
-                                float(q.l2 - double(f[i].z)), float(q.w - double(f[i].w)));
-        }
-        if ((r = own_up(fw, &fw->rule[k], rl[k].data(), rl[k].size())) ||
-            (r = own_up(fw, &fw->rulef[k], f.data(), f.size())) ||
-            (r = own_up(fw, &fw->rulel[k], fl.data(), fl.size())))
+        std::vector<float4> f(rl[k].size());
+        for (size_t i = 0; i < rl[k].size(); ++i)
+            f[i] = make_float4(float(rl[k][i].l0), float(rl[k][i].l1), float(rl[k][i].l2), float(rl[k][i].w));
+        if ((r = own_up(fw, &fw->rule[k], rl[k].data(), rl[k].size())) || (r = own_up(fw, &fw->rulef[k], f.data(), f.size())))
             return fail(r);
         fw->nrule[k] = int(rl[k].size());
     }
