@@ -103,6 +103,109 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
     return s;
 }
 
+// The mixed path's FP64 points (where FP32 cancels), split by what cancels: the offsets' lengths, the edges' dot and
+// cross products, the stable forms l_i l_j + r_i.r_j, the solid angle's numerator and denominator and the vectors
+// l_k r_j + l_j r_k are formed in FP64 (with KMathHyb's square root), and the functions and the derivative algebra on
+// them run in FP32, where no difference of nearly equal terms is left. The same s, ds/dr_a and shape factors as
+// sv_exact_vjp<double, KMathHyb>, at FP32 accuracy, with about a quarter of its FP64 work.
+__device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3<double> r0, v3<double> r1,
+                                                    v3<double> r2, v3<double> r, v3<float> m, int side, double plane_tol,
+                                                    v3<float>& g0, v3<float>& g1, v3<float>& g2,
+                                                    ExactShape<float>& sh) {
+    const v3<double> R[3] = {r0, r1, r2};
+    double l64[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) l64[a] = KMathHyb::sqrt(dot(R[a], R[a]));
+    float l[3], p[3], s2[3];
+    v3<float> c[3], Rf[3];
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = (e + 1) % 3;
+        const double pe = dot(R[i], R[j]);
+        const v3<double> ce = cross(R[i], R[j]);
+        const double lilj = l64[i] * l64[j];
+        // l_i l_j + p without cancellation: |c|^2 / (l_i l_j - p) where p < 0
+        const double se = pe < 0.0 ? KMathHyb::div(norm2(ce), lilj - pe) : lilj + pe;
+        l[e] = float(l64[e]);
+        p[e] = float(pe);
+        s2[e] = float(se);
+        c[e] = f3(ce);
+        Rf[e] = f3(R[e]);
+    }
+    const double N64 = dot(r0, cross(r1, r2));
+    const double D64 = l64[0] * l64[1] * l64[2] + dot(r0, r1) * l64[2] + dot(r0, r2) * l64[1] + dot(r1, r2) * l64[0];
+    const v3<float> V[3] = {f3(l64[2] * r1 + l64[1] * r2), f3(l64[2] * r0 + l64[0] * r2), f3(l64[1] * r0 + l64[0] * r1)};
+    const double z = dot(r, S.n);
+    const float N = float(N64), D = float(D64);
+    // FP32 from here
+    const float i4pi = 1.f / (4.f * vp_pi<float>());
+    v3<float> gr[3] = {mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f)};
+    float lbar[3] = {0.f, 0.f, 0.f};
+    float sv = 0.f;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = (e + 1) % 3;
+        const float len = float(S.len[e]);
+        const float num = l[i] + l[j] + len;
+        const v3<float> nu = f3(S.nu[e]);
+        const float coef = dot(nu, m) * i4pi;
+        float L, dLdli, dLdlj, dLdp;
+        if (p[e] < 0.f) {
+            const float den = l[i] * l[j] - p[e];
+            const float c2 = norm2(c[e]);
+            L = logf(num * num * (den / (2.f * c2)));
+            dLdli = 2.f / num + l[j] / den;
+            dLdlj = 2.f / num + l[i] / den;
+            dLdp = -1.f / den;
+            const float k2 = coef * (-1.f / c2) * 2.f;
+            gr[i] += k2 * cross(Rf[j], c[e]);
+            gr[j] += k2 * cross(c[e], Rf[i]);
+        } else {
+            const float den = s2[e];
+            L = log1pf(len * num / den);
+            dLdli = 2.f / num - l[j] / den;
+            dLdlj = 2.f / num - l[i] / den;
+            dLdp = -1.f / den;
+        }
+        sv += L * coef;
+        lbar[i] += coef * dLdli;
+        lbar[j] += coef * dLdlj;
+        gr[i] += (coef * dLdp) * Rf[j];
+        gr[j] += (coef * dLdp) * Rf[i];
+        sh.L[e] = L;
+        sh.dLdlen[e] = 2.f / num;
+    }
+    const float nm = dot(f3(S.n), m) * i4pi;
+    if (fabs(z) <= plane_tol * S.diam) {
+        const v3<double> q[3] = {-r0, -r1, -r2};
+        sh.Om = side == 0 ? 0.f
+                          : float(side) * 2.f * vp_pi<float>() *
+                                float(inplane_fraction_rel(q, S.n, S.area, plane_tol));
+    } else {
+        sh.Om = 2.f * atan2f(N, D);
+    }
+    if (N * N + D * D > 0.f) {
+        const float h = 2.f / (N * N + D * D);
+        const float Nb = nm * D * h, Db = -nm * N * h;
+        gr[0] += Nb * c[1];
+        gr[1] += Nb * c[2];
+        gr[2] += Nb * c[0];
+        lbar[0] += Db * s2[1];
+        lbar[1] += Db * s2[2];
+        lbar[2] += Db * s2[0];
+        gr[0] += Db * V[0];
+        gr[1] += Db * V[1];
+        gr[2] += Db * V[2];
+    }
+    sv += sh.Om * nm;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) gr[a] += (lbar[a] / l[a]) * Rf[a];
+    g0 = gr[0];
+    g1 = gr[1];
+    g2 = gr[2];
+    return sv;
+}
+
 // s = w·m of the multipole form (source_triangle.jl:100-119) and its derivatives with respect to r = x - c, to the
 // corner offsets d_a (gd) and the area (ga)
 template <class T>

@@ -26,6 +26,7 @@ template <class T> __host__ __device__ __forceinline__ v3<T> cross(v3<T> a, v3<T
     return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
 }
 template <class T> __host__ __device__ __forceinline__ T norm2(v3<T> a) { return dot(a, a); }
+__host__ __device__ __forceinline__ v3<float> f3(v3<double> v) { return v3<float>{float(v.x), float(v.y), float(v.z)}; }
 
 __device__ __forceinline__ float vsqrt(float a) { return sqrtf(a); }
 __device__ __forceinline__ double vsqrt(double a) { return sqrt(a); }

@@ -834,7 +834,6 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
     return true;
 }
 
-__device__ __forceinline__ v3<float> f3(v3<double> v) { return mk3(float(v.x), float(v.y), float(v.z)); }
 
 // the mixed path's FP64 point (a triangle source's point the FP32 guard refused), warp sums: the kernel and its
 // derivatives in FP64 geometry with the FP32-based functions, added to this lane's FP32 partials
@@ -860,16 +859,19 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAccW& acc, doubl
         const v3<float> gdf[3] = {f3(gd[0]), f3(gd[1]), f3(gd[2])};
         adj_acc_far(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(sv_far(S, r)), f3(gx), gdf, float(ga));
     } else {
-        v3<double> g0, g1, g2;
-        ExactShape<double> shp;
-        sv = sv_exact_vjp<double, KMathHyb>(S, ra, rb, rc, r, pc.m, pc.side, 1e-12, g0, g1, g2, shp);
-        const double i4pi = 1.0 / (4.0 * vp_pi<double>());
-        const v3<double> w = (shp.L[0] * S.nu[0] + shp.L[1] * S.nu[1] + shp.L[2] * S.nu[2] + shp.Om * S.n) * i4pi;
-        gx = g0 + g1 + g2;
-        const float Lf[3] = {float(shp.L[0]), float(shp.L[1]), float(shp.L[2])};
-        const float dLf[3] = {float(shp.dLdlen[0]), float(shp.dLdlen[1]), float(shp.dLdlen[2])};
-        adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(w), f3(gx), f3(g0), f3(g1), f3(g2), Lf, dLf,
-                      float(shp.Om));
+        v3<float> g0, g1, g2;
+        ExactShape<float> shp;
+        const float svf = sv_exact_vjp_split(S, ra, rb, rc, r, pc.mf, pc.side, 1e-12, g0, g1, g2, shp);
+        const float i4pi = 1.f / (4.f * vp_pi<float>());
+        const v3<float> w =
+            (shp.L[0] * f3(S.nu[0]) + shp.L[1] * f3(S.nu[1]) + shp.L[2] * f3(S.nu[2]) + shp.Om * f3(S.n)) * i4pi;
+        const v3<float> gxf = g0 + g1 + g2;
+        adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, w, gxf, g0, g1, g2, shp.L, shp.dLdlen, shp.Om);
+        if (pc.dep)
+            for (int k = 0; k < pc.nadj; ++k)
+                rule_point(pc, pc.nukf[k], pc.binvf, acc.me->Bbf[k], acc.me->Fbf[k], float(W), fl0, fl1, fl2, svf,
+                           gxf, pc.Xcf);
+        return;
     }
     if (pc.dep)
         for (int k = 0; k < pc.nadj; ++k)
