@@ -107,16 +107,19 @@ __device__ __forceinline__ T sv_exact_vjp(const SrcKern<T>& S, v3<T> r0, v3<T> r
 // cross products, the stable forms l_i l_j + r_i.r_j, the solid angle's numerator and denominator and the vectors
 // l_k r_j + l_j r_k are formed in FP64 (with KMathHyb's square root), and the functions and the derivative algebra on
 // them run in FP32, where no difference of nearly equal terms is left. The same s, ds/dr_a and shape factors as
-// sv_exact_vjp<double, KMathHyb>, at FP32 accuracy, with about a quarter of its FP64 work.
-__device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3<double> r0, v3<double> r1,
-                                                    v3<double> r2, v3<double> r, v3<float> m, int side, double plane_tol,
-                                                    v3<float>& g0, v3<float>& g1, v3<float>& g2,
-                                                    ExactShape<float>& sh) {
+// sv_exact_vjp<double, KMathHyb>, at FP32 accuracy, with about a quarter of its FP64 work. Returns false, with the
+// outputs unset, for a point so near a corner or an edge's line that the terms leave FP32's range (a corner offset
+// under 1e-10, an edge cross product |c|^2 under 1e-30); the caller takes that point wholly in FP64.
+__device__ __forceinline__ bool sv_exact_vjp_split(const SrcKern<double>& S, v3<double> r0, v3<double> r1,
+                                                   v3<double> r2, v3<double> r, v3<float> m, int side, double plane_tol,
+                                                   float& svo, v3<float>& g0, v3<float>& g1, v3<float>& g2,
+                                                   ExactShape<float>& sh) {
     const v3<double> R[3] = {r0, r1, r2};
     double l64[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) l64[a] = KMathHyb::sqrt(dot(R[a], R[a]));
-    float l[3], p[3], s2[3];
+    if (!(fmin(l64[0], fmin(l64[1], l64[2])) > 1e-10)) return false;
+    float l[3], p[3], s2[3], c2[3];
     v3<float> c[3], Rf[3];
 #pragma unroll
     for (int e = 0; e < 3; ++e) {
@@ -125,7 +128,10 @@ __device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3
         const v3<double> ce = cross(R[i], R[j]);
         const double lilj = l64[i] * l64[j];
         // l_i l_j + p without cancellation: |c|^2 / (l_i l_j - p) where p < 0
-        const double se = pe < 0.0 ? KMathHyb::div(norm2(ce), lilj - pe) : lilj + pe;
+        const double c2e = norm2(ce);
+        if (pe < 0.0 && !(c2e > 1e-30)) return false;
+        const double se = pe < 0.0 ? KMathHyb::div(c2e, lilj - pe) : lilj + pe;
+        c2[e] = float(c2e);
         l[e] = float(l64[e]);
         p[e] = float(pe);
         s2[e] = float(se);
@@ -137,6 +143,11 @@ __device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3
     const v3<float> V[3] = {f3(l64[2] * r1 + l64[1] * r2), f3(l64[2] * r0 + l64[0] * r2), f3(l64[1] * r0 + l64[0] * r1)};
     const double z = dot(r, S.n);
     const float N = float(N64), D = float(D64);
+    // the solid angle's derivative factors 2 (D, N) / (N^2 + D^2), formed in FP64: the squares of N and D leave
+    // FP32's range where the offsets are small
+    const double nd2 = N64 * N64 + D64 * D64;
+    const double hnd = nd2 > 0.0 ? KMathHyb::div(2.0, nd2) : 0.0;
+    const float hD = float(hnd * D64), hN = float(hnd * N64);
     // FP32 from here
     const float i4pi = 1.f / (4.f * vp_pi<float>());
     v3<float> gr[3] = {mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f), mk3(0.f, 0.f, 0.f)};
@@ -152,12 +163,11 @@ __device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3
         float L, dLdli, dLdlj, dLdp;
         if (p[e] < 0.f) {
             const float den = l[i] * l[j] - p[e];
-            const float c2 = norm2(c[e]);
-            L = logf(num * num * (den / (2.f * c2)));
+            L = logf(num * num * (den / (2.f * c2[e])));
             dLdli = 2.f / num + l[j] / den;
             dLdlj = 2.f / num + l[i] / den;
             dLdp = -1.f / den;
-            const float k2 = coef * (-1.f / c2) * 2.f;
+            const float k2 = coef * (-1.f / c2[e]) * 2.f;
             gr[i] += k2 * cross(Rf[j], c[e]);
             gr[j] += k2 * cross(c[e], Rf[i]);
         } else {
@@ -184,9 +194,8 @@ __device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3
     } else {
         sh.Om = 2.f * atan2f(N, D);
     }
-    if (N * N + D * D > 0.f) {
-        const float h = 2.f / (N * N + D * D);
-        const float Nb = nm * D * h, Db = -nm * N * h;
+    if (nd2 > 0.0) {
+        const float Nb = nm * hD, Db = -nm * hN;
         gr[0] += Nb * c[1];
         gr[1] += Nb * c[2];
         gr[2] += Nb * c[0];
@@ -200,10 +209,14 @@ __device__ __forceinline__ float sv_exact_vjp_split(const SrcKern<double>& S, v3
     sv += sh.Om * nm;
 #pragma unroll
     for (int a = 0; a < 3; ++a) gr[a] += (lbar[a] / l[a]) * Rf[a];
+    if (!(isfinite(sv) && isfinite(gr[0].x + gr[0].y + gr[0].z + gr[1].x + gr[1].y + gr[1].z + gr[2].x + gr[2].y +
+                                   gr[2].z)))
+        return false;
+    svo = sv;
     g0 = gr[0];
     g1 = gr[1];
     g2 = gr[2];
-    return sv;
+    return true;
 }
 
 // s = w·m of the multipole form (source_triangle.jl:100-119) and its derivatives with respect to r = x - c, to the

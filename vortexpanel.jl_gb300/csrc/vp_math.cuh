@@ -162,6 +162,51 @@ __device__ __forceinline__ v3<T> sv_exact3(const SrcKern<T>& S, v3<T> ra, v3<T> 
     return (wt + Om * S.n) * (T(1) / (T(4) * vp_pi<T>()));
 }
 
+// The mixed path's FP64 points of the exact kernel, split by what cancels: the offsets' lengths (KMathHyb's square
+// root), the edges' dot products and squared cross products, and the solid angle's numerator and denominator are
+// formed in FP64; the logs, the atan2 and the sums on them run in FP32, where no difference of nearly equal terms is
+// left (l_i l_j - p with p < 0 and l_i l_j + p with p >= 0 are sums of non-negative terms). The value of
+// sv_exact3<double, KMathHyb> at FP32 accuracy, with about half its FP64 work. Returns false, with w unset, for a
+// point so near a corner or an edge's line that the terms leave FP32's range (a corner offset under 1e-10, an edge
+// cross product |c|^2 under 1e-30); the caller takes that point wholly in FP64.
+__device__ __forceinline__ bool sv_exact3_split(const SrcKern<double>& S, v3<double> ra, v3<double> rb, v3<double> rc,
+                                                v3<double> r, int side, double plane_tol, v3<float>& w) {
+    const v3<double> R[3] = {ra, rb, rc};
+    double l64[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) l64[a] = KMathHyb::sqrt(dot(R[a], R[a]));
+    if (!(fmin(l64[0], fmin(l64[1], l64[2])) > 1e-10)) return false;
+    v3<float> wt = mk3(0.f, 0.f, 0.f);
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = (e + 1) % 3;
+        const double pe = dot(R[i], R[j]);
+        const float li = float(l64[i]), lj = float(l64[j]), p = float(pe), len = float(S.len[e]);
+        const float num = li + lj + len;
+        float L;
+        if (pe < 0.0) {
+            const double c2e = norm2(cross(R[i], R[j]));
+            if (!(c2e > 1e-30)) return false;
+            const float c2 = float(c2e);
+            L = logf(num * num * ((li * lj - p) / (2.f * c2)));
+        } else {
+            L = log1pf(len * num / (li * lj + p));
+        }
+        wt += L * f3(S.nu[e]);
+    }
+    float Om;
+    if (fabs(dot(r, S.n)) <= plane_tol * S.diam) {
+        const v3<double> q[3] = {-ra, -rb, -rc};
+        Om = side == 0 ? 0.f : float(side) * 2.f * vp_pi<float>() * float(inplane_fraction_rel(q, S.n, S.area, plane_tol));
+    } else {
+        const double N = dot(ra, cross(rb, rc));
+        const double D = l64[0] * l64[1] * l64[2] + dot(ra, rb) * l64[2] + dot(ra, rc) * l64[1] + dot(rb, rc) * l64[0];
+        Om = 2.f * atan2f(float(N), float(D));
+    }
+    w = (wt + Om * f3(S.n)) * (1.f / (4.f * vp_pi<float>()));
+    return isfinite(w.x + w.y + w.z);
+}
+
 // The exact kernel in FP32 where FP32 is accurate, for a point off the source's singular set: returns false (and
 // leaves w unset) when the point is near a corner, next to an edge segment (the offsets to its ends nearly
 // antiparallel), or near the plane over the triangle (the branch of the solid angle), where the log/atan forms

@@ -529,10 +529,18 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double
         S.area = sh.Sarea;
         S.diam = sh.Sdiam;
         double fd = pc.a->kernel_far * S.diam;
-        // the mixed path's FP64 points (where FP32 cancels): FP64 geometry, FP32-based functions (KMathHyb)
-        v3<double> w = dot(r, r) > fd * fd ? sv_far(S, r)
-                       : pc.fp32            ? sv_exact3<double, KMathHyb>(S, ra, rb, rc, r, pc.side, 1e-12)
-                                            : sv_exact3(S, ra, rb, rc, r, pc.side, 1e-12);
+        // the mixed path's FP64 points (where FP32 cancels): what cancels in FP64, the functions on it in FP32
+        // (sv_exact3_split), or FP64 geometry with FP32-based functions (KMathHyb) where the split leaves FP32's range
+        v3<double> w;
+        v3<float> wf;
+        if (dot(r, r) > fd * fd)
+            w = sv_far(S, r);
+        else if (!pc.fp32)
+            w = sv_exact3(S, ra, rb, rc, r, pc.side, 1e-12);
+        else if (sv_exact3_split(S, ra, rb, rc, r, pc.side, 1e-12, wf))
+            w = mk3(double(wf.x), double(wf.y), double(wf.z));
+        else
+            w = sv_exact3<double, KMathHyb>(S, ra, rb, rc, r, pc.side, 1e-12);
         acc.P[0] += (W * psi.x) * w;
         acc.P[1] += (W * psi.y) * w;
         acc.P[2] += (W * psi.z) * w;
@@ -861,17 +869,30 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAccW& acc, doubl
     } else {
         v3<float> g0, g1, g2;
         ExactShape<float> shp;
-        const float svf = sv_exact_vjp_split(S, ra, rb, rc, r, pc.mf, pc.side, 1e-12, g0, g1, g2, shp);
-        const float i4pi = 1.f / (4.f * vp_pi<float>());
-        const v3<float> w =
-            (shp.L[0] * f3(S.nu[0]) + shp.L[1] * f3(S.nu[1]) + shp.L[2] * f3(S.nu[2]) + shp.Om * f3(S.n)) * i4pi;
-        const v3<float> gxf = g0 + g1 + g2;
-        adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, w, gxf, g0, g1, g2, shp.L, shp.dLdlen, shp.Om);
-        if (pc.dep)
-            for (int k = 0; k < pc.nadj; ++k)
-                rule_point(pc, pc.nukf[k], pc.binvf, acc.me->Bbf[k], acc.me->Fbf[k], float(W), fl0, fl1, fl2, svf,
-                           gxf, pc.Xcf);
-        return;
+        float svf;
+        if (sv_exact_vjp_split(S, ra, rb, rc, r, pc.mf, pc.side, 1e-12, svf, g0, g1, g2, shp)) {
+            const float i4pi = 1.f / (4.f * vp_pi<float>());
+            const v3<float> w =
+                (shp.L[0] * f3(S.nu[0]) + shp.L[1] * f3(S.nu[1]) + shp.L[2] * f3(S.nu[2]) + shp.Om * f3(S.n)) * i4pi;
+            const v3<float> gxf = g0 + g1 + g2;
+            adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, w, gxf, g0, g1, g2, shp.L, shp.dLdlen, shp.Om);
+            if (pc.dep)
+                for (int k = 0; k < pc.nadj; ++k)
+                    rule_point(pc, pc.nukf[k], pc.binvf, acc.me->Bbf[k], acc.me->Fbf[k], float(W), fl0, fl1, fl2,
+                               svf, gxf, pc.Xcf);
+            return;
+        }
+        // offsets outside FP32's range: all in FP64
+        v3<double> h0, h1, h2;
+        ExactShape<double> shd;
+        sv = sv_exact_vjp<double, KMathHyb>(S, ra, rb, rc, r, pc.m, pc.side, 1e-12, h0, h1, h2, shd);
+        const double i4pi = 1.0 / (4.0 * vp_pi<double>());
+        const v3<double> w = (shd.L[0] * S.nu[0] + shd.L[1] * S.nu[1] + shd.L[2] * S.nu[2] + shd.Om * S.n) * i4pi;
+        gx = h0 + h1 + h2;
+        const float Lf[3] = {float(shd.L[0]), float(shd.L[1]), float(shd.L[2])};
+        const float dLf[3] = {float(shd.dLdlen[0]), float(shd.dLdlen[1]), float(shd.dLdlen[2])};
+        adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(w), f3(gx), f3(h0), f3(h1), f3(h2), Lf, dLf,
+                      float(shd.Om));
     }
     if (pc.dep)
         for (int k = 0; k < pc.nadj; ++k)
