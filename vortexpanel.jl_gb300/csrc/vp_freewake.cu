@@ -17,14 +17,14 @@ int vp_assemble_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const
 
 namespace {
 
-// the particles' part of explicit_rhs: one warp per test triangle, the lanes over the particles (particle_rows). Rows
-// are added with atomics (a slot's rows come from several test triangles).
+// the particles' part of explicit_rhs: one warp per test triangle, the lanes over the particles (particle_rows). Each
+// triangle writes its three rows; a slot's rows (from several test triangles) are summed afterwards in triangle order.
 struct BlobRhsArgs {
     const TriGeo* tri;
     int ntri, nblob;
     const double* blobs;  // x (3), alpha (3), delta
     ParticleRule pr;
-    double* rhs;
+    double* trow;         // ntri x 3
 };
 
 template <class T>
@@ -35,8 +35,8 @@ __global__ void __launch_bounds__(128) blob_rhs_kernel(BlobRhsArgs a) {
     double rows[3] = {0, 0, 0};
     for (int k = lane; k < a.nblob; k += 32) particle_rows<T>(a.pr, Tr, a.blobs + 7 * size_t(k), rows);
     for (int k = 0; k < 3; ++k) {
-        double v = warp_sum(rows[k]);
-        if (lane == k && v != 0.0) atomicAdd(a.rhs + Tr.slot[k], v);
+        const double v = warp_sum(rows[k]);
+        if (lane == k) a.trow[3 * size_t(w) + k] = v;
     }
 }
 
@@ -186,9 +186,9 @@ extern "C" int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* o, int nn
         std::vector<double> hb(blobs, blobs + 7 * size_t(nblob));
         TriGeo* d_tg;
         RulePt *d_rf, *d_rn;
-        double* d_b;
+        double *d_b, *d_trow;
         if ((r = dl.up(ctx, &d_tg, tg)) || (r = dl.up(ctx, &d_rf, rfar)) || (r = dl.up(ctx, &d_rn, rnear)) ||
-            (r = dl.up(ctx, &d_b, hb)))
+            (r = dl.up(ctx, &d_b, hb)) || (r = dl.alloc(ctx, &d_trow, 3 * size_t(ntri))))
             return r;
         BlobRhsArgs a{};
         a.tri = d_tg;
@@ -203,7 +203,7 @@ extern "C" int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* o, int nn
         a.pr.near_depth = o->near_depth;
         a.pr.far_ratio = o->far_ratio;
         a.pr.near_ratio = o->near_ratio;
-        a.rhs = d_rhs;
+        a.trow = d_trow;
         const int nb = (ntri * 32 + 127) / 128;
         if (o->precision == VP_FP64)
             blob_rhs_kernel<double><<<nb, 128, 0, ctx->stream>>>(a);
@@ -211,6 +211,13 @@ extern "C" int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* o, int nn
             blob_rhs_kernel<float><<<nb, 128, 0, ctx->stream>>>(a);
         ctx->launches++;
         VP_CUDA(ctx, cudaGetLastError());
+        std::vector<double> trow(3 * size_t(ntri));
+        VP_CUDA(ctx, vp_d2h(ctx, trow.data(), d_trow, sizeof(double) * 3 * ntri));
+        VP_CUDA(ctx, vp_d2h(ctx, rhs, d_rhs, sizeof(double) * nslot));
+        VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int t = 0; t < ntri; ++t)
+            for (int k = 0; k < 3; ++k) rhs[corner_slot[3 * t + k]] += trow[3 * size_t(t) + k];
+        return VP_OK;
     }
     VP_CUDA(ctx, vp_d2h(ctx, rhs, d_rhs, sizeof(double) * nslot));
     VP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));

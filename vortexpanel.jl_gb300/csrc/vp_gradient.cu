@@ -13,12 +13,14 @@
 //     a last kernel turns into derivatives with respect to the source's corners once per source.
 // Kernels (one CUDA stream):
 //   1. far tier: one CTA per (128-source tile, chunk of test tiles), one thread per source keeping its sums in
-//      registers across the chunk; test-side sums reduced over the CTA per test and added with FP64 atomics;
+//      registers across the chunk; test-side sums reduced over the CTA per test and added to fixed-point
+//      accumulators (vp_fixed.cuh), whose totals do not depend on the order of the additions;
 //   2. non-far pairs: one warp per test triangle, every pair's rule built and walked as in the assembly (the same
 //      templates with the adjoint accumulator), per-pair warp sums, test side in registers, source side added to SA;
 //      the tip filaments and the freestream term;
 //   3. finish: one thread per triangle turns TA and SA into node derivatives.
 #include "vp_pairs.cuh"
+#include "vp_fixed.cuh"
 
 namespace {
 
@@ -41,7 +43,9 @@ __device__ __forceinline__ void sa_flat(const SrcAdj<T>& s, T* f) {
     f[40] = s.Sb;
 }
 
-__device__ __forceinline__ SrcAdj<double> sa_unflat(const double* f) {
+__device__ __forceinline__ SrcAdj<double> sa_unflat(const vp_fx* x) {
+    double f[NSA];
+    for (int k = 0; k < NSA; ++k) f[k] = fx_get(x[k]);
     SrcAdj<double> s;
     for (int k = 0; k < 3; ++k) {
         s.Gr[k] = mk3(f[3 * k], f[3 * k + 1], f[3 * k + 2]);
@@ -75,8 +79,8 @@ struct AdjFarArgs {
     int pad[2];
     const CentF* scent[2];
     const TriGeo* sgeo[2];
-    double* SA[ADJ_MAX][2];
-    double* TA[ADJ_MAX];
+    vp_fx* SA[ADJ_MAX][2];
+    vp_fx* TA[ADJ_MAX];
     float ratio32;
     double ratio, kernel_far;
 };
@@ -264,7 +268,7 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
             if (ts[i].t < 0) continue;
             T v = T(0);
             for (int w = 0; w < FAR_NT / 32; ++w) v += red[i][w][jf];
-            if (v != T(0)) atomicAdd(a.TA[j] + size_t(ts[i].t) * NTA + f, double(v));
+            if (v != T(0)) fx_add(a.TA[j] + size_t(ts[i].t) * NTA + f, double(v));
         }
     }
     if (sv) {
@@ -272,10 +276,10 @@ __global__ void __launch_bounds__(FAR_NT) adj_far_kernel(AdjFarArgs a) {
         for (int j = 0; j < K; ++j) {
             T f[NSA];
             sa_flat(acc[j], f);
-            double* dst = a.SA[j][set] + size_t(s) * NSA;
+            vp_fx* dst = a.SA[j][set] + size_t(s) * NSA;
 #pragma unroll
             for (int k = 0; k < NSA; ++k)
-                if (f[k] != T(0)) atomicAdd(dst + k, double(f[k]));
+                if (f[k] != T(0)) fx_add(dst + k, double(f[k]));
         }
     }
 }
@@ -286,11 +290,12 @@ struct AdjExtra {
     const double* gam_b;  // Gamma_S of the body triangles (3 each)
     const double* gam_w;  // and of the wake triangles
     double V[3], dV[3];
-    double* SA[2];
-    double* TA;
-    double* gx;           // body node derivatives (3 each)
-    double* gwx;          // wake node derivatives (3 each)
-    double* dal;
+    // the sums, in order-independent fixed point (vp_fixed.cuh): the gradients are the same from run to run
+    vp_fx* SA[2];
+    vp_fx* TA;
+    vp_fx* gx;            // body node derivatives (3 each)
+    vp_fx* gwx;           // wake node derivatives (3 each)
+    vp_fx* dal;
 };
 
 // ------------------------------------------------------------------------------------------------------------------
@@ -572,9 +577,8 @@ __device__ unsigned adj_chunk(PairCtx& pc, AdjChunkSh& ns, const AdjMulti& mx, i
             const SrcAdj<double> sa = src_of_pair(xS, d, m, nT);
             double g[NSA];
             sa_flat(sa, g);
-            double* dst = mx.x[j].SA[wake ? 1 : 0] + size_t(s) * NSA;
-            for (int z = 0; z < NSA; ++z)
-                if (g[z] != 0.0) atomicAdd(dst + z, g[z]);
+            vp_fx* dst = mx.x[j].SA[wake ? 1 : 0] + size_t(s) * NSA;
+            for (int z = 0; z < NSA; ++z) fx_add(dst + z, g[z]);
         }
     }
     __syncwarp();
@@ -635,7 +639,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_lanes_kernel(NearArgs a, 
 #pragma unroll
         for (int k = 0; k < NTA; ++k)
             if (k == lane) mine = v[k];
-        if (lane < NTA && mine != 0.0) atomicAdd(mx.x[j].TA + size_t(t) * NTA + lane, mine);
+        if (lane < NTA) fx_add(mx.x[j].TA + size_t(t) * NTA + lane, mine);
     }
     for (int k = 0; k < 6; ++k) {
         unsigned long long pk = P[k], qk = Q[k];
@@ -657,10 +661,10 @@ __device__ __forceinline__ void flush_gdir(PairCtx& pc, const AdjMulti& mx, cons
         const AdjExtra& x = mx.x[k];
         if (d < 18 && pc.gdir[k] != 0.0) {
             if (d < 9)
-                atomicAdd(x.gx + 3 * T.node[d / 3] + d % 3, pc.gdir[k]);
+                fx_add(x.gx + 3 * T.node[d / 3] + d % 3, pc.gdir[k]);
             else if (S)
-                atomicAdd((wake ? x.gwx + 3 * S->slot[(d - 9) / 3] : x.gx + 3 * S->node[(d - 9) / 3]) + (d - 9) % 3,
-                          pc.gdir[k]);
+                fx_add((wake ? x.gwx + 3 * S->slot[(d - 9) / 3] : x.gx + 3 * S->node[(d - 9) / 3]) + (d - 9) % 3,
+                       pc.gdir[k]);
         }
         pc.gdir[k] = 0;
     }
@@ -769,12 +773,12 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, 
 #pragma unroll
             for (int k = 0; k < NTA; ++k)
                 if (k == lane) tmine = v[k];
-            if (lane < NTA && tmine != 0.0) atomicAdd(mx.x[j].TA + size_t(t) * NTA + lane, tmine);
+            if (lane < NTA) fx_add(mx.x[j].TA + size_t(t) * NTA + lane, tmine);
             // the source side: lane k adds field k
             SrcAdj<double> sa = src_of_pair(xS, d, pc.m, nT);
             double f[NSA];
             sa_flat(sa, f);
-            double* dst = mx.x[j].SA[set] + size_t(s) * NSA;
+            vp_fx* dst = mx.x[j].SA[set] + size_t(s) * NSA;
             double mine = 0, mine2 = 0;
 #pragma unroll
             for (int k = 0; k < 32; ++k)
@@ -782,8 +786,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_pairs_kernel(NearArgs a, 
 #pragma unroll
             for (int k = 32; k < NSA; ++k)
                 if (k - 32 == lane) mine2 = f[k];
-            if (mine != 0.0) atomicAdd(dst + lane, mine);
-            if (lane < NSA - 32 && mine2 != 0.0) atomicAdd(dst + 32 + lane, mine2);
+            fx_add(dst + lane, mine);
+            if (lane < NSA - 32) fx_add(dst + 32 + lane, mine2);
         }
         __syncwarp();
         P[tier] += 1;
@@ -839,13 +843,13 @@ __device__ void far_filament_adj(const NearArgs& a, const AdjMulti& mx, const Pa
     for (int j = 0; j < mx.nadj; ++j) {
         U[j] += Qs[j];
         fs[j] += dot(Qs[j], n);
-        double* g = mx.x[j].gwx;
-        atomicAdd(g + 3 * ia + 0, -Ga[j].x);
-        atomicAdd(g + 3 * ia + 1, -Ga[j].y);
-        atomicAdd(g + 3 * ia + 2, -Ga[j].z);
-        atomicAdd(g + 3 * ib + 0, -Gb[j].x);
-        atomicAdd(g + 3 * ib + 1, -Gb[j].y);
-        atomicAdd(g + 3 * ib + 2, -Gb[j].z);
+        vp_fx* g = mx.x[j].gwx;
+        fx_add(g + 3 * ia + 0, -Ga[j].x);
+        fx_add(g + 3 * ia + 1, -Ga[j].y);
+        fx_add(g + 3 * ia + 2, -Ga[j].z);
+        fx_add(g + 3 * ib + 0, -Gb[j].x);
+        fx_add(g + 3 * ib + 1, -Gb[j].y);
+        fx_add(g + 3 * ib + 2, -Gb[j].z);
     }
 }
 
@@ -958,8 +962,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
                     if (lane < 3) {
                         const double ga[3] = {d.Gr[0].x, d.Gr[0].y, d.Gr[0].z},
                                      gb[3] = {d.Gr[1].x, d.Gr[1].y, d.Gr[1].z};
-                        atomicAdd(mx.x[j].gwx + 3 * ia + lane, -ga[lane]);
-                        atomicAdd(mx.x[j].gwx + 3 * ib + lane, -gb[lane]);
+                        fx_add(mx.x[j].gwx + 3 * ia + lane, -ga[lane]);
+                        fx_add(mx.x[j].gwx + 3 * ib + lane, -gb[lane]);
                     }
                 }
                 __syncwarp();
@@ -989,8 +993,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) adj_near_kernel(NearArgs a, A
 #pragma unroll
         for (int k = 0; k < NTA; ++k)
             if (k == lane) mine = v[k];
-        if (lane < NTA && mine != 0.0) atomicAdd(mx.x[j].TA + size_t(t) * NTA + lane, mine);
-        if (lane == 0) atomicAdd(mx.x[j].dal, dal[j]);
+        if (lane < NTA) fx_add(mx.x[j].TA + size_t(t) * NTA + lane, mine);
+        if (lane == 0) fx_add(mx.x[j].dal, dal[j]);
     }
     if (lane == 0) {
         for (int k = 0; k < 6; ++k) {
@@ -1008,13 +1012,13 @@ struct AdjFinish {
     const TriGeo* tri;
     const TriGeo* wtri;
     int ntri, nwtri, nslot;
-    const double* TA;
-    const double* SA[2];
+    const vp_fx* TA;
+    const vp_fx* SA[2];
     const double* mu;
     double V[3], dV[3];
-    double* gx;   // body node derivatives (3 each)
-    double* gwx;  // wake node derivatives
-    double* dal;
+    vp_fx* gx;   // body node derivatives (3 each)
+    vp_fx* gwx;  // wake node derivatives
+    vp_fx* dal;
 };
 
 __global__ void adj_finish_kernel(AdjFinish f) {
@@ -1027,7 +1031,8 @@ __global__ void adj_finish_kernel(AdjFinish f) {
         v3<double> v[3], gr[3] = {mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0), mk3(0.0, 0.0, 0.0)};
         tri_corners(g, v);
         if (!wake) {
-            const double* ta = f.TA + size_t(s) * NTA;
+            double ta[NTA];
+            for (int k = 0; k < NTA; ++k) ta[k] = fx_get(f.TA[size_t(s) * NTA + k]);
             v3<double> Xg[3] = {mk3(ta[0], ta[1], ta[2]), mk3(ta[3], ta[4], ta[5]), mk3(ta[6], ta[7], ta[8])};
             test_adj_grad(v, Xg, mk3(ta[9], ta[10], ta[11]), ta[12], gr);
         }
@@ -1035,16 +1040,16 @@ __global__ void adj_finish_kernel(AdjFinish f) {
         double mu[3];
         for (int k = 0; k < 3; ++k) mu[k] = f.mu[(wake ? f.nslot : 0) + g.slot[k]];
         src_adj_grad(v, sa, mu, !wake, mk3(f.V[0], f.V[1], f.V[2]), mk3(f.dV[0], f.dV[1], f.dV[2]), gr, &dal);
-        double* dst = wake ? f.gwx : f.gx;
+        vp_fx* dst = wake ? f.gwx : f.gx;
         for (int k = 0; k < 3; ++k) {
             const int node = wake ? g.slot[k] : g.node[k];
-            atomicAdd(dst + 3 * node, gr[k].x);
-            atomicAdd(dst + 3 * node + 1, gr[k].y);
-            atomicAdd(dst + 3 * node + 2, gr[k].z);
+            fx_add(dst + 3 * node, gr[k].x);
+            fx_add(dst + 3 * node + 1, gr[k].y);
+            fx_add(dst + 3 * node + 2, gr[k].z);
         }
     }
     dal = warp_sum(dal);
-    if ((threadIdx.x & 31) == 0 && dal != 0.0) atomicAdd(f.dal, dal);
+    if ((threadIdx.x & 31) == 0) fx_add(f.dal, dal);
 }
 
 template <class T>
@@ -1166,19 +1171,20 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     mx.nadj = nadj;
     for (int k = 0; k < nadj; ++k) {
         AdjExtra& ex = mx.x[k];
-        double *d_nu, *d_SA0, *d_SA1, *d_TA, *d_gx, *d_gwx, *d_dal;
+        double* d_nu;
+        vp_fx *d_SA0, *d_SA1, *d_TA, *d_gx, *d_gwx, *d_dal;
         std::vector<double> hnu(nu + size_t(k) * nslot, nu + size_t(k + 1) * nslot);
         if ((r = dl.up(ctx, &d_nu, hnu)) || (r = dl.alloc(ctx, &d_SA0, size_t(NSA) * ntri)) ||
             (r = dl.alloc(ctx, &d_SA1, size_t(NSA) * std::max(nwtri, 1))) ||
             (r = dl.alloc(ctx, &d_TA, size_t(NTA) * ntri)) || (r = dl.alloc(ctx, &d_gx, size_t(3) * nnode)) ||
             (r = dl.alloc(ctx, &d_gwx, size_t(3) * std::max(nwnode, 1))) || (r = dl.alloc(ctx, &d_dal, 1)))
             return r;
-        VP_CUDA(ctx, cudaMemsetAsync(d_SA0, 0, sizeof(double) * NSA * ntri, ctx->stream));
-        VP_CUDA(ctx, cudaMemsetAsync(d_SA1, 0, sizeof(double) * NSA * std::max(nwtri, 1), ctx->stream));
-        VP_CUDA(ctx, cudaMemsetAsync(d_TA, 0, sizeof(double) * NTA * ntri, ctx->stream));
-        VP_CUDA(ctx, cudaMemsetAsync(d_gx, 0, sizeof(double) * 3 * nnode, ctx->stream));
-        VP_CUDA(ctx, cudaMemsetAsync(d_gwx, 0, sizeof(double) * 3 * std::max(nwnode, 1), ctx->stream));
-        VP_CUDA(ctx, cudaMemsetAsync(d_dal, 0, sizeof(double), ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_SA0, 0, sizeof(vp_fx) * NSA * ntri, ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_SA1, 0, sizeof(vp_fx) * NSA * std::max(nwtri, 1), ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_TA, 0, sizeof(vp_fx) * NTA * ntri, ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_gx, 0, sizeof(vp_fx) * 3 * nnode, ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_gwx, 0, sizeof(vp_fx) * 3 * std::max(nwnode, 1), ctx->stream));
+        VP_CUDA(ctx, cudaMemsetAsync(d_dal, 0, sizeof(vp_fx), ctx->stream));
         ex.nu = d_nu;
         ex.mu = d_mu;
         ex.gam_b = d_gamb;
@@ -1277,16 +1283,21 @@ int vp_adjoint_impl(vp_ctx* ctx, const vp_assembly_options* o, int nnode, const 
     }
     vp_phase_end(ctx);
     unsigned long long hs[13];
+    std::vector<vp_fx> hgx(size_t(nadj) * 3 * nnode), hgw(size_t(nadj) * 3 * std::max(nwnode, 1)), hdal(nadj);
     for (int k = 0; k < nadj; ++k) {
         const AdjExtra& ex = mx.x[k];
-        VP_CUDA(ctx, vp_d2h(ctx, grad_x + size_t(k) * 3 * nnode, ex.gx, sizeof(double) * 3 * nnode));
+        VP_CUDA(ctx, vp_d2h(ctx, hgx.data() + size_t(k) * 3 * nnode, ex.gx, sizeof(vp_fx) * 3 * nnode));
         if (nwnode > 0)
-            VP_CUDA(ctx, vp_d2h(ctx, grad_wx + size_t(k) * 3 * nwnode, ex.gwx, sizeof(double) * 3 * nwnode));
-        VP_CUDA(ctx, vp_d2h(ctx, dalpha + k, ex.dal, sizeof(double)));
+            VP_CUDA(ctx, vp_d2h(ctx, hgw.data() + size_t(k) * 3 * nwnode, ex.gwx, sizeof(vp_fx) * 3 * nwnode));
+        VP_CUDA(ctx, vp_d2h(ctx, hdal.data() + k, ex.dal, sizeof(vp_fx)));
     }
     VP_CUDA(ctx, vp_d2h(ctx, hs, d_stats, sizeof(hs)));
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, std::string("adjoint kernels: ") + cudaGetErrorString(e));
+    for (size_t i = 0; i < size_t(nadj) * 3 * nnode; ++i) grad_x[i] = fx_get(hgx[i]);
+    if (nwnode > 0)
+        for (size_t i = 0; i < size_t(nadj) * 3 * nwnode; ++i) grad_wx[i] = fx_get(hgw[i]);
+    for (int k = 0; k < nadj; ++k) dalpha[k] = fx_get(hdal[k]);
     if (stats) {
         const int nq = ps.nq;
         long long total = (long long)ntri * (ntri + nwtri) + (long long)ntri * nfil;

@@ -510,6 +510,12 @@ __device__ __forceinline__ void fold32(FwdAcc& acc) {
     acc.nf = 0;
 }
 
+// the split evaluation's fallback, out of line (rare): FP64 geometry with the FP32-based functions
+__device__ __noinline__ v3<double> exact64_hyb(const SrcKern<double>& S, v3<double> ra, v3<double> rb, v3<double> rc,
+                                               v3<double> r, int side) {
+    return sv_exact3<double, KMathHyb>(S, ra, rb, rc, r, side, 1e-12);
+}
+
 // evaluate one point (barycentric l on T, weight W) in FP64
 __device__ __noinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double l0, double l1, double l2, double W) {
     const WarpSh& sh = *pc.sh;
@@ -540,7 +546,7 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, FwdAcc& acc, double
         else if (sv_exact3_split(S, ra, rb, rc, r, pc.side, 1e-12, wf))
             w = mk3(double(wf.x), double(wf.y), double(wf.z));
         else
-            w = sv_exact3<double, KMathHyb>(S, ra, rb, rc, r, pc.side, 1e-12);
+            w = exact64_hyb(S, ra, rb, rc, r, pc.side);
         acc.P[0] += (W * psi.x) * w;
         acc.P[1] += (W * psi.y) * w;
         acc.P[2] += (W * psi.z) * w;
@@ -843,6 +849,24 @@ __device__ __noinline__ bool eval_point32(const PairCtx& pc, AdjAcc& acc, float 
 }
 
 
+// the exact kernel and its derivatives wholly in FP64 geometry (KMathHyb), added to this lane's FP32 partials: the
+// split evaluation's fallback, kept out of line so that the common path's code stays small
+__device__ __noinline__ double exact_vjp64_acc(const PairCtx& pc, AdjAccW& acc, const SrcKern<double>& S,
+                                               v3<double> ra, v3<double> rb, v3<double> rc, v3<double> r,
+                                               const float* Wn, float fl0, float fl1, float fl2, v3<double>& gx) {
+    v3<double> h0, h1, h2;
+    ExactShape<double> shd;
+    const double sv = sv_exact_vjp<double, KMathHyb>(S, ra, rb, rc, r, pc.m, pc.side, 1e-12, h0, h1, h2, shd);
+    const double i4pi = 1.0 / (4.0 * vp_pi<double>());
+    const v3<double> w = (shd.L[0] * S.nu[0] + shd.L[1] * S.nu[1] + shd.L[2] * S.nu[2] + shd.Om * S.n) * i4pi;
+    gx = h0 + h1 + h2;
+    const float Lf[3] = {float(shd.L[0]), float(shd.L[1]), float(shd.L[2])};
+    const float dLf[3] = {float(shd.dLdlen[0]), float(shd.dLdlen[1]), float(shd.dLdlen[2])};
+    adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(w), f3(gx), f3(h0), f3(h1), f3(h2), Lf, dLf,
+                  float(shd.Om));
+    return sv;
+}
+
 // the mixed path's FP64 point (a triangle source's point the FP32 guard refused), warp sums: the kernel and its
 // derivatives in FP64 geometry with the FP32-based functions, added to this lane's FP32 partials
 __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAccW& acc, double l0, double l1, double l2, double W) {
@@ -882,17 +906,8 @@ __device__ __noinline__ void eval_point64(const PairCtx& pc, AdjAccW& acc, doubl
                                svf, gxf, pc.Xcf);
             return;
         }
-        // offsets outside FP32's range: all in FP64
-        v3<double> h0, h1, h2;
-        ExactShape<double> shd;
-        sv = sv_exact_vjp<double, KMathHyb>(S, ra, rb, rc, r, pc.m, pc.side, 1e-12, h0, h1, h2, shd);
-        const double i4pi = 1.0 / (4.0 * vp_pi<double>());
-        const v3<double> w = (shd.L[0] * S.nu[0] + shd.L[1] * S.nu[1] + shd.L[2] * S.nu[2] + shd.Om * S.n) * i4pi;
-        gx = h0 + h1 + h2;
-        const float Lf[3] = {float(shd.L[0]), float(shd.L[1]), float(shd.L[2])};
-        const float dLf[3] = {float(shd.dLdlen[0]), float(shd.dLdlen[1]), float(shd.dLdlen[2])};
-        adj_acc_exact(acc.me->f, pc.nadj, Wn, fl0, fl1, fl2, f3(w), f3(gx), f3(h0), f3(h1), f3(h2), Lf, dLf,
-                      float(shd.Om));
+        // offsets outside FP32's range: all in FP64, out of line (rare)
+        sv = exact_vjp64_acc(pc, acc, S, ra, rb, rc, r, Wn, fl0, fl1, fl2, gx);
     }
     if (pc.dep)
         for (int k = 0; k < pc.nadj; ++k)
