@@ -158,7 +158,8 @@ int vp_solve_transposed(vp_ctx* ctx, const vp_factor* F, int nrhs, const double*
  * (grad_wx, nwnode x 3 per vector) and the angle of attack (dalpha, nadj), with sigma = -vinf·n differentiated as such
  * and dvinf = d vinf / d alpha. The quadrature of every pair is the assembly's; the vectors share one evaluation of
  * every point. stats may be NULL. For J(x, q) with M q = r: dJ/dx = dJ/dx|_q - dF/dx with nu = C xi,
- * mu = [C q; W q], xi from vp_solve_transposed with g = dJ/dq. */
+ * mu = [C q; W q], xi from vp_solve_transposed with g = dJ/dq. The outputs are the same bit for bit from call to call
+ * on the same inputs (the sums over pairs are exact integer sums of once-rounded terms, whatever their order). */
 int vp_adjoint(vp_ctx* ctx, const vp_assembly_options* opts, int nnode, const double* x, int ntri, const int* tris,
                const int* corner_slot, int nslot, int ntouch, const int* touch_pairs, const double* sigma,
                const double* vinf, int nwnode, const double* wx, int nwtri, const int* wtris, int nfil, const int* fil,

@@ -1,7 +1,7 @@
 // Host check of the order-independent fixed-point sums (vortexpanel.jl_gb300/csrc/vp_fixed.cuh). Reads a count and
 // that many doubles from stdin, adds them to one accumulator (1) in input order, (2) in several shuffled orders and
-// (3) from several threads at once, each thread adding its share with relaxed atomic fetch-adds on the same words,
-// as the device's atomics do; prints one line per run: the three value words, the flag word and the value read back.
+// (3) from several threads at once, each thread adding its share with relaxed atomic adds on the same words, as the
+// device's atomics do; prints one line per run: the six digit words, the flag word and the value read back.
 #define __host__
 #define __device__
 #include "vp_fixed.cuh"
@@ -12,18 +12,13 @@
 #include <thread>
 #include <vector>
 
-static unsigned long long plain_add(unsigned long long* p, unsigned long long x) {
-    const unsigned long long o = *p;
-    *p = o + x;
-    return o;
-}
+static void plain_add(long long* p, long long x) { *p += x; }
 
-static unsigned long long atomic_add(unsigned long long* p, unsigned long long x) {
-    return __atomic_fetch_add(p, x, __ATOMIC_RELAXED);
-}
+static void atomic_add(long long* p, long long x) { __atomic_fetch_add(p, x, __ATOMIC_RELAXED); }
 
 static void print(const vp_fx& a) {
-    std::printf("%016llx %016llx %016llx %llu %.17g\n", a.w[0], a.w[1], a.w[2], a.w[3], fx_get(a));
+    for (int k = 0; k < 6; ++k) std::printf("%lld ", a.d[k]);
+    std::printf("%llu %.17g\n", a.flag, fx_get(a));
 }
 
 int main() {
