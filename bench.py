@@ -40,9 +40,9 @@ FLOP_FWD_POINT = 248
 FLOP_ADJ_EVAL = 620
 FLOP_ADJ_SUMS = 110
 # DRAM bytes per touching/contact point of the pair-parallel kernels, from ncu captures on the 28 x 14 per side wing
-# (115.3M such points): adj_pairs_kernel 0.048 GB read + 0.835 GB written, near_kernel_pairs 0.011 + 0.187 GB. It is
+# (115.3M such points): adj_pairs_kernel 0.091 GB read + 1.308 GB written, near_kernel_pairs 0.024 + 0.390 GB. It is
 # stack traffic of the walkers' frames and spills, which grows with the points; the algorithmic bytes are a few MB.
-DRAM_PER_TOUCH_POINT = {"adj_pairs": 7.66, "near_pairs": 1.72}
+DRAM_PER_TOUCH_POINT = {"adj_pairs": 12.13, "near_pairs": 3.59}
 NCHORD, NSPAN, ASPECT, ALPHA = 112, 56, 8.0, 5.0
 SIZES = {"wing25k": (112, 56), "medium": (56, 28), "small": (28, 14)}  # panels per side: chordwise, spanwise
 
