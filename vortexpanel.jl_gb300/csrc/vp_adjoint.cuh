@@ -225,8 +225,9 @@ template <class T>
 __device__ __forceinline__ T sv_far_vjp(const SrcKern<T>& S, v3<T> r, v3<T> m, v3<T>& gr, v3<T>* gd, T& ga) {
     const T k = S.area / (T(4) * vp_pi<T>());
     T R2 = dot(r, r);
-    T R = vsqrt(R2);
-    T iR2 = T(1) / R2, iR3 = iR2 / R, iR5 = iR3 * iR2, iR7 = iR5 * iR2, iR9 = iR7 * iR2, iR11 = iR9 * iR2;
+    T iR2, iR3;
+    inv_r23(R2, iR2, iR3);
+    T iR5 = iR3 * iR2, iR7 = iR5 * iR2, iR9 = iR7 * iR2, iR11 = iR9 * iR2;
     T rm = dot(r, m);
     // F·m = iR3 rm + sum_a g_a(dr, dd, rm, dm, R2)
     T Fm = iR3 * rm;

@@ -38,6 +38,20 @@ __device__ __forceinline__ float vacos(float a) { return acosf(a); }
 __device__ __forceinline__ double vacos(double a) { return acos(a); }
 template <class T> __device__ __forceinline__ T vnorm(v3<T> a) { return vsqrt(dot(a, a)); }
 
+// 1/R^2 and 1/R^3 of the multipole forms from R^2. FP32: one reciprocal square root (rsqrtf, a few ulp, far below the
+// multipole's truncation error and FP32's own rounding of the sums) instead of a square root and two IEEE divisions,
+// the far tiers' special-function bound. FP64: the square root and the divisions.
+__device__ __forceinline__ void inv_r23(float R2, float& iR2, float& iR3) {
+    const float iR = rsqrtf(R2);
+    iR2 = iR * iR;
+    iR3 = iR2 * iR;
+}
+__device__ __forceinline__ void inv_r23(double R2, double& iR2, double& iR3) {
+    const double R = sqrt(R2);
+    iR2 = 1.0 / R2;
+    iR3 = iR2 / R;
+}
+
 // The scalar functions of the exact kernel and its derivatives, as a policy of the evaluation.
 // KMath<T>: the plain FP32 or FP64 functions.
 // KMathHyb: the FP64 evaluation of the mixed-precision path, for the points that FP32 cannot take (near a source's
@@ -279,8 +293,9 @@ __device__ __forceinline__ bool sv_exact3_guarded(const SrcKern<float>& S, v3<fl
 template <class T>
 __device__ __forceinline__ v3<T> sv_far(const SrcKern<T>& S, v3<T> r) {
     T R2 = dot(r, r);
-    T R = vsqrt(R2);
-    T iR2 = T(1) / R2, iR3 = iR2 / R, iR5 = iR3 * iR2, iR7 = iR5 * iR2, iR9 = iR7 * iR2;
+    T iR2, iR3;
+    inv_r23(R2, iR2, iR3);
+    T iR5 = iR3 * iR2, iR7 = iR5 * iR2, iR9 = iR7 * iR2;
     v3<T> w = iR3 * r;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
