@@ -125,8 +125,13 @@ extern "C" int vp_explicit_rhs(vp_ctx* ctx, const vp_assembly_options* o, int nn
                                const double* sheet_mu, int nseg, const double* seg_x, const double* seg_gamma,
                                int nblob, const double* blobs, double* rhs) {
     if (!ctx || !o || !x || !tris || !corner_slot || !rhs || nsheet < 0 || nseg < 0 || nblob < 0 ||
-        (nsheet > 0 && (!sheet_x || !sheet_mu)) || (nseg > 0 && (!seg_x || !seg_gamma)) || (nblob > 0 && !blobs))
+        (nsheet > 0 && (!sheet_x || !sheet_mu)) || (nseg > 0 && (!seg_x || !seg_gamma)) || (nblob > 0 && !blobs) ||
+        ntri < 0 || nnode < 0 || nslot < 0)
         return vp_fail(ctx, VP_ERR_ARG, "bad argument");
+    for (size_t k = 0; k < 3 * size_t(ntri); ++k) {
+        if (tris[k] < 0 || tris[k] >= nnode) return vp_fail(ctx, VP_ERR_ARG, "triangle node out of range");
+        if (corner_slot[k] < 0 || corner_slot[k] >= nslot) return vp_fail(ctx, VP_ERR_ARG, "corner slot out of range");
+    }
     if (cudaSetDevice(ctx->device) != cudaSuccess) return vp_fail(ctx, VP_ERR_CUDA, "cudaSetDevice");
     int r;
     DevList dl;
