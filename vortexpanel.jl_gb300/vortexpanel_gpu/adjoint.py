@@ -26,6 +26,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import D, check, load
+from ._vec import cross3, norm3, scatter_add
 from .api import (AssemblyOptions, _dp, _ip, assemble, build_elements, default_context, factorize_galerkin,
                   solve_galerkin, source_strengths)
 
@@ -94,14 +95,14 @@ def cl_pressure(g, dm, mu_slot, V, dV, eL, deL, S):
     forces.jl:11-20). Returns CL, dCL/dmu (slots), dCL/dx at fixed mu (nnode x 3), dCL/dalpha at fixed mu."""
     x, t = g.x, g.tris
     a, b, c = x[t[:, 0]], x[t[:, 1]], x[t[:, 2]]
-    nA = np.cross(b - a, c - a)
-    A2 = np.linalg.norm(nA, axis=1)
+    nA = cross3(b - a, c - a)
+    A2 = norm3(nA)
     n = nA / A2[:, None]
     e = [c - b, a - c, b - a]
     m = np.asarray(mu_slot)[dm.corner_slot]
     G = sum(m[:, k:k + 1] * e[k] for k in range(3))
     i2 = 1.0 / A2 ** 2
-    gmu = np.cross(nA, G) * i2[:, None]
+    gmu = cross3(nA, G) * i2[:, None]
     Vn = n @ V
     u = V - Vn[:, None] * n + gmu
     V2 = V @ V
@@ -114,12 +115,11 @@ def cl_pressure(g, dm, mu_slot, V, dV, eL, deL, S):
     nA_b = -(cp / (2 * S))[:, None] * eL
     u_b = (cp_b * (-2 / V2))[:, None] * u
     n_b = -Vn[:, None] * u_b - np.einsum("ij,ij->i", u_b, n)[:, None] * V
-    G_b = np.cross(u_b, nA) * i2[:, None]
+    G_b = cross3(u_b, nA) * i2[:, None]
     trip = np.einsum("ij,ij->i", u_b, gmu)  # u_b·(nA x G) / |nA|^2
-    nA_b += np.cross(G, u_b) * i2[:, None] - (2 * trip * i2)[:, None] * nA
+    nA_b += cross3(G, u_b) * i2[:, None] - (2 * trip * i2)[:, None] * nA
     m_b = np.stack([np.einsum("ij,ij->i", G_b, e[k]) for k in range(3)], axis=1)
-    dmu = np.zeros(dm.nslot)
-    np.add.at(dmu, dm.corner_slot.ravel(), m_b.ravel())
+    dmu = scatter_add(dm.nslot, dm.corner_slot, m_b.ravel())
     xa_b, xb_b, xc_b = np.zeros_like(a), np.zeros_like(a), np.zeros_like(a)
     # e_0 = c - b, e_1 = a - c, e_2 = b - a
     for k, (p, q) in enumerate(((2, 1), (0, 2), (1, 0))):
@@ -128,13 +128,11 @@ def cl_pressure(g, dm, mu_slot, V, dV, eL, deL, S):
         (xa_b, xb_b, xc_b)[q][:] -= eb
     nA_b += (n_b - np.einsum("ij,ij->i", n_b, n)[:, None] * n) / A2[:, None]
     u1, u2 = b - a, c - a
-    u1_b, u2_b = np.cross(u2, nA_b), np.cross(nA_b, u1)
+    u1_b, u2_b = cross3(u2, nA_b), cross3(nA_b, u1)
     xb_b += u1_b
     xc_b += u2_b
     xa_b -= u1_b + u2_b
-    gx = np.zeros_like(x)
-    for k, xb in enumerate((xa_b, xb_b, xc_b)):
-        np.add.at(gx, t[:, k], xb)
+    gx = scatter_add(len(x), t.T, np.concatenate([xa_b, xb_b, xc_b]))
     # alpha: V and e_L
     V_b = (u_b - np.einsum("ij,ij->i", u_b, n)[:, None] * n).sum(axis=0) + (cp_b * 2 * uu / V2 ** 2).sum() * V
     Fv = -(cp[:, None] * nA).sum(axis=0) / 2

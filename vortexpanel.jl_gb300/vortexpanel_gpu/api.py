@@ -22,6 +22,7 @@ import scipy.sparse as sp
 
 from . import _lib, autotune
 from ._lib import D, I, check, default_context, load
+from ._vec import cross3, norm3
 
 TIER_NAMES = ("self", "edge", "vertex", "contact", "near", "far")
 
@@ -94,14 +95,14 @@ class Elements:
 def build_elements(g) -> Elements:
     x, t = g.x, g.tris
     a, b, c = x[t[:, 0]], x[t[:, 1]], x[t[:, 2]]
-    nA = np.cross(b - a, c - a)
-    A2 = np.linalg.norm(nA, axis=1)
+    nA = cross3(b - a, c - a)
+    A2 = norm3(nA)
     if np.any(~(A2 > 0)):
         raise ValueError(f"degenerate triangle {int(np.argmin(A2))}")
     n = nA / A2[:, None]
     e = [c - b, a - c, b - a]
-    diam = np.maximum.reduce([np.linalg.norm(b - a, axis=1), np.linalg.norm(c - b, axis=1), np.linalg.norm(a - c, axis=1)])
-    return Elements(n, A2 / 2, (a + b + c) / 3, diam, [np.cross(n, ek) / A2[:, None] for ek in e],
+    diam = np.maximum.reduce([norm3(b - a), norm3(c - b), norm3(a - c)])
+    return Elements(n, A2 / 2, (a + b + c) / 3, diam, [cross3(n, ek) / A2[:, None] for ek in e],
                     [-ek / A2[:, None] for ek in e], np.ascontiguousarray(np.concatenate([a, b, c], axis=1)))
 
 
